@@ -1,0 +1,24 @@
+"""GB300 (sm_103a) two-site DMRG path of chemtensor_mojo.
+
+The compute lives in ``libctdmrg.so`` (hand-written CUDA for sm_103a behind a
+plain C ABI, ``include/ctdmrg.h``); this package is the thin host layer that
+mirrors the reference's Mojo API (``src/m_tensor``, ``src/state``,
+``src/algorithms``) on top of it.  There is no CPU fallback: calls fail when
+the library or a CUDA device is missing.
+"""
+from ._lib import CTDMRGError, load as load_library  # noqa: F401
+from .dense_tensor import (DenseTensor, DeviceContext, create_dense_tensor, create_dense_tensor_from_data,  # noqa
+                           create_dense_tensor_random, create_dense_tensor_uninitialized, dense_tensor_dot,
+                           dense_tensor_svd_trunc, get_context)
+from .mps_state import (MatrixProductOperator, MatrixProductState, MPOSite, MPSSite, create_product_mps,  # noqa
+                        create_random_mps_c_compatible, create_uniform_mps, mpo_from_arrays, mps_from_arrays,
+                        mps_norm, mps_right_normalize, mps_to_statevector, random_mps_c_compatible_arrays)
+from .hamiltonians import (create_bose_hubbard_mpo, create_fermi_hubbard_mpo, create_heisenberg_mpo,  # noqa
+                           create_heisenberg_xxz_mpo, create_ising_1d_mpo, create_spin_half_xxz_mpo,
+                           create_transverse_ising_mpo)
+from .environments import (build_right_environments, expectation_value, expectation_value_normalized,  # noqa
+                           update_left_environment, update_right_environment)
+from .dmrg import (DMRGParams, DMRGStats, DMRGWorkspace, apply_two_site_heff, build_two_site_theta,  # noqa
+                   dmrg_local_update_two_site, dmrg_two_site, lanczos_two_site_optimize, split_two_site_theta_svd)
+
+__version__ = "0.1.0"

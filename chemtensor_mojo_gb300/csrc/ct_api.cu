@@ -1,0 +1,483 @@
+// C ABI of libctdmrg (include/ctdmrg.h): handle lifecycle, scratch arena,
+// argument validation, and the entry points that replace the reference's
+// DenseTensor / environment / DMRG functions on the two-site DMRG path.
+#include <stdarg.h>
+#include <math.h>
+#include <chrono>
+#include <algorithm>
+
+#include "ct_ops.cuh"
+
+// ---------------------------------------------------------------------------
+// errors, handle, arena
+// ---------------------------------------------------------------------------
+void ct_seterr(ct_handle* h, const char* fmt, ...) {
+    if (!h) return;
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    h->err = buf;
+}
+
+int ct_reserve(ct_handle* h, size_t bytes) {
+    if (bytes <= h->ws_cap) return CT_OK;
+    size_t want = bytes + bytes / 4 + (1u << 20);
+    if (h->ws_limit && want > h->ws_limit) want = bytes;
+    if (h->ws_limit && want > h->ws_limit) {
+        ct_seterr(h, "workspace of %zu bytes exceeds the limit of %zu bytes", bytes, h->ws_limit);
+        return CT_ERR_OOM;
+    }
+    if (h->ws) {
+        CT_CUDA(h, cudaStreamSynchronize(h->stream));
+        CT_CUDA(h, cudaFree(h->ws));
+        h->ws = nullptr;
+        h->ws_cap = 0;
+    }
+    cudaError_t e = cudaMalloc((void**)&h->ws, want);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        h->ws = nullptr;
+        ct_seterr(h, "cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
+        return CT_ERR_OOM;
+    }
+    h->ws_cap = want;
+    return CT_OK;
+}
+
+static int check_status(ct_handle* h) {
+    int st = 0;
+    CT_CUDA(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CT_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (st != 0) {
+        CT_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
+        if (h->err.empty()) ct_seterr(h, "device status %d", st);
+        return st;
+    }
+    return CT_OK;
+}
+
+#define CT_NULLCHK(h, p)                                                   \
+    do {                                                                   \
+        if (!(p)) {                                                        \
+            ct_seterr((h), "%s: null pointer argument '%s'", __func__, #p); \
+            return CT_ERR_INVALID;                                         \
+        }                                                                  \
+    } while (0)
+
+#define CT_POSCHK(h, v)                                                          \
+    do {                                                                         \
+        if ((v) <= 0) {                                                          \
+            ct_seterr((h), "%s: dimension %s=%lld must be > 0", __func__, #v, (long long)(v)); \
+            return CT_ERR_SHAPE;                                                 \
+        }                                                                        \
+    } while (0)
+
+static int check_prec(ct_handle* h, int prec) {
+    if (prec == CT_PREC_FP64) return CT_OK;
+    if (prec == CT_PREC_TF32X3) {
+        if (ct_tc_available(h)) return CT_OK;
+        ct_seterr(h, "TF32x3 tensor-core path needs an sm_103 device");
+        return CT_ERR_UNSUPPORTED;
+    }
+    ct_seterr(h, "unknown precision %d", prec);
+    return CT_ERR_INVALID;
+}
+
+extern "C" {
+
+int ct_version(void) { return CTDMRG_VERSION; }
+
+const char* ct_error_string(int s) {
+    switch (s) {
+        case CT_OK: return "ok";
+        case CT_ERR_INVALID: return "invalid argument";
+        case CT_ERR_CUDA: return "CUDA error";
+        case CT_ERR_OOM: return "out of device memory";
+        case CT_ERR_NOCONV: return "iterative solver did not converge";
+        case CT_ERR_ZERO_NORM: return "initial vector has zero norm";
+        case CT_ERR_SHAPE: return "shape mismatch";
+        case CT_ERR_UNSUPPORTED: return "unsupported";
+        case CT_ERR_NONFINITE: return "non-finite value";
+        case CT_ERR_EMPTY: return "truncation kept no singular values";
+        default: return "unknown status";
+    }
+}
+
+const char* ct_last_error(ct_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int ct_create(int device, void* stream, ct_handle** out) {
+    if (!out) return CT_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        (void)cudaGetLastError();
+        return CT_ERR_CUDA;
+    }
+    if (device < 0 || device >= ndev) return CT_ERR_INVALID;
+    ct_handle* h = new ct_handle();
+    h->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        delete h;
+        return CT_ERR_CUDA;
+    }
+    cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (stream) {
+        h->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete h;
+            return CT_ERR_CUDA;
+        }
+        h->own_stream = true;
+    }
+    bool ok = cudaMalloc((void**)&h->d_status, sizeof(int)) == cudaSuccess &&
+              cudaMalloc((void**)&h->d_scalars, CT_NSCALARS * sizeof(double)) == cudaSuccess &&
+              cudaMalloc((void**)&h->d_partials, CT_NPARTIALS * sizeof(double)) == cudaSuccess &&
+              cudaMalloc((void**)&h->d_flags, CT_NFLAGS * sizeof(int)) == cudaSuccess;
+    if (ok) ok = cudaMemset(h->d_status, 0, sizeof(int)) == cudaSuccess &&
+                 cudaMemset(h->d_flags, 0, CT_NFLAGS * sizeof(int)) == cudaSuccess &&
+                 cudaMemset(h->d_scalars, 0, CT_NSCALARS * sizeof(double)) == cudaSuccess;
+    if (!ok) {
+        ct_destroy(h);
+        return CT_ERR_OOM;
+    }
+    *out = h;
+    return CT_OK;
+}
+
+int ct_destroy(ct_handle* h) {
+    if (!h) return CT_ERR_INVALID;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaFree(h->ws);
+    cudaFree(h->d_status);
+    cudaFree(h->d_scalars);
+    cudaFree(h->d_partials);
+    cudaFree(h->d_flags);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return CT_OK;
+}
+
+int ct_set_stream(ct_handle* h, void* stream) {
+    CT_NULLCHK(h, h);
+    if (h->own_stream && h->stream) {
+        cudaStreamSynchronize(h->stream);
+        cudaStreamDestroy(h->stream);
+        h->own_stream = false;
+    }
+    if (stream) {
+        h->stream = (cudaStream_t)stream;
+    } else {
+        CT_CUDA(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        h->own_stream = true;
+    }
+    return CT_OK;
+}
+
+int ct_synchronize(ct_handle* h) {
+    CT_NULLCHK(h, h);
+    CT_CUDA(h, cudaStreamSynchronize(h->stream));
+    return CT_OK;
+}
+
+int ct_get_status(ct_handle* h, int* status_out) {
+    CT_NULLCHK(h, h);
+    CT_NULLCHK(h, status_out);
+    int st = 0;
+    CT_CUDA(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CT_CUDA(h, cudaStreamSynchronize(h->stream));
+    CT_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
+    *status_out = st;
+    return CT_OK;
+}
+
+int ct_workspace_bytes(ct_handle* h, int64_t* bytes_out) {
+    CT_NULLCHK(h, h);
+    CT_NULLCHK(h, bytes_out);
+    *bytes_out = (int64_t)h->ws_cap;
+    return CT_OK;
+}
+
+int ct_set_workspace_limit(ct_handle* h, int64_t bytes) {
+    CT_NULLCHK(h, h);
+    if (bytes < 0) return CT_ERR_INVALID;
+    h->ws_limit = (size_t)bytes;
+    return CT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// dense tensor core
+// ---------------------------------------------------------------------------
+int ct_gemm(ct_handle* h, int prec, int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha,
+            const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc) {
+    CT_NULLCHK(h, h);
+    CT_TRY(check_prec(h, prec));
+    if (m < 0 || n < 0 || k < 0) return CT_ERR_SHAPE;
+    if (m == 0 || n == 0) return CT_OK;
+    CT_NULLCHK(h, C);
+    if (k > 0) {
+        CT_NULLCHK(h, A);
+        CT_NULLCHK(h, B);
+    }
+    // row-major op(A)[m,k]: trans_a=0 -> A[i*lda + p], trans_a=1 -> A[p*lda + i]
+    if ((!trans_a && lda < k) || (trans_a && lda < m) || (!trans_b && ldb < n) || (trans_b && ldb < k) || ldc < n) {
+        ct_seterr(h, "ct_gemm: leading dimension too small");
+        return CT_ERR_SHAPE;
+    }
+    if (prec == CT_PREC_TF32X3 && k > 0) {
+        CT_TRY(ct_reserve(h, ct_tc_gemm_ws_bytes(m, n, k)));
+        Arena ar(h);
+        CT_TRY(ct_tc_gemm(h, ar, trans_a, trans_b, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc));
+        return CT_OK;
+    }
+    GemmDesc g{};
+    g.M = m; g.N = n; g.K = k;
+    g.A = A; g.sAm = trans_a ? 1 : lda; g.sAk = trans_a ? lda : 1;
+    g.B = B; g.sBk = trans_b ? 1 : ldb; g.sBn = trans_b ? ldb : 1;
+    g.C = C; g.sCm = ldc; g.sCn = 1;
+    g.alpha = alpha; g.beta = beta; g.nb1 = 1; g.nb0 = 1;
+    return ct_gemm_f64_launch(h, g);
+}
+
+int ct_permute(ct_handle* h, const double* in, double* out, int rank, const int64_t* shape, const int32_t* perm) {
+    CT_NULLCHK(h, h);
+    CT_NULLCHK(h, in);
+    CT_NULLCHK(h, out);
+    CT_NULLCHK(h, shape);
+    CT_NULLCHK(h, perm);
+    for (int i = 0; i < rank; ++i)
+        if (shape[i] < 0) return CT_ERR_SHAPE;
+    return ct_permute_launch(h, in, out, rank, shape, perm);
+}
+
+int ct_vec_dot(ct_handle* h, int64_t n, const double* x, const double* y, double* result_host) {
+    CT_NULLCHK(h, h);
+    CT_NULLCHK(h, result_host);
+    if (n < 0) return CT_ERR_SHAPE;
+    if (n == 0) {
+        *result_host = 0.0;
+        return CT_OK;
+    }
+    CT_NULLCHK(h, x);
+    CT_NULLCHK(h, y);
+    CT_TRY(ct_reduce_dot(h, n, x, y, h->d_scalars + SC_DOT, nullptr));
+    CT_CUDA(h, cudaMemcpyAsync(result_host, h->d_scalars + SC_DOT, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CT_CUDA(h, cudaStreamSynchronize(h->stream));
+    return CT_OK;
+}
+
+int ct_vec_norm_sq(ct_handle* h, int64_t n, const double* x, double* result_host) {
+    CT_NULLCHK(h, h);
+    CT_NULLCHK(h, result_host);
+    if (n < 0) return CT_ERR_SHAPE;
+    if (n == 0) {
+        *result_host = 0.0;
+        return CT_OK;
+    }
+    CT_NULLCHK(h, x);
+    CT_TRY(ct_reduce_nrm2sq(h, n, x, h->d_scalars + SC_DOT, nullptr));
+    CT_CUDA(h, cudaMemcpyAsync(result_host, h->d_scalars + SC_DOT, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CT_CUDA(h, cudaStreamSynchronize(h->stream));
+    return CT_OK;
+}
+
+int ct_vec_axpy(ct_handle* h, int64_t n, double alpha, const double* x, double* y) {
+    CT_NULLCHK(h, h);
+    if (n < 0) return CT_ERR_SHAPE;
+    if (n == 0) return CT_OK;
+    CT_NULLCHK(h, x);
+    CT_NULLCHK(h, y);
+    return ct_vec_axpy_launch(h, n, alpha, x, y);
+}
+
+int ct_vec_scale(ct_handle* h, int64_t n, double alpha, double* x) {
+    CT_NULLCHK(h, h);
+    if (n < 0) return CT_ERR_SHAPE;
+    if (n == 0) return CT_OK;
+    CT_NULLCHK(h, x);
+    return ct_vec_scale_launch(h, n, alpha, x);
+}
+
+int ct_env_identity(ct_handle* h, double* E, int64_t w, int64_t D) {
+    CT_NULLCHK(h, h);
+    CT_NULLCHK(h, E);
+    CT_POSCHK(h, w);
+    CT_POSCHK(h, D);
+    return ct_identity_env(h, E, w, D);
+}
+
+// ---------------------------------------------------------------------------
+// two-site DMRG building blocks
+// ---------------------------------------------------------------------------
+int ct_theta2(ct_handle* h, int prec, const double* A_i, const double* A_ip1, double* theta, int64_t Dl, int64_t d,
+              int64_t Dm, int64_t Dr) {
+    CT_NULLCHK(h, h);
+    CT_TRY(check_prec(h, prec));
+    CT_NULLCHK(h, A_i);
+    CT_NULLCHK(h, A_ip1);
+    CT_NULLCHK(h, theta);
+    CT_POSCHK(h, Dl);
+    CT_POSCHK(h, d);
+    CT_POSCHK(h, Dm);
+    CT_POSCHK(h, Dr);
+    return ct_theta_run(h, prec, A_i, A_ip1, theta, Dl, d, Dm, Dr);
+}
+
+int ct_heff2_apply(ct_handle* h, int prec, const double* theta, const double* L, const double* R, const double* W1,
+                   const double* W2, double* out, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wM,
+                   int64_t wR) {
+    CT_NULLCHK(h, h);
+    CT_TRY(check_prec(h, prec));
+    CT_NULLCHK(h, theta);
+    CT_NULLCHK(h, L);
+    CT_NULLCHK(h, R);
+    CT_NULLCHK(h, W1);
+    CT_NULLCHK(h, W2);
+    CT_NULLCHK(h, out);
+    CT_POSCHK(h, Dl);
+    CT_POSCHK(h, d);
+    CT_POSCHK(h, Dr);
+    CT_POSCHK(h, wL);
+    CT_POSCHK(h, wM);
+    CT_POSCHK(h, wR);
+    CT_TRY(ct_reserve(h, ct_heff_ws_bytes(prec, Dl, d, Dr, wL, wM, wR)));
+    Arena ar(h);
+    HeffPlan p;
+    CT_TRY(ct_heff_prepare(h, ar, p, prec, L, R, W1, W2, Dl, d, Dr, wL, wM, wR));
+    CT_TRY(ct_heff_run(h, p, theta, out, nullptr));
+    return CT_OK;
+}
+
+int ct_env_left(ct_handle* h, int prec, const double* Lprev, const double* A, const double* W, double* Lnext,
+                int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR) {
+    CT_NULLCHK(h, h);
+    CT_TRY(check_prec(h, prec));
+    CT_NULLCHK(h, Lprev);
+    CT_NULLCHK(h, A);
+    CT_NULLCHK(h, W);
+    CT_NULLCHK(h, Lnext);
+    CT_POSCHK(h, Dl);
+    CT_POSCHK(h, d);
+    CT_POSCHK(h, Dr);
+    CT_POSCHK(h, wL);
+    CT_POSCHK(h, wR);
+    CT_TRY(ct_reserve(h, ct_env_ws_bytes(prec, Dl, d, Dr, wL, wR)));
+    Arena ar(h);
+    return ct_env_left_run(h, ar, prec, Lprev, A, W, Lnext, Dl, d, Dr, wL, wR);
+}
+
+int ct_env_right(ct_handle* h, int prec, const double* Rnext, const double* A, const double* W, double* Rprev,
+                 int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR) {
+    CT_NULLCHK(h, h);
+    CT_TRY(check_prec(h, prec));
+    CT_NULLCHK(h, Rnext);
+    CT_NULLCHK(h, A);
+    CT_NULLCHK(h, W);
+    CT_NULLCHK(h, Rprev);
+    CT_POSCHK(h, Dl);
+    CT_POSCHK(h, d);
+    CT_POSCHK(h, Dr);
+    CT_POSCHK(h, wL);
+    CT_POSCHK(h, wR);
+    CT_TRY(ct_reserve(h, ct_env_ws_bytes(prec, Dl, d, Dr, wL, wR)));
+    Arena ar(h);
+    return ct_env_right_run(h, ar, prec, Rnext, A, W, Rprev, Dl, d, Dr, wL, wR);
+}
+
+int ct_lanczos2(ct_handle* h, int prec, const double* theta_in, double* theta_out, const double* L, const double* R,
+                const double* W1, const double* W2, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wM,
+                int64_t wR, int max_iter, double tol, int max_rotations, int reorth, double* energy_host,
+                int* numiter_host, double* alpha_host, double* beta_host) {
+    CT_NULLCHK(h, h);
+    CT_TRY(check_prec(h, prec));
+    CT_NULLCHK(h, theta_in);
+    CT_NULLCHK(h, theta_out);
+    CT_NULLCHK(h, L);
+    CT_NULLCHK(h, R);
+    CT_NULLCHK(h, W1);
+    CT_NULLCHK(h, W2);
+    CT_NULLCHK(h, energy_host);
+    CT_POSCHK(h, Dl);
+    CT_POSCHK(h, d);
+    CT_POSCHK(h, Dr);
+    CT_POSCHK(h, wL);
+    CT_POSCHK(h, wM);
+    CT_POSCHK(h, wR);
+    if (theta_in == theta_out) {
+        ct_seterr(h, "ct_lanczos2: theta_in and theta_out must not alias");
+        return CT_ERR_INVALID;
+    }
+    CT_TRY(ct_reserve(h, ct_lanczos_ws_bytes(prec, Dl, d, Dr, wL, wM, wR, max_iter)));
+    Arena ar(h);
+    LanczosResult res;
+    CT_TRY(ct_lanczos_run(h, ar, prec, theta_in, theta_out, L, R, W1, W2, Dl, d, Dr, wL, wM, wR, max_iter, tol,
+                          max_rotations, reorth, &res));
+    int nk = 0;
+    CT_CUDA(h, cudaMemcpyAsync(energy_host, res.d_energy, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CT_CUDA(h, cudaMemcpyAsync(&nk, res.d_numiter, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    if (alpha_host)
+        CT_CUDA(h, cudaMemcpyAsync(alpha_host, h->d_scalars + SC_ALPHA, max_iter * sizeof(double),
+                                   cudaMemcpyDeviceToHost, h->stream));
+    if (beta_host && max_iter > 1)
+        CT_CUDA(h, cudaMemcpyAsync(beta_host, h->d_scalars + SC_BETA, (max_iter - 1) * sizeof(double),
+                                   cudaMemcpyDeviceToHost, h->stream));
+    CT_TRY(check_status(h));
+    if (numiter_host) *numiter_host = nk;
+    return CT_OK;
+}
+
+int ct_svd_trunc(ct_handle* h, const double* M, int64_t m, int64_t n, int64_t chi_max, double eps_trunc, double* U,
+                 double* S, double* Vt, int64_t* chi_host) {
+    CT_NULLCHK(h, h);
+    CT_NULLCHK(h, chi_host);
+    if (m < 0 || n < 0 || chi_max < 0) return CT_ERR_SHAPE;
+    if (m == 0 || n == 0) {
+        *chi_host = 0;
+        return CT_OK;
+    }
+    CT_NULLCHK(h, M);
+    CT_NULLCHK(h, U);
+    CT_NULLCHK(h, S);
+    CT_NULLCHK(h, Vt);
+    CT_TRY(ct_reserve(h, ct_svd_ws_bytes(m, n, 2)));
+    Arena ar(h);
+    SvdOut o;
+    CT_TRY(ct_svd_run(h, ar, M, m, n, chi_max, eps_trunc, 2, U, Vt, S, &o));
+    CT_TRY(check_status(h));
+    *chi_host = o.chi;
+    return CT_OK;
+}
+
+int ct_svd_split(ct_handle* h, const double* theta, int64_t Dl, int64_t d, int64_t Dr, int64_t chi_max,
+                 double eps_trunc, int left_to_right, double* A_out, double* B_out, double* S_out, int64_t* chi_host,
+                 double* discarded_host) {
+    CT_NULLCHK(h, h);
+    CT_NULLCHK(h, theta);
+    CT_NULLCHK(h, A_out);
+    CT_NULLCHK(h, B_out);
+    CT_NULLCHK(h, chi_host);
+    CT_POSCHK(h, Dl);
+    CT_POSCHK(h, d);
+    CT_POSCHK(h, Dr);
+    if (chi_max < 0) return CT_ERR_SHAPE;
+    const int64_t m = Dl * d, n = d * Dr;
+    const int mode = left_to_right ? 0 : 1;
+    CT_TRY(ct_reserve(h, ct_svd_ws_bytes(m, n, mode)));
+    Arena ar(h);
+    // |theta|^2 in FP64 on the device (dmrg.mojo:176)
+    CT_TRY(ct_reduce_nrm2sq(h, m * n, theta, h->d_scalars + SC_THETA_NSQ, nullptr));
+    double tn = 0.0;
+    CT_CUDA(h, cudaMemcpyAsync(&tn, h->d_scalars + SC_THETA_NSQ, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    SvdOut o;
+    CT_TRY(ct_svd_run(h, ar, theta, m, n, chi_max, eps_trunc, mode, A_out, B_out, S_out, &o));
+    CT_TRY(check_status(h));
+    *chi_host = o.chi;
+    if (discarded_host) *discarded_host = (tn > 0.0) ? (tn - o.sum_s2_kept) / tn : 0.0;
+    return CT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,200 @@
+// Shared definitions of libctdmrg: handle, scratch arena, error plumbing,
+// launch helpers and device-side reduction primitives.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+#include <string>
+#include <vector>
+
+#include "../../include/ctdmrg.h"
+
+// ---------------------------------------------------------------------------
+// handle
+// ---------------------------------------------------------------------------
+struct ct_handle {
+    int device = 0;
+    int num_sms = 152;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int* d_status = nullptr;        // sticky first device error code
+    double* d_scalars = nullptr;    // small device scalars (CT_NSCALARS doubles)
+    double* d_partials = nullptr;   // reduction partials (CT_NPARTIALS doubles)
+    int* d_flags = nullptr;         // small int scratch (CT_NFLAGS ints)
+    // scratch arena: one device allocation, carved per call
+    char* ws = nullptr;
+    size_t ws_cap = 0;
+    size_t ws_limit = 0;            // 0 = unlimited
+    std::string err;
+    // tensor-core path state
+    bool tc_checked = false;
+    bool tc_ok = false;
+};
+
+enum { CT_NSCALARS = 1024, CT_NPARTIALS = 8192, CT_NFLAGS = 256 };
+
+// scalar slots inside d_scalars
+enum {
+    SC_DOT = 0,            // generic reduction result
+    SC_NORM = 1,
+    SC_ENERGY = 2,
+    SC_TMP0 = 3,
+    SC_TMP1 = 4,
+    SC_DISCARD = 5,
+    SC_THETA_NSQ = 6,
+    SC_RITZ = 64,          // Ritz coefficients (<= 128)
+    SC_ALPHA = 256,        // Lanczos alpha (<= 128)
+    SC_BETA = 512,         // Lanczos beta (<= 128)
+    SC_MISC = 768
+};
+// int slots inside d_flags
+enum { FL_STOP = 0, FL_NUMITER = 1, FL_ROT = 2, FL_CHI = 3, FL_TMP = 4, FL_CNT = 8 };
+
+#define CT_MAX_KRYLOV 128
+
+void ct_seterr(ct_handle* h, const char* fmt, ...);
+
+#define CT_CUDA(h, x)                                                                      \
+    do {                                                                                   \
+        cudaError_t e_ = (x);                                                              \
+        if (e_ != cudaSuccess) {                                                           \
+            ct_seterr((h), "%s:%d %s -> %s", __FILE__, __LINE__, #x, cudaGetErrorString(e_)); \
+            return CT_ERR_CUDA;                                                            \
+        }                                                                                  \
+    } while (0)
+
+#define CT_TRY(x)                  \
+    do {                           \
+        int s_ = (x);              \
+        if (s_ != CT_OK) return s_; \
+    } while (0)
+
+#define CT_LAUNCH_CHECK(h) CT_CUDA(h, cudaGetLastError())
+
+static inline int64_t ct_cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+static inline int64_t ct_round_up(int64_t a, int64_t b) { return ct_cdiv(a, b) * b; }
+
+// Scratch arena: reserve() grows (synchronising) before carving; carve() hands
+// out 256-byte aligned pieces in order.  A call's pieces live until the next
+// reserve() of that handle.
+struct Arena {
+    ct_handle* h;
+    size_t off = 0;
+    explicit Arena(ct_handle* hh) : h(hh) {}
+    template <class T>
+    T* take(size_t count) {
+        size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+        if (off + bytes > h->ws_cap) return nullptr;
+        T* p = reinterpret_cast<T*>(h->ws + off);
+        off += bytes;
+        return p;
+    }
+};
+int ct_reserve(ct_handle* h, size_t bytes);
+static inline size_t ct_bytes(size_t count, size_t elem) { return (count * elem + 255) & ~size_t(255); }
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double ct_warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float ct_warp_sumf(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum; every thread gets the result.  sm must hold >= 32 doubles.
+template <int NT>
+__device__ __forceinline__ double ct_block_sum(double v, double* sm) {
+    v = ct_warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sm[wid] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (wid == 0) {
+        r = (lane < NT / 32) ? sm[lane] : 0.0;
+        r = ct_warp_sum(r);
+        if (lane == 0) sm[0] = r;
+    }
+    __syncthreads();
+    r = sm[0];
+    return r;
+}
+
+__device__ __forceinline__ void ct_set_status(int* st, int code) {
+    if (st) atomicCAS(st, 0, code);
+}
+
+// kernels that belong to an early-terminating loop read this flag first
+__device__ __forceinline__ bool ct_skip(const int* skip) { return skip != nullptr && *(volatile const int*)skip != 0; }
+
+// ---------------------------------------------------------------------------
+// internal entry points shared between translation units
+// ---------------------------------------------------------------------------
+struct GemmDesc {
+    int64_t M, N, K;
+    const double* A; int64_t sAm, sAk;
+    const double* B; int64_t sBk, sBn;
+    double* C; int64_t sCm, sCn;
+    double alpha, beta;
+    int64_t nb1, nb0;                      // batch = nb1 x nb0
+    int64_t sA1, sA0, sB1, sB0, sC1, sC0;  // batch strides
+    const int* skip;
+};
+int ct_gemm_f64_launch(ct_handle* h, const GemmDesc& g);
+
+// out(o, j, i) = sum_k Wt[j, k] * in(o, k, i);  j = j1 * J0 + j0
+struct MpoDesc {
+    int64_t O, K, J, I;
+    const double* in; int64_t sIo, sIk, sIi;
+    double* out; int64_t sOo, sOi; int64_t J0, sOj1, sOj0;
+    const double* Wt;   // device [J][K]
+    const int* skip;
+};
+int ct_mpo_apply_f64_launch(ct_handle* h, const MpoDesc& m);
+
+// W-matrix builders (device) for the contractions
+int ct_build_w12(ct_handle* h, const double* W1, const double* W2, double* W12t, int64_t wL,
+                 int64_t d, int64_t wM, int64_t wR);
+int ct_build_wt_left(ct_handle* h, const double* W, double* Wt, int64_t wL, int64_t d, int64_t wR);
+int ct_build_wt_right(ct_handle* h, const double* W, double* Wt, int64_t wL, int64_t d, int64_t wR);
+
+// vector kernels (ct_vec.cu)
+int ct_reduce_dot(ct_handle* h, int64_t n, const double* x, const double* y, double* d_out,
+                  const int* skip);
+int ct_reduce_nrm2sq(ct_handle* h, int64_t n, const double* x, double* d_out, const int* skip);
+int ct_scale_by_inv_sqrt(ct_handle* h, int64_t n, const double* x, double* y,
+                         const double* d_nsq, const int* skip, int zero_code);
+int ct_fill(ct_handle* h, double* x, int64_t n, double v);
+int ct_copy(ct_handle* h, double* dst, const double* src, int64_t n);
+int ct_permute_launch(ct_handle* h, const double* in, double* out, int rank, const int64_t* shape,
+                      const int32_t* perm);
+int ct_identity_env(ct_handle* h, double* E, int64_t w, int64_t D);
+
+// Lanczos pieces
+int ct_lanczos_update(ct_handle* h, int64_t n, double* w, const double* vj, const double* vjm1,
+                      int j, double beta_threshold, const int* skip);
+int ct_lanczos_next(ct_handle* h, int64_t n, const double* w, double* vnext, int j, const int* skip);
+int ct_lanczos_alpha(ct_handle* h, int64_t n, const double* vj, const double* w, int j,
+                     const int* skip);
+int ct_lanczos_reorth(ct_handle* h, int64_t n, double* w, const double* V, int64_t ldv, int nvec,
+                      double* coeff_scratch, const int* skip);
+int ct_tridiag_eig(ct_handle* h, int max_iter, double tol, int max_rotations);
+int ct_ritz(ct_handle* h, int64_t n, const double* V, int64_t ldv, double* out);
+
+// SVD (ct_svd.cu)
+struct SvdOut {
+    int64_t chi = 0;
+    double sum_s2_all = 0.0;  // sum of all min(m,n) s^2 (sorted order)
+    double sum_s2_kept = 0.0;
+};
+// tensor-core path (ct_tc.cu)
+struct TcGemm;
+int ct_tc_available(ct_handle* h);

@@ -1,0 +1,108 @@
+// Plain-form FP64 contraction kernel: a strided, batched SIMT GEMM.
+//
+// C(m,n) = alpha * sum_k A(m,k) B(k,n) + beta * C(m,n) with arbitrary element
+// strides for every index and a two-level batch index, so every contraction of
+// the path (dense_tensor_dot, dense_tensor.mojo:963-1328, and the permute +
+// GEMM chains of dmrg.mojo:254-374 / environments.mojo:99-417) is one launch
+// with the permutes folded into the operand addressing -- no physical
+// transposes.  FP64 on GB300 issues at a small fraction of the FP32 rate, so
+// a 64x64x16 smem tile with a 4x4 register block already saturates the FP64
+// pipe; the tensor-core path lives in ct_tc.cu.
+#include "ct_common.cuh"
+
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
+
+template <bool A_K_CONTIG, bool B_N_CONTIG>
+__global__ void __launch_bounds__(NT) gemm_f64_kernel(GemmDesc g) {
+    if (ct_skip(g.skip)) return;
+    __shared__ double As[BK][BM + 1];
+    __shared__ double Bs[BK][BN + 1];
+
+    const int64_t bz = blockIdx.z;
+    const int64_t b1 = bz / g.nb0, b0 = bz % g.nb0;
+    const double* A = g.A + b1 * g.sA1 + b0 * g.sA0;
+    const double* B = g.B + b1 * g.sB1 + b0 * g.sB0;
+    double* C = g.C + b1 * g.sC1 + b0 * g.sC0;
+
+    const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+
+    double acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+
+    for (int64_t k0 = 0; k0 < g.K; k0 += BK) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int e = tid + NT * r;
+            int mm, kk;
+            if (A_K_CONTIG) { kk = e % BK; mm = e / BK; }
+            else            { mm = e % BM; kk = e / BM; }
+            const int64_t gm = m0 + mm, gk = k0 + kk;
+            As[kk][mm] = (gm < g.M && gk < g.K) ? A[gm * g.sAm + gk * g.sAk] : 0.0;
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int e = tid + NT * r;
+            int nn, kk;
+            if (B_N_CONTIG) { nn = e % BN; kk = e / BN; }
+            else            { kk = e % BK; nn = e / BK; }
+            const int64_t gn = n0 + nn, gk = k0 + kk;
+            Bs[kk][nn] = (gn < g.N && gk < g.K) ? B[gk * g.sBk + gn * g.sBn] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            double a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int64_t gm = m0 + ty + 16 * i;
+        if (gm >= g.M) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t gn = n0 + tx + 16 * j;
+            if (gn >= g.N) continue;
+            double* c = C + gm * g.sCm + gn * g.sCn;
+            double v = g.alpha * acc[i][j];
+            if (g.beta != 0.0) v = fma(g.beta, *c, v);
+            *c = v;
+        }
+    }
+}
+
+}  // namespace
+
+int ct_gemm_f64_launch(ct_handle* h, const GemmDesc& g) {
+    if (g.M <= 0 || g.N <= 0) return CT_OK;
+    const int64_t nb = g.nb1 * g.nb0;
+    if (nb <= 0) return CT_OK;
+    if (g.K <= 0 && g.beta == 1.0) return CT_OK;  // C unchanged; K = 0 otherwise gives C = beta*C
+    dim3 grid((unsigned)ct_cdiv(g.N, BN), (unsigned)ct_cdiv(g.M, BM), (unsigned)nb);
+    if (grid.y > 65535 || grid.z > 65535) {
+        ct_seterr(h, "gemm grid too large (M=%lld nb=%lld)", (long long)g.M, (long long)nb);
+        return CT_ERR_UNSUPPORTED;
+    }
+    const bool ak = (g.sAk == 1);
+    const bool bn = (g.sBn == 1);
+    if (ak && bn) gemm_f64_kernel<true, true><<<grid, NT, 0, h->stream>>>(g);
+    else if (ak) gemm_f64_kernel<true, false><<<grid, NT, 0, h->stream>>>(g);
+    else if (bn) gemm_f64_kernel<false, true><<<grid, NT, 0, h->stream>>>(g);
+    else gemm_f64_kernel<false, false><<<grid, NT, 0, h->stream>>>(g);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}

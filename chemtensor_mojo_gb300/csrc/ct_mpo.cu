@@ -1,0 +1,129 @@
+// MPO legs of the contraction chains: small-K, memory-bound contractions.
+//
+// The reference contracts the MPO tensors with two GEMMs plus permutes per
+// H_eff apply (dmrg.mojo:326-356) and one per environment update
+// (environments.mojo:158-175, :374-396).  Here W_i and W_{i+1} are first fused
+// into one (d^2 wR) x (wL d^2) matrix W12 (sum over the middle MPO bond, once
+// per bond) and applied in a single pass over the intermediate: each thread
+// owns one column i of in(o, :, i), streams its K inputs once per chunk of 8
+// outputs and keeps the weights in shared memory.
+#include "ct_common.cuh"
+
+namespace {
+
+constexpr int MPO_NT = 128;
+constexpr int MPO_JC = 8;
+
+__global__ void __launch_bounds__(MPO_NT) mpo_apply_f64_kernel(MpoDesc m) {
+    if (ct_skip(m.skip)) return;
+    extern __shared__ double wsm[];
+    const int64_t JK = m.J * m.K;
+    for (int64_t t = threadIdx.x; t < JK; t += MPO_NT) wsm[t] = m.Wt[t];
+    __syncthreads();
+    const int64_t o = blockIdx.y;
+    const int64_t i = (int64_t)blockIdx.x * MPO_NT + threadIdx.x;
+    if (i >= m.I) return;
+    const double* in = m.in + o * m.sIo + i * m.sIi;
+    double* out = m.out + o * m.sOo + i * m.sOi;
+    for (int64_t j0 = 0; j0 < m.J; j0 += MPO_JC) {
+        double acc[MPO_JC];
+#pragma unroll
+        for (int jj = 0; jj < MPO_JC; ++jj) acc[jj] = 0.0;
+        const int nj = (int)((m.J - j0) < MPO_JC ? (m.J - j0) : MPO_JC);
+        for (int64_t k = 0; k < m.K; ++k) {
+            const double x = in[k * m.sIk];
+#pragma unroll
+            for (int jj = 0; jj < MPO_JC; ++jj)
+                if (jj < nj) acc[jj] = fma(wsm[(j0 + jj) * m.K + k], x, acc[jj]);
+        }
+#pragma unroll
+        for (int jj = 0; jj < MPO_JC; ++jj) {
+            if (jj >= nj) break;
+            const int64_t j = j0 + jj;
+            const int64_t j1 = j / m.J0, jr = j % m.J0;
+            out[j1 * m.sOj1 + jr * m.sOj0] = acc[jj];
+        }
+    }
+}
+
+// W12t[(t1 t2 wR), (wL s1 s2)] = sum_wM W1[wL,s1,t1,wM] W2[wM,s2,t2,wR]
+__global__ void build_w12_kernel(const double* W1, const double* W2, double* W12t, int64_t wL,
+                                 int64_t d, int64_t wM, int64_t wR) {
+    const int64_t J = d * d * wR, K = wL * d * d;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= J * K) return;
+    const int64_t j = t / K, k = t % K;
+    const int64_t wr = j % wR, t2 = (j / wR) % d, t1 = j / (wR * d);
+    const int64_t s2 = k % d, s1 = (k / d) % d, wl = k / (d * d);
+    double acc = 0.0;
+    for (int64_t wm = 0; wm < wM; ++wm) {
+        const double a = W1[((wl * d + s1) * d + t1) * wM + wm];
+        const double b = W2[((wm * d + s2) * d + t2) * wR + wr];
+        acc = fma(a, b, acc);
+    }
+    W12t[t] = acc;
+}
+
+// Wt[(s' wR), (wL s)] = W[wL, s, s', wR]   (left environment)
+__global__ void build_wt_left_kernel(const double* W, double* Wt, int64_t wL, int64_t d, int64_t wR) {
+    const int64_t J = d * wR, K = wL * d;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= J * K) return;
+    const int64_t j = t / K, k = t % K;
+    const int64_t sp = j / wR, wr = j % wR, wl = k / d, s = k % d;
+    Wt[t] = W[((wl * d + s) * d + sp) * wR + wr];
+}
+
+// Wt[(wL s'), (wR s)] = W[wL, s, s', wR]   (right environment)
+__global__ void build_wt_right_kernel(const double* W, double* Wt, int64_t wL, int64_t d, int64_t wR) {
+    const int64_t J = wL * d, K = wR * d;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= J * K) return;
+    const int64_t j = t / K, k = t % K;
+    const int64_t wl = j / d, sp = j % d, wr = k / d, s = k % d;
+    Wt[t] = W[((wl * d + s) * d + sp) * wR + wr];
+}
+
+}  // namespace
+
+int ct_mpo_apply_f64_launch(ct_handle* h, const MpoDesc& m) {
+    if (m.O <= 0 || m.I <= 0 || m.J <= 0) return CT_OK;
+    const size_t smem = (size_t)(m.J * m.K) * sizeof(double);
+    if (smem > 200 * 1024) {
+        ct_seterr(h, "MPO weight matrix too large (%lld x %lld)", (long long)m.J, (long long)m.K);
+        return CT_ERR_UNSUPPORTED;
+    }
+    static bool attr_set = false;
+    if (!attr_set) {
+        CT_CUDA(h, cudaFuncSetAttribute(mpo_apply_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        200 * 1024));
+        attr_set = true;
+    }
+    if (m.O > 65535) return CT_ERR_UNSUPPORTED;
+    dim3 grid((unsigned)ct_cdiv(m.I, MPO_NT), (unsigned)m.O);
+    mpo_apply_f64_kernel<<<grid, MPO_NT, smem, h->stream>>>(m);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_build_w12(ct_handle* h, const double* W1, const double* W2, double* W12t, int64_t wL,
+                 int64_t d, int64_t wM, int64_t wR) {
+    const int64_t n = (d * d * wR) * (wL * d * d);
+    build_w12_kernel<<<(unsigned)ct_cdiv(n, 256), 256, 0, h->stream>>>(W1, W2, W12t, wL, d, wM, wR);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_build_wt_left(ct_handle* h, const double* W, double* Wt, int64_t wL, int64_t d, int64_t wR) {
+    const int64_t n = (d * wR) * (wL * d);
+    build_wt_left_kernel<<<(unsigned)ct_cdiv(n, 256), 256, 0, h->stream>>>(W, Wt, wL, d, wR);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_build_wt_right(ct_handle* h, const double* W, double* Wt, int64_t wL, int64_t d, int64_t wR) {
+    const int64_t n = (wL * d) * (wR * d);
+    build_wt_right_kernel<<<(unsigned)ct_cdiv(n, 256), 256, 0, h->stream>>>(W, Wt, wL, d, wR);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}

@@ -1,0 +1,235 @@
+// Contraction chains of the two-site DMRG path, built from the strided GEMM
+// (ct_gemm_f64.cu), the MPO apply (ct_mpo.cu) and, for the mixed form, the
+// tcgen05 GEMM (ct_tc.cu).  Layouts of the intermediates are chosen so that
+// every permute of the reference chains becomes operand addressing:
+//
+//   H_eff (dmrg.mojo:254-374)
+//     T1[Dl', wL, s1, s2, Dr] = sum_Dl L[wL,Dl,Dl'] th[Dl,(s1 s2 Dr)]      GEMM, batch wL
+//     T3[Dl', t1, t2, wR, Dr] = sum_(wL s1 s2) W12[..] T1[Dl',(wL s1 s2),Dr] MPO apply
+//     out[(Dl' t1 t2), Dr']   = sum_(wR Dr) T3[..,(wR Dr)] R[(wR Dr), Dr'] GEMM
+//   left env (environments.mojo:99-201)
+//     T1[Dl', wL, s, Dr] = sum_Dl L[wL,Dl,Dl'] A[Dl,(s Dr)]                GEMM, batch wL
+//     T2[Dl', s', wR, Dr] = sum_(wL s) W[wL,s,s',wR] T1                    MPO apply
+//     Ln[(wR Dr), Dr'] = sum_(Dl' s') T2[(Dl' s'),(wR Dr)] A[(Dl' s'),Dr'] GEMM
+//   right env (environments.mojo:309-417)
+//     T1[Dr', wR, s, Dl] = sum_Dr R[wR,Dr,Dr'] A[Dl,s,Dr]                  GEMM, batch (wR,s)
+//     T2[wL, Dl, s', Dr'] = sum_(wR s) W[wL,s,s',wR] T1                    MPO apply
+//     Rp[wL, Dl, Dl'] = sum_(s' Dr') T2[wL,Dl,(s' Dr')] A[Dl',(s' Dr')]    GEMM, batch wL
+#include "ct_ops.cuh"
+
+size_t ct_heff_ws_bytes(int prec, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wM, int64_t wR) {
+    (void)wM;
+    if (prec == CT_PREC_TF32X3) return ct_tc_heff_ws_bytes(Dl, d, Dr, wL, wM, wR);
+    const int64_t t1 = Dl * wL * d * d * Dr;
+    const int64_t t3 = Dl * d * d * wR * Dr;
+    const int64_t w12 = (d * d * wR) * (wL * d * d);
+    return ct_bytes(t1, 8) + ct_bytes(t3, 8) + ct_bytes(w12, 8);
+}
+
+// Per-bond preparation (W12) is separated so that a Lanczos run builds it once.
+int ct_heff_prepare(ct_handle* h, Arena& ar, HeffPlan& p, int prec, const double* L, const double* R,
+                    const double* W1, const double* W2, int64_t Dl, int64_t d, int64_t Dr, int64_t wL,
+                    int64_t wM, int64_t wR) {
+    p.prec = prec;
+    p.L = L; p.R = R; p.W1 = W1; p.W2 = W2;
+    p.Dl = Dl; p.d = d; p.Dr = Dr; p.wL = wL; p.wM = wM; p.wR = wR;
+    if (prec == CT_PREC_TF32X3) return ct_tc_heff_prepare(h, ar, p);
+    p.T1 = ar.take<double>(Dl * wL * d * d * Dr);
+    p.T3 = ar.take<double>(Dl * d * d * wR * Dr);
+    p.W12 = ar.take<double>((d * d * wR) * (wL * d * d));
+    if (!p.T1 || !p.T3 || !p.W12) return CT_ERR_OOM;
+    return ct_build_w12(h, W1, W2, p.W12, wL, d, wM, wR);
+}
+
+int ct_heff_run(ct_handle* h, const HeffPlan& p, const double* theta, double* out, const int* skip) {
+    if (p.prec == CT_PREC_TF32X3) return ct_tc_heff_run(h, p, theta, out, skip);
+    const int64_t Dl = p.Dl, d = p.d, Dr = p.Dr, wL = p.wL, wR = p.wR;
+    const int64_t n1 = d * d * Dr;
+    {   // T1[Dl', wL, n1] = sum_Dl L[wL, Dl, Dl'] theta[Dl, n1]
+        GemmDesc g{};
+        g.M = Dl; g.N = n1; g.K = Dl;
+        g.A = p.L; g.sAm = 1; g.sAk = Dl;
+        g.B = theta; g.sBk = n1; g.sBn = 1;
+        g.C = p.T1; g.sCm = wL * n1; g.sCn = 1;
+        g.alpha = 1.0; g.beta = 0.0;
+        g.nb1 = wL; g.nb0 = 1;
+        g.sA1 = Dl * Dl; g.sB1 = 0; g.sC1 = n1;
+        g.skip = skip;
+        CT_TRY(ct_gemm_f64_launch(h, g));
+    }
+    {   // T3[Dl', (t1 t2 wR), Dr] = sum_k W12t[j, k] T1[Dl', k, Dr]
+        MpoDesc m{};
+        m.O = Dl; m.K = wL * d * d; m.J = d * d * wR; m.I = Dr;
+        m.in = p.T1; m.sIo = wL * d * d * Dr; m.sIk = Dr; m.sIi = 1;
+        m.out = p.T3; m.sOo = d * d * wR * Dr; m.sOi = 1; m.J0 = m.J; m.sOj1 = 0; m.sOj0 = Dr;
+        m.Wt = p.W12; m.skip = skip;
+        CT_TRY(ct_mpo_apply_f64_launch(h, m));
+    }
+    {   // out[(Dl' t1 t2), Dr'] = sum_(wR Dr) T3[.., (wR Dr)] R[(wR Dr), Dr']
+        GemmDesc g{};
+        g.M = Dl * d * d; g.N = Dr; g.K = wR * Dr;
+        g.A = p.T3; g.sAm = wR * Dr; g.sAk = 1;
+        g.B = p.R; g.sBk = Dr; g.sBn = 1;
+        g.C = out; g.sCm = Dr; g.sCn = 1;
+        g.alpha = 1.0; g.beta = 0.0; g.nb1 = 1; g.nb0 = 1;
+        g.skip = skip;
+        CT_TRY(ct_gemm_f64_launch(h, g));
+    }
+    return CT_OK;
+}
+
+size_t ct_env_ws_bytes(int prec, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR) {
+    if (prec == CT_PREC_TF32X3) return ct_tc_env_ws_bytes(Dl, d, Dr, wL, wR);
+    const int64_t t1 = Dl * d * Dr * (wL > wR ? wL : wR);
+    const int64_t wt = (wL * d) * (wR * d);
+    return 2 * ct_bytes(t1, 8) + ct_bytes(wt, 8);
+}
+
+int ct_env_left_run(ct_handle* h, Arena& ar, int prec, const double* Lp, const double* A, const double* W,
+                    double* Ln, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR) {
+    if (prec == CT_PREC_TF32X3) return ct_tc_env_left_run(h, ar, Lp, A, W, Ln, Dl, d, Dr, wL, wR);
+    double* T1 = ar.take<double>(Dl * wL * d * Dr);
+    double* T2 = ar.take<double>(Dl * d * wR * Dr);
+    double* Wt = ar.take<double>((d * wR) * (wL * d));
+    if (!T1 || !T2 || !Wt) return CT_ERR_OOM;
+    CT_TRY(ct_build_wt_left(h, W, Wt, wL, d, wR));
+    const int64_t n1 = d * Dr;
+    {
+        GemmDesc g{};
+        g.M = Dl; g.N = n1; g.K = Dl;
+        g.A = Lp; g.sAm = 1; g.sAk = Dl;
+        g.B = A; g.sBk = n1; g.sBn = 1;
+        g.C = T1; g.sCm = wL * n1; g.sCn = 1;
+        g.alpha = 1.0; g.beta = 0.0; g.nb1 = wL; g.nb0 = 1;
+        g.sA1 = Dl * Dl; g.sC1 = n1;
+        CT_TRY(ct_gemm_f64_launch(h, g));
+    }
+    {
+        MpoDesc m{};
+        m.O = Dl; m.K = wL * d; m.J = d * wR; m.I = Dr;
+        m.in = T1; m.sIo = wL * d * Dr; m.sIk = Dr; m.sIi = 1;
+        m.out = T2; m.sOo = d * wR * Dr; m.sOi = 1; m.J0 = m.J; m.sOj1 = 0; m.sOj0 = Dr;
+        m.Wt = Wt;
+        CT_TRY(ct_mpo_apply_f64_launch(h, m));
+    }
+    {
+        GemmDesc g{};
+        g.M = wR * Dr; g.N = Dr; g.K = Dl * d;
+        g.A = T2; g.sAm = 1; g.sAk = wR * Dr;
+        g.B = A; g.sBk = Dr; g.sBn = 1;
+        g.C = Ln; g.sCm = Dr; g.sCn = 1;
+        g.alpha = 1.0; g.beta = 0.0; g.nb1 = 1; g.nb0 = 1;
+        CT_TRY(ct_gemm_f64_launch(h, g));
+    }
+    return CT_OK;
+}
+
+int ct_env_right_run(ct_handle* h, Arena& ar, int prec, const double* Rn, const double* A, const double* W,
+                     double* Rp, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR) {
+    if (prec == CT_PREC_TF32X3) return ct_tc_env_right_run(h, ar, Rn, A, W, Rp, Dl, d, Dr, wL, wR);
+    double* T1 = ar.take<double>(Dr * wR * d * Dl);
+    double* T2 = ar.take<double>(wL * Dl * d * Dr);
+    double* Wt = ar.take<double>((wL * d) * (wR * d));
+    if (!T1 || !T2 || !Wt) return CT_ERR_OOM;
+    CT_TRY(ct_build_wt_right(h, W, Wt, wL, d, wR));
+    {   // T1[Dr', wR, s, Dl] = sum_Dr R[wR, Dr, Dr'] A[Dl, s, Dr]; batch (wR, s)
+        GemmDesc g{};
+        g.M = Dr; g.N = Dl; g.K = Dr;
+        g.A = Rn; g.sAm = 1; g.sAk = Dr;
+        g.B = A; g.sBk = 1; g.sBn = d * Dr;
+        g.C = T1; g.sCm = wR * d * Dl; g.sCn = 1;
+        g.alpha = 1.0; g.beta = 0.0;
+        g.nb1 = wR; g.nb0 = d;
+        g.sA1 = Dr * Dr; g.sA0 = 0;
+        g.sB1 = 0; g.sB0 = Dr;
+        g.sC1 = d * Dl; g.sC0 = Dl;
+        CT_TRY(ct_gemm_f64_launch(h, g));
+    }
+    {   // T2[wL, Dl, s', Dr'] = sum_(wR s) Wt[(wL s'), (wR s)] T1[Dr', (wR s), Dl]
+        MpoDesc m{};
+        m.O = Dr; m.K = wR * d; m.J = wL * d; m.I = Dl;
+        m.in = T1; m.sIo = wR * d * Dl; m.sIk = Dl; m.sIi = 1;
+        m.out = T2; m.sOo = 1; m.sOi = d * Dr; m.J0 = d; m.sOj1 = Dl * d * Dr; m.sOj0 = Dr;
+        m.Wt = Wt;
+        CT_TRY(ct_mpo_apply_f64_launch(h, m));
+    }
+    {   // Rp[wL, Dl, Dl'] = sum_(s' Dr') T2[wL, Dl, (s' Dr')] A[Dl', (s' Dr')]; batch wL
+        GemmDesc g{};
+        g.M = Dl; g.N = Dl; g.K = d * Dr;
+        g.A = T2; g.sAm = d * Dr; g.sAk = 1;
+        g.B = A; g.sBk = 1; g.sBn = d * Dr;
+        g.C = Rp; g.sCm = Dl; g.sCn = 1;
+        g.alpha = 1.0; g.beta = 0.0; g.nb1 = wL; g.nb0 = 1;
+        g.sA1 = Dl * d * Dr; g.sC1 = Dl * Dl;
+        CT_TRY(ct_gemm_f64_launch(h, g));
+    }
+    return CT_OK;
+}
+
+int ct_theta_run(ct_handle* h, int prec, const double* Ai, const double* Aj, double* theta, int64_t Dl,
+                 int64_t d, int64_t Dm, int64_t Dr) {
+    (void)prec;  // once per bond: always FP64
+    GemmDesc g{};
+    g.M = Dl * d; g.N = d * Dr; g.K = Dm;
+    g.A = Ai; g.sAm = Dm; g.sAk = 1;
+    g.B = Aj; g.sBk = d * Dr; g.sBn = 1;
+    g.C = theta; g.sCm = d * Dr; g.sCn = 1;
+    g.alpha = 1.0; g.beta = 0.0; g.nb1 = 1; g.nb0 = 1;
+    return ct_gemm_f64_launch(h, g);
+}
+
+// ---------------------------------------------------------------------------
+// Lanczos (dmrg.mojo:486-756), everything device resident
+// ---------------------------------------------------------------------------
+size_t ct_lanczos_ws_bytes(int prec, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wM, int64_t wR,
+                           int max_iter) {
+    const int64_t N = Dl * d * d * Dr;
+    return ct_bytes(N * (int64_t)max_iter, 8) + ct_bytes(N, 8) + ct_heff_ws_bytes(prec, Dl, d, Dr, wL, wM, wR);
+}
+
+int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, double* theta_out, const double* L,
+                   const double* R, const double* W1, const double* W2, int64_t Dl, int64_t d, int64_t Dr,
+                   int64_t wL, int64_t wM, int64_t wR, int max_iter, double tol, int max_rotations, int reorth,
+                   LanczosResult* res) {
+    if (max_iter < 1 || max_iter > 64) {
+        ct_seterr(h, "max_krylov_iter must be in [1, 64], got %d", max_iter);
+        return CT_ERR_UNSUPPORTED;
+    }
+    const int64_t N = Dl * d * d * Dr;
+    double* V = ar.take<double>(N * (int64_t)max_iter);
+    double* w = ar.take<double>(N);
+    if (!V || !w) return CT_ERR_OOM;
+    HeffPlan plan;
+    CT_TRY(ct_heff_prepare(h, ar, plan, prec, L, R, W1, W2, Dl, d, Dr, wL, wM, wR));
+    const int* stop = h->d_flags + FL_STOP;
+    CT_TRY(ct_lanczos_init(h, max_iter));
+    // v0 = theta / |theta|  (zero norm -> CT_ERR_ZERO_NORM, dmrg.mojo:605-611)
+    CT_TRY(ct_reduce_nrm2sq(h, N, theta_in, h->d_scalars + SC_NORM, nullptr));
+    CT_TRY(ct_scale_by_inv_sqrt(h, N, theta_in, V, h->d_scalars + SC_NORM, nullptr, CT_ERR_ZERO_NORM));
+    const double thr = 100.0 * (double)N * 2.2204460492503131e-16;
+    for (int j = 0; j < max_iter - 1; ++j) {
+        double* vj = V + (int64_t)j * N;
+        const double* vjm1 = (j > 0) ? V + (int64_t)(j - 1) * N : nullptr;
+        CT_TRY(ct_heff_run(h, plan, vj, w, stop));
+        CT_TRY(ct_lanczos_alpha(h, N, vj, w, j, stop));
+        CT_TRY(ct_lanczos_update(h, N, w, vj, vjm1, j, thr, stop));
+        if (reorth) CT_TRY(ct_lanczos_reorth_beta(h, N, w, V, N, j + 1, j, thr, stop));
+        CT_TRY(ct_lanczos_next(h, N, w, V + (int64_t)(j + 1) * N, j, stop));
+    }
+    {   // final alpha-only iteration, only when no breakdown (dmrg.mojo:691-703)
+        const int j = max_iter - 1;
+        double* vj = V + (int64_t)j * N;
+        CT_TRY(ct_heff_run(h, plan, vj, w, stop));
+        CT_TRY(ct_lanczos_alpha(h, N, vj, w, j, stop));
+    }
+    CT_TRY(ct_tridiag_eig(h, max_iter, tol, max_rotations));
+    CT_TRY(ct_ritz(h, N, V, N, w));
+    CT_TRY(ct_reduce_nrm2sq(h, N, w, h->d_scalars + SC_NORM, nullptr));
+    CT_TRY(ct_scale_by_inv_sqrt(h, N, w, theta_out, h->d_scalars + SC_NORM, nullptr, 0));
+    if (res) {
+        res->d_energy = h->d_scalars + SC_ENERGY;
+        res->d_numiter = h->d_flags + FL_NUMITER;
+        res->applies_upper = max_iter;
+    }
+    return CT_OK;
+}

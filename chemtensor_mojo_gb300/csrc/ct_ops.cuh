@@ -1,0 +1,67 @@
+// Internal interfaces of the contraction chains and the Lanczos driver.
+#pragma once
+#include "ct_common.cuh"
+
+struct HeffPlan {
+    int prec = CT_PREC_FP64;
+    const double *L = nullptr, *R = nullptr, *W1 = nullptr, *W2 = nullptr;
+    int64_t Dl = 0, d = 0, Dr = 0, wL = 0, wM = 0, wR = 0;
+    // FP64 form
+    double* T1 = nullptr;
+    double* T3 = nullptr;
+    double* W12 = nullptr;
+    // mixed form (ct_tc.cu)
+    void* tc = nullptr;
+};
+
+struct LanczosResult {
+    double* d_energy = nullptr;
+    int* d_numiter = nullptr;
+    int applies_upper = 0;
+};
+
+size_t ct_heff_ws_bytes(int prec, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wM, int64_t wR);
+int ct_heff_prepare(ct_handle* h, Arena& ar, HeffPlan& p, int prec, const double* L, const double* R,
+                    const double* W1, const double* W2, int64_t Dl, int64_t d, int64_t Dr, int64_t wL,
+                    int64_t wM, int64_t wR);
+int ct_heff_run(ct_handle* h, const HeffPlan& p, const double* theta, double* out, const int* skip);
+
+size_t ct_env_ws_bytes(int prec, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR);
+int ct_env_left_run(ct_handle* h, Arena& ar, int prec, const double* Lp, const double* A, const double* W,
+                    double* Ln, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR);
+int ct_env_right_run(ct_handle* h, Arena& ar, int prec, const double* Rn, const double* A, const double* W,
+                     double* Rp, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR);
+int ct_theta_run(ct_handle* h, int prec, const double* Ai, const double* Aj, double* theta, int64_t Dl,
+                 int64_t d, int64_t Dm, int64_t Dr);
+
+size_t ct_lanczos_ws_bytes(int prec, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wM, int64_t wR,
+                           int max_iter);
+int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, double* theta_out, const double* L,
+                   const double* R, const double* W1, const double* W2, int64_t Dl, int64_t d, int64_t Dr,
+                   int64_t wL, int64_t wM, int64_t wR, int max_iter, double tol, int max_rotations, int reorth,
+                   LanczosResult* res);
+
+// vector helpers (ct_vec.cu)
+int ct_vec_axpy_launch(ct_handle* h, int64_t n, double alpha, const double* x, double* y);
+int ct_vec_scale_launch(ct_handle* h, int64_t n, double alpha, double* x);
+int ct_lanczos_init(ct_handle* h, int max_iter);
+int ct_lanczos_reorth_beta(ct_handle* h, int64_t n, double* w, const double* V, int64_t ldv, int nvec, int j,
+                           double beta_threshold, const int* skip);
+
+// SVD workspace (ct_svd.cu)
+size_t ct_svd_ws_bytes(int64_t m, int64_t n, int mode);
+int ct_svd_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t chi_max,
+               double eps_trunc, int mode, double* A, double* B, double* S, SvdOut* out);
+
+// mixed form (ct_tc.cu)
+size_t ct_tc_heff_ws_bytes(int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wM, int64_t wR);
+int ct_tc_heff_prepare(ct_handle* h, Arena& ar, HeffPlan& p);
+int ct_tc_heff_run(ct_handle* h, const HeffPlan& p, const double* theta, double* out, const int* skip);
+size_t ct_tc_env_ws_bytes(int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR);
+int ct_tc_env_left_run(ct_handle* h, Arena& ar, const double* Lp, const double* A, const double* W, double* Ln,
+                       int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR);
+int ct_tc_env_right_run(ct_handle* h, Arena& ar, const double* Rn, const double* A, const double* W, double* Rp,
+                        int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR);
+int ct_tc_gemm(ct_handle* h, Arena& ar, int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha,
+               const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc);
+size_t ct_tc_gemm_ws_bytes(int64_t m, int64_t n, int64_t k);

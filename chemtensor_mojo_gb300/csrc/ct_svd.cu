@@ -1,0 +1,390 @@
+// Device SVD split: one-sided (Hestenes) Jacobi in FP64 + the reference's
+// truncation rule, replacing the host LAPACK dgesdd round trip of
+// dense_tensor_svd_trunc_lapack_f64 (dense_tensor.mojo:1483-1592) and the
+// host-side S absorption of split_two_site_theta_svd (dmrg.mojo:143-252).
+//
+// The factor that must come out orthonormal is the one that is accumulated:
+//   left-to-right  (A = U, B = S Vt): rotate the ROWS of M; the accumulated
+//                  rotations are U, the rotated rows are S Vt;
+//   right-to-left  (A = U S, B = Vt): rotate the COLUMNS of M; the
+//                  accumulated rotations are V, the rotated columns are U S.
+// No division by a singular value is needed in either sweep direction.
+//
+// Small problems run in one CTA with everything in shared memory (no host
+// round trip); large ones run one launch per round-robin round, n/2 pairs in
+// parallel, with a rotation counter read back once per sweep.
+#include "ct_ops.cuh"
+
+namespace {
+
+constexpr int SVD_NT = 256;
+constexpr int SVD_MAX_SWEEPS = 60;
+
+__device__ __forceinline__ void tournament_pair(int P, int r, int k, int& p, int& q) {
+    if (k == 0) {
+        p = P - 1;
+        q = r;
+    } else {
+        p = (r + k) % (P - 1);
+        q = (r - k + (P - 1)) % (P - 1);
+    }
+}
+
+// Rotation that orthogonalises two vectors with |x_p|^2=a, |x_q|^2=b, <x_p,x_q>=c.
+__device__ __forceinline__ bool jacobi_rot(double a, double b, double c, double tol, double& cs, double& sn) {
+    if (c == 0.0 || !(fabs(c) > tol * sqrt(a * b))) return false;
+    const double zeta = (b - a) / (2.0 * c);
+    double t;
+    if (fabs(zeta) > 1e150) t = 0.5 / zeta;
+    else t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+    cs = 1.0 / sqrt(1.0 + t * t);
+    sn = cs * t;
+    return true;
+}
+
+// ---- init: X (nvec x len) from M, Q = I ---------------------------------------
+__global__ void svd_init_kernel(const double* M, int64_t m, int64_t n, int cols, double* X, int64_t ldx,
+                                double* Q, int64_t nvec) {
+    const int64_t len = cols ? m : n;
+    const int64_t tot = nvec * len;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = t / len, e = t % len;
+        X[v * ldx + e] = cols ? M[e * n + v] : M[v * n + e];
+    }
+    const int64_t tq = nvec * nvec;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tq; t += (int64_t)gridDim.x * blockDim.x)
+        Q[t] = ((t / nvec) == (t % nvec)) ? 1.0 : 0.0;
+}
+
+// ---- large path: one round, one CTA per pair -------------------------------
+__global__ void __launch_bounds__(SVD_NT) svd_round_kernel(double* X, int64_t len, int64_t ldx, double* Q,
+                                                           int64_t nvec, int P, int r, double tol, int* rot_count) {
+    __shared__ double sm[32];
+    __shared__ double rot[2];
+    __shared__ int do_rot;
+    int p, q;
+    tournament_pair(P, r, blockIdx.x, p, q);
+    if (p >= nvec || q >= nvec) return;
+    double* xp = X + (int64_t)p * ldx;
+    double* xq = X + (int64_t)q * ldx;
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int64_t i = threadIdx.x; i < len; i += SVD_NT) {
+        const double u = xp[i], v = xq[i];
+        a = fma(u, u, a);
+        b = fma(v, v, b);
+        c = fma(u, v, c);
+    }
+    a = ct_block_sum<SVD_NT>(a, sm);
+    b = ct_block_sum<SVD_NT>(b, sm);
+    c = ct_block_sum<SVD_NT>(c, sm);
+    if (threadIdx.x == 0) {
+        double cs, sn;
+        do_rot = jacobi_rot(a, b, c, tol, cs, sn) ? 1 : 0;
+        if (do_rot) {
+            rot[0] = cs;
+            rot[1] = sn;
+            atomicAdd(rot_count, 1);
+        }
+    }
+    __syncthreads();
+    if (!do_rot) return;
+    const double cs = rot[0], sn = rot[1];
+    for (int64_t i = threadIdx.x; i < len; i += SVD_NT) {
+        const double u = xp[i], v = xq[i];
+        xp[i] = cs * u - sn * v;
+        xq[i] = sn * u + cs * v;
+    }
+    double* qp = Q + (int64_t)p * nvec;
+    double* qq = Q + (int64_t)q * nvec;
+    for (int64_t i = threadIdx.x; i < nvec; i += SVD_NT) {
+        const double u = qp[i], v = qq[i];
+        qp[i] = cs * u - sn * v;
+        qq[i] = sn * u + cs * v;
+    }
+}
+
+// ---- small path: whole Jacobi in one CTA, X and Q in shared memory ------------
+__global__ void __launch_bounds__(SVD_NT) svd_small_kernel(double* Xg, int64_t len, int64_t ldx, double* Qg,
+                                                           int nvec, double tol, int max_sweeps, int* status) {
+    extern __shared__ double ssm[];
+    double* X = ssm;                         // nvec x len
+    double* Q = ssm + (int64_t)nvec * len;   // nvec x nvec
+    for (int64_t t = threadIdx.x; t < (int64_t)nvec * len; t += SVD_NT) X[t] = Xg[(t / len) * ldx + t % len];
+    for (int64_t t = threadIdx.x; t < (int64_t)nvec * nvec; t += SVD_NT) Q[t] = Qg[t];
+    __syncthreads();
+    const int P = nvec + (nvec & 1);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = SVD_NT / 32;
+    bool converged = false;
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+        int rotated = 0;
+        for (int r = 0; r < P - 1; ++r) {
+            for (int k = warp; k < P / 2; k += nw) {
+                int p, q;
+                tournament_pair(P, r, k, p, q);
+                if (p >= nvec || q >= nvec) continue;
+                double* xp = X + (int64_t)p * len;
+                double* xq = X + (int64_t)q * len;
+                double a = 0.0, b = 0.0, c = 0.0;
+                for (int64_t i = lane; i < len; i += 32) {
+                    const double u = xp[i], v = xq[i];
+                    a = fma(u, u, a);
+                    b = fma(v, v, b);
+                    c = fma(u, v, c);
+                }
+                a = ct_warp_sum(a);
+                b = ct_warp_sum(b);
+                c = ct_warp_sum(c);
+                double cs, sn;
+                if (jacobi_rot(a, b, c, tol, cs, sn)) {
+                    rotated = 1;
+                    for (int64_t i = lane; i < len; i += 32) {
+                        const double u = xp[i], v = xq[i];
+                        xp[i] = cs * u - sn * v;
+                        xq[i] = sn * u + cs * v;
+                    }
+                    double* qp = Q + (int64_t)p * nvec;
+                    double* qq = Q + (int64_t)q * nvec;
+                    for (int i = lane; i < nvec; i += 32) {
+                        const double u = qp[i], v = qq[i];
+                        qp[i] = cs * u - sn * v;
+                        qq[i] = sn * u + cs * v;
+                    }
+                }
+                __syncwarp();
+            }
+            __syncthreads();
+        }
+        if (!__syncthreads_or(rotated)) {
+            converged = true;
+            break;
+        }
+    }
+    if (!converged && threadIdx.x == 0) ct_set_status(status, CT_ERR_NOCONV);
+    __syncthreads();
+    for (int64_t t = threadIdx.x; t < (int64_t)nvec * len; t += SVD_NT) Xg[(t / len) * ldx + t % len] = X[t];
+    for (int64_t t = threadIdx.x; t < (int64_t)nvec * nvec; t += SVD_NT) Qg[t] = Q[t];
+}
+
+// sigma_j = |x_j|, one warp per vector
+__global__ void svd_norms_kernel(const double* X, int64_t len, int64_t ldx, int64_t nvec, double* sig) {
+    const int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x & 31;
+    if (v >= nvec) return;
+    double a = 0.0;
+    for (int64_t i = lane; i < len; i += 32) {
+        const double u = X[v * ldx + i];
+        a = fma(u, u, a);
+    }
+    a = ct_warp_sum(a);
+    if (lane == 0) sig[v] = sqrt(a);
+}
+
+// descending order, ties by index: perm[rank(j)] = j
+__global__ void svd_rank_kernel(const double* sig, int64_t nvec, int* perm) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nvec) return;
+    const double sj = sig[j];
+    int64_t rank = 0;
+    for (int64_t i = 0; i < nvec; ++i) {
+        const double si = sig[i];
+        if (si > sj || (si == sj && i < j)) ++rank;
+    }
+    perm[rank] = (int)j;
+}
+
+// chi rule of dense_tensor.mojo:1528-1548, FP64, sequential sums in sorted order
+__global__ void svd_trunc_kernel(const double* sig, const int* perm, int64_t k, int64_t chi_max, double eps,
+                                 double* scalars, int* flags) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int64_t chi = k < chi_max ? k : chi_max;
+    double total = 0.0, kept_at = 0.0;
+    for (int64_t i = 0; i < k; ++i) {
+        const double s = sig[perm[i]];
+        total += s * s;
+    }
+    if (eps > 0.0 && k > 0) {
+        if (total <= 0.0) {
+            chi = 0;
+        } else {
+            double kept = 0.0;
+            const int64_t limit = k < chi_max ? k : chi_max;
+            chi = limit;
+            for (int64_t t = 1; t <= limit; ++t) {
+                const double s = sig[perm[t - 1]];
+                kept += s * s;
+                if ((total - kept) / total <= eps) {
+                    chi = t;
+                    break;
+                }
+            }
+        }
+    }
+    for (int64_t i = 0; i < chi; ++i) {
+        const double s = sig[perm[i]];
+        kept_at += s * s;
+    }
+    flags[FL_CHI] = (int)chi;
+    scalars[SC_TMP0] = total;
+    scalars[SC_TMP1] = kept_at;
+}
+
+// outputs; vectors = rows (cols=0) or columns (cols=1) of M
+__global__ void svd_gather_kernel(const double* X, int64_t ldx, const double* Q, int64_t nvec, const double* sig,
+                                  const int* perm, const int* flags, int64_t m, int64_t n, int cols, int mode,
+                                  double* A, double* B, double* S) {
+    const int64_t chi = flags[FL_CHI];
+    // A: m x chi
+    const int64_t totA = m * chi;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < totA; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / chi, c = t % chi;
+        const int64_t v = perm[c];
+        double val;
+        if (!cols) {
+            val = Q[v * nvec + r];                       // U
+            if (mode == 1) val *= sig[v];                // U S
+        } else {
+            val = X[v * ldx + r];                        // U S
+            if (mode == 0 || mode == 2) {                // U
+                const double s = sig[v];
+                val = (s > 0.0) ? val / s : 0.0;
+            }
+        }
+        A[t] = val;
+    }
+    // B: chi x n
+    const int64_t totB = chi * n;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < totB; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = t / n, x = t % n;
+        const int64_t v = perm[c];
+        double val;
+        if (!cols) {
+            val = X[v * ldx + x];                        // S Vt
+            if (mode == 1 || mode == 2) {                // Vt
+                const double s = sig[v];
+                val = (s > 0.0) ? val / s : 0.0;
+            }
+        } else {
+            val = Q[v * nvec + x];                       // Vt
+            if (mode == 0) val *= sig[v];                // S Vt
+        }
+        B[t] = val;
+    }
+    if (S) {
+        for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < chi; t += (int64_t)gridDim.x * blockDim.x)
+            S[t] = sig[perm[t]];
+    }
+}
+
+}  // namespace
+
+static void svd_geometry(int64_t m, int64_t n, int mode, int& cols, int64_t& nvec, int64_t& len) {
+    // mode 0 (A=U, B=S Vt) rotates rows; mode 1 (A=U S, B=Vt) rotates columns;
+    // mode 2 (U, S, Vt) rotates the shorter side.
+    if (mode == 0) cols = 0;
+    else if (mode == 1) cols = 1;
+    else cols = (m > n) ? 1 : 0;
+    nvec = cols ? n : m;
+    len = cols ? m : n;
+}
+
+size_t ct_svd_ws_bytes(int64_t m, int64_t n, int mode) {
+    int cols;
+    int64_t nvec, len;
+    svd_geometry(m, n, mode, cols, nvec, len);
+    return ct_bytes(nvec * len, 8) + ct_bytes(nvec * nvec, 8) + ct_bytes(nvec, 8) + ct_bytes(nvec, 4);
+}
+
+int ct_svd_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t chi_max, double eps_trunc,
+               int mode, double* A, double* B, double* S, SvdOut* out) {
+    if (m <= 0 || n <= 0) {
+        out->chi = 0;
+        return CT_OK;
+    }
+    int cols;
+    int64_t nvec, len;
+    svd_geometry(m, n, mode, cols, nvec, len);
+    const int64_t ldx = len;
+    const int64_t k = m < n ? m : n;
+    if (nvec > (int64_t)1 << 20) return CT_ERR_UNSUPPORTED;
+    double* X = ar.take<double>(nvec * ldx);
+    double* Q = ar.take<double>(nvec * nvec);
+    double* sig = ar.take<double>(nvec);
+    int* perm = ar.take<int>(nvec);
+    if (!X || !Q || !sig || !perm) return CT_ERR_OOM;
+
+    {
+        const int64_t tot = nvec * (len > nvec ? len : nvec);
+        int g = (int)ct_cdiv(tot, 256);
+        if (g > h->num_sms * 16) g = h->num_sms * 16;
+        if (g < 1) g = 1;
+        svd_init_kernel<<<g, 256, 0, h->stream>>>(M, m, n, cols, X, ldx, Q, nvec);
+        CT_LAUNCH_CHECK(h);
+    }
+    const double tol = 2.2204460492503131e-16 * sqrt((double)(len > 1 ? len : 1)) * 4.0;
+    const size_t small_bytes = (size_t)(nvec * len + nvec * nvec) * sizeof(double);
+    if (nvec >= 2) {
+        if (small_bytes <= 200 * 1024) {
+            static bool attr = false;
+            if (!attr) {
+                CT_CUDA(h, cudaFuncSetAttribute(svd_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                200 * 1024));
+                attr = true;
+            }
+            svd_small_kernel<<<1, SVD_NT, small_bytes, h->stream>>>(X, len, ldx, Q, (int)nvec, tol, SVD_MAX_SWEEPS,
+                                                                    h->d_status);
+            CT_LAUNCH_CHECK(h);
+        } else {
+            const int P = (int)(nvec + (nvec & 1));
+            int* d_rot = h->d_flags + FL_ROT;
+            bool converged = false;
+            for (int sweep = 0; sweep < SVD_MAX_SWEEPS; ++sweep) {
+                CT_CUDA(h, cudaMemsetAsync(d_rot, 0, sizeof(int), h->stream));
+                for (int r = 0; r < P - 1; ++r) {
+                    svd_round_kernel<<<P / 2, SVD_NT, 0, h->stream>>>(X, len, ldx, Q, nvec, P, r, tol, d_rot);
+                }
+                CT_LAUNCH_CHECK(h);
+                int rot = 0;
+                CT_CUDA(h, cudaMemcpyAsync(&rot, d_rot, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+                CT_CUDA(h, cudaStreamSynchronize(h->stream));
+                if (rot == 0) {
+                    converged = true;
+                    break;
+                }
+            }
+            if (!converged) {
+                ct_seterr(h, "Jacobi SVD did not converge in %d sweeps (%lld x %lld)", SVD_MAX_SWEEPS,
+                          (long long)m, (long long)n);
+                return CT_ERR_NOCONV;
+            }
+        }
+    }
+    svd_norms_kernel<<<(unsigned)ct_cdiv(nvec * 32, 256), 256, 0, h->stream>>>(X, len, ldx, nvec, sig);
+    svd_rank_kernel<<<(unsigned)ct_cdiv(nvec, 256), 256, 0, h->stream>>>(sig, nvec, perm);
+    svd_trunc_kernel<<<1, 32, 0, h->stream>>>(sig, perm, k, chi_max, eps_trunc, h->d_scalars, h->d_flags);
+    CT_LAUNCH_CHECK(h);
+    int chi = 0;
+    double sums[2];
+    CT_CUDA(h, cudaMemcpyAsync(&chi, h->d_flags + FL_CHI, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CT_CUDA(h, cudaMemcpyAsync(sums, h->d_scalars + SC_TMP0, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CT_CUDA(h, cudaStreamSynchronize(h->stream));
+    int st = 0;
+    CT_CUDA(h, cudaMemcpy(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st != 0) {
+        CT_CUDA(h, cudaMemset(h->d_status, 0, sizeof(int)));
+        ct_seterr(h, "device SVD reported status %d", st);
+        return st;
+    }
+    out->chi = chi;
+    out->sum_s2_all = sums[0];
+    out->sum_s2_kept = sums[1];
+    if (chi > 0) {
+        const int64_t tot = (m > n ? m : n) * (int64_t)chi;
+        int g = (int)ct_cdiv(tot, 256);
+        if (g > h->num_sms * 16) g = h->num_sms * 16;
+        if (g < 1) g = 1;
+        svd_gather_kernel<<<g, 256, 0, h->stream>>>(X, ldx, Q, nvec, sig, perm, h->d_flags, m, n, cols, mode, A, B,
+                                                    S);
+        CT_LAUNCH_CHECK(h);
+    }
+    return CT_OK;
+}

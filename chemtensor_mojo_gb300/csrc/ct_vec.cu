@@ -1,0 +1,502 @@
+// FP64 vector algebra of the Lanczos solver and the dense-tensor reductions.
+//
+// The reference reduces with one thread per 256-block summing serially and a
+// single thread summing the partials, then copies one scalar to the host and
+// synchronises per call (dense_tensor.mojo:142-210); its DMRG Lanczos moves
+// every Krylov vector to the host per step (dmrg.mojo:640-689).  Here every
+// reduction is a grid of 256-thread blocks doing warp-shuffle tree sums over
+// 16-byte loads, followed by a one-block finisher that sums the partials in a
+// fixed order (bitwise reproducible) and runs the scalar epilogue on the
+// device (alpha, beta, the breakdown test, 1/norm), so a whole Lanczos run is
+// enqueued without a host round trip.
+#include "ct_common.cuh"
+
+namespace {
+
+constexpr int RT = 256;
+
+__device__ __forceinline__ bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+
+// ---- phase 1: per-block partial sums --------------------------------------
+// mode 0: sum x*y, mode 1: sum x*x
+template <int MODE>
+__global__ void __launch_bounds__(RT) partial_kernel(int64_t n, const double* __restrict__ x,
+                                                     const double* __restrict__ y, double* partials,
+                                                     const int* skip) {
+    if (ct_skip(skip)) return;
+    __shared__ double sm[32];
+    double acc = 0.0;
+    const int64_t stride = (int64_t)gridDim.x * RT;
+    int64_t start = (int64_t)blockIdx.x * RT + threadIdx.x;
+    const bool vec = aligned16(x) && (MODE == 1 || aligned16(y));
+    if (vec) {
+        const int64_t n2 = n / 2;
+        const double2* x2 = reinterpret_cast<const double2*>(x);
+        const double2* y2 = reinterpret_cast<const double2*>(y);
+        for (int64_t i = start; i < n2; i += stride) {
+            const double2 a = x2[i];
+            if (MODE == 0) {
+                const double2 b = y2[i];
+                acc = fma(a.x, b.x, acc);
+                acc = fma(a.y, b.y, acc);
+            } else {
+                acc = fma(a.x, a.x, acc);
+                acc = fma(a.y, a.y, acc);
+            }
+        }
+        if ((n & 1) && start == 0) {
+            const double a = x[n - 1];
+            acc = fma(a, MODE == 0 ? y[n - 1] : a, acc);
+        }
+    } else {
+        for (int64_t i = start; i < n; i += stride) {
+            const double a = x[i];
+            acc = fma(a, MODE == 0 ? y[i] : a, acc);
+        }
+    }
+    acc = ct_block_sum<RT>(acc, sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+}
+
+__device__ double finish_sum(const double* partials, int np, double* sm) {
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < np; i += RT) acc += partials[i];
+    return ct_block_sum<RT>(acc, sm);
+}
+
+// ---- phase 2 finishers ------------------------------------------------------
+__global__ void __launch_bounds__(RT) finish_store_kernel(const double* partials, int np, double* out,
+                                                          const int* skip) {
+    if (ct_skip(skip)) return;
+    __shared__ double sm[32];
+    const double s = finish_sum(partials, np, sm);
+    if (threadIdx.x == 0) *out = s;
+}
+
+int grid_for(ct_handle* h, int64_t n) {
+    int64_t g = ct_cdiv(n, (int64_t)RT * 8);
+    const int64_t cap = (int64_t)h->num_sms * 8;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    if (g > CT_NPARTIALS) g = CT_NPARTIALS;
+    return (int)g;
+}
+
+// ---- elementwise -------------------------------------------------------------
+__global__ void axpy_kernel(int64_t n, double alpha, const double* x, double* y) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = fma(alpha, x[i], y[i]);
+}
+__global__ void scale_kernel(int64_t n, double alpha, double* x) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] *= alpha;
+}
+__global__ void fill_kernel(double* x, int64_t n, double v) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = v;
+}
+// y = x / sqrt(*nsq); status zero_code when sqrt(nsq) < 1e-14 (dmrg.mojo:605-611)
+__global__ void scale_inv_sqrt_kernel(int64_t n, const double* x, double* y, const double* nsq,
+                                      const int* skip, int* status, int zero_code) {
+    if (ct_skip(skip)) return;
+    const double nrm = sqrt(*nsq);
+    const bool zero = !(nrm >= 1e-14);
+    if (zero) {
+        if (blockIdx.x == 0 && threadIdx.x == 0 && zero_code != 0) ct_set_status(status, zero_code);
+    }
+    const double inv = zero ? 0.0 : 1.0 / nrm;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = x[i] * inv;
+}
+
+__global__ void identity_env_kernel(double* E, int64_t w, int64_t D) {
+    const int64_t n = w * D * D;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = (t / D) % D, c = t % D;
+        E[t] = (r == c) ? 1.0 : 0.0;
+    }
+}
+
+struct PermArgs {
+    int rank;
+    int64_t n;
+    int64_t out_shape[6];
+    int64_t in_stride_of_out_axis[6];
+};
+__global__ void permute_kernel(const double* in, double* out, PermArgs a) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < a.n; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t rem = t, src = 0;
+        for (int ax = a.rank - 1; ax >= 0; --ax) {
+            const int64_t idx = rem % a.out_shape[ax];
+            rem /= a.out_shape[ax];
+            src += idx * a.in_stride_of_out_axis[ax];
+        }
+        out[t] = in[src];
+    }
+}
+
+// ---- Lanczos -------------------------------------------------------------------
+// alpha_j = <v_j, w>   -> scalars[SC_ALPHA + j]
+__global__ void __launch_bounds__(RT) lanczos_alpha_finish(const double* partials, int np, double* scalars,
+                                                           int j, const int* skip) {
+    if (ct_skip(skip)) return;
+    __shared__ double sm[32];
+    const double s = finish_sum(partials, np, sm);
+    if (threadIdx.x == 0) scalars[SC_ALPHA + j] = s;
+}
+
+// w -= alpha_j v_j + beta_{j-1} v_{j-1}; partial |w|^2
+__global__ void __launch_bounds__(RT) lanczos_update_kernel(int64_t n, double* w, const double* vj,
+                                                            const double* vjm1, const double* scalars,
+                                                            int j, double* partials, const int* skip) {
+    if (ct_skip(skip)) return;
+    __shared__ double sm[32];
+    const double a = scalars[SC_ALPHA + j];
+    const double b = (j > 0) ? scalars[SC_BETA + j - 1] : 0.0;
+    double acc = 0.0;
+    const int64_t stride = (int64_t)gridDim.x * RT;
+    for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) {
+        double x = w[i] - a * vj[i];
+        if (vjm1) x -= b * vjm1[i];
+        w[i] = x;
+        acc = fma(x, x, acc);
+    }
+    acc = ct_block_sum<RT>(acc, sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+}
+
+// beta_j = sqrt(sum); breakdown test beta < 100 n eps (dmrg.mojo:630-673)
+__global__ void __launch_bounds__(RT) lanczos_beta_finish(const double* partials, int np, double* scalars,
+                                                          int* flags, int j, double thr, const int* skip) {
+    if (ct_skip(skip)) return;
+    __shared__ double sm[32];
+    const double s = finish_sum(partials, np, sm);
+    if (threadIdx.x == 0) {
+        const double b = sqrt(s);
+        if (b < thr) {
+            flags[FL_NUMITER] = j + 1;
+            flags[FL_STOP] = 1;
+        } else {
+            scalars[SC_BETA + j] = b;
+        }
+    }
+}
+
+__global__ void lanczos_next_kernel(int64_t n, const double* w, double* vnext, const double* scalars, int j,
+                                    const int* skip) {
+    if (ct_skip(skip)) return;
+    const double inv = 1.0 / scalars[SC_BETA + j];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        vnext[i] = w[i] * inv;
+}
+
+// reorthogonalisation: coeff[v] = <V[v], w>  (partials laid out [block][nvec])
+__global__ void __launch_bounds__(RT) multidot_kernel(int64_t n, const double* w, const double* V, int64_t ldv,
+                                                      int nvec, double* partials, const int* skip) {
+    if (ct_skip(skip)) return;
+    __shared__ double sm[32];
+    const int64_t stride = (int64_t)gridDim.x * RT;
+    for (int v = 0; v < nvec; ++v) {
+        double acc = 0.0;
+        const double* x = V + (int64_t)v * ldv;
+        for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) acc = fma(x[i], w[i], acc);
+        acc = ct_block_sum<RT>(acc, sm);
+        if (threadIdx.x == 0) partials[(int64_t)blockIdx.x * nvec + v] = acc;
+    }
+}
+__global__ void __launch_bounds__(RT) multidot_finish(const double* partials, int np, int nvec, double* coeff,
+                                                      const int* skip) {
+    if (ct_skip(skip)) return;
+    __shared__ double sm[32];
+    for (int v = 0; v < nvec; ++v) {
+        double acc = 0.0;
+        for (int b = threadIdx.x; b < np; b += RT) acc += partials[(int64_t)b * nvec + v];
+        acc = ct_block_sum<RT>(acc, sm);
+        if (threadIdx.x == 0) coeff[v] = acc;
+    }
+}
+__global__ void __launch_bounds__(RT) multiaxpy_norm_kernel(int64_t n, double* w, const double* V, int64_t ldv,
+                                                            int nvec, const double* coeff, double* partials,
+                                                            const int* skip) {
+    if (ct_skip(skip)) return;
+    __shared__ double sm[32];
+    __shared__ double c[CT_MAX_KRYLOV];
+    for (int v = threadIdx.x; v < nvec; v += RT) c[v] = coeff[v];
+    __syncthreads();
+    double acc = 0.0;
+    const int64_t stride = (int64_t)gridDim.x * RT;
+    for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) {
+        double x = w[i];
+        for (int v = 0; v < nvec; ++v) x -= c[v] * V[(int64_t)v * ldv + i];
+        w[i] = x;
+        acc = fma(x, x, acc);
+    }
+    acc = ct_block_sum<RT>(acc, sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+}
+
+// Ritz vector: out = sum_{i < numiter} c_i V[i]
+__global__ void ritz_kernel(int64_t n, const double* V, int64_t ldv, const double* scalars, const int* flags,
+                            double* out) {
+    const int nk = flags[FL_NUMITER];
+    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int i = 0; i < nk; ++i) acc = fma(scalars[SC_RITZ + i], V[(int64_t)i * ldv + x], acc);
+        out[x] = acc;
+    }
+}
+
+// Classical Jacobi on the nK x nK tridiagonal matrix (dmrg.mojo:507-598),
+// one warp, T and V in shared memory.  Pivot: largest |T[i][j]| (i<j) with
+// the first occurrence in row-major order winning ties, like the reference's
+// strict '>' scan from (0,1).
+__global__ void tridiag_jacobi_kernel(double* scalars, int* flags, int* status, double tol, int max_rot,
+                                      int converged_mode) {
+    extern __shared__ double tsm[];
+    const int n = flags[FL_NUMITER];
+    const int lane = threadIdx.x;
+    if (n <= 0) {
+        if (lane == 0) ct_set_status(status, CT_ERR_INVALID);
+        return;
+    }
+    double* A = tsm;           // n x n
+    double* V = tsm + n * n;   // n x n
+    for (int t = lane; t < n * n; t += 32) {
+        const int i = t / n, j = t % n;
+        double a = 0.0;
+        if (i == j) a = scalars[SC_ALPHA + i];
+        else if (j == i + 1) a = scalars[SC_BETA + i];
+        else if (i == j + 1) a = scalars[SC_BETA + j];
+        A[t] = a;
+        V[t] = (i == j) ? 1.0 : 0.0;
+    }
+    __syncwarp();
+    if (n == 1) {
+        if (lane == 0) {
+            scalars[SC_ENERGY] = A[0];
+            scalars[SC_RITZ] = 1.0;
+        }
+        return;
+    }
+    bool done = false;
+    for (int rot = 0; rot < max_rot; ++rot) {
+        // pivot search
+        double best = -1.0;
+        int bidx = 0x7fffffff;
+        for (int i = lane; i < n; i += 32) {
+            for (int j = i + 1; j < n; ++j) {
+                const double v = fabs(A[i * n + j]);
+                if (v > best) { best = v; bidx = i * n + j; }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+            if (ob > best || (ob == best && oi < bidx)) { best = ob; bidx = oi; }
+        }
+        if (best < tol) { done = true; break; }
+        const int p = bidx / n, q = bidx % n;
+        const double app = A[p * n + p], aqq = A[q * n + q], apq = A[p * n + q];
+        const double phi = 0.5 * atan2(2.0 * apq, aqq - app);
+        const double c = cos(phi), s = sin(phi);
+        __syncwarp();
+        for (int k = lane; k < n; k += 32) {
+            if (k != p && k != q) {
+                const double aik = A[k * n + p], akq = A[k * n + q];
+                const double nkp = c * aik - s * akq;
+                const double nkq = s * aik + c * akq;
+                A[k * n + p] = nkp; A[p * n + k] = nkp;
+                A[k * n + q] = nkq; A[q * n + k] = nkq;
+            }
+            const double vip = V[k * n + p], viq = V[k * n + q];
+            V[k * n + p] = c * vip - s * viq;
+            V[k * n + q] = s * vip + c * viq;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            A[p * n + p] = c * c * app - 2.0 * s * c * apq + s * s * aqq;
+            A[q * n + q] = s * s * app + 2.0 * s * c * apq + c * c * aqq;
+            A[p * n + q] = 0.0;
+            A[q * n + p] = 0.0;
+        }
+        __syncwarp();
+    }
+    if (converged_mode && !done && lane == 0) ct_set_status(status, CT_ERR_NOCONV);
+    if (lane == 0) {
+        int mi = 0;
+        double mv = A[0];
+        for (int i = 1; i < n; ++i)
+            if (A[i * n + i] < mv) { mv = A[i * n + i]; mi = i; }
+        double nrm = 0.0;
+        for (int i = 0; i < n; ++i) nrm += V[i * n + mi] * V[i * n + mi];
+        nrm = sqrt(nrm);
+        for (int i = 0; i < n; ++i) scalars[SC_RITZ + i] = (nrm > 0.0) ? V[i * n + mi] / nrm : V[i * n + mi];
+        scalars[SC_ENERGY] = mv;
+    }
+}
+
+__global__ void init_lanczos_flags(int* flags, int max_iter) {
+    flags[FL_STOP] = 0;
+    flags[FL_NUMITER] = max_iter;
+}
+
+int elem_grid(ct_handle* h, int64_t n) {
+    int64_t g = ct_cdiv(n, 256);
+    const int64_t cap = (int64_t)h->num_sms * 16;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+}  // namespace
+
+int ct_reduce_dot(ct_handle* h, int64_t n, const double* x, const double* y, double* d_out, const int* skip) {
+    const int g = grid_for(h, n);
+    partial_kernel<0><<<g, RT, 0, h->stream>>>(n, x, y, h->d_partials, skip);
+    finish_store_kernel<<<1, RT, 0, h->stream>>>(h->d_partials, g, d_out, skip);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_reduce_nrm2sq(ct_handle* h, int64_t n, const double* x, double* d_out, const int* skip) {
+    const int g = grid_for(h, n);
+    partial_kernel<1><<<g, RT, 0, h->stream>>>(n, x, nullptr, h->d_partials, skip);
+    finish_store_kernel<<<1, RT, 0, h->stream>>>(h->d_partials, g, d_out, skip);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_scale_by_inv_sqrt(ct_handle* h, int64_t n, const double* x, double* y, const double* d_nsq,
+                         const int* skip, int zero_code) {
+    scale_inv_sqrt_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, x, y, d_nsq, skip, h->d_status, zero_code);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_fill(ct_handle* h, double* x, int64_t n, double v) {
+    if (n <= 0) return CT_OK;
+    fill_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(x, n, v);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_copy(ct_handle* h, double* dst, const double* src, int64_t n) {
+    if (n <= 0) return CT_OK;
+    CT_CUDA(h, cudaMemcpyAsync(dst, src, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    return CT_OK;
+}
+
+int ct_identity_env(ct_handle* h, double* E, int64_t w, int64_t D) {
+    const int64_t n = w * D * D;
+    if (n <= 0) return CT_OK;
+    identity_env_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(E, w, D);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_permute_launch(ct_handle* h, const double* in, double* out, int rank, const int64_t* shape,
+                      const int32_t* perm) {
+    if (rank < 1 || rank > 6) return CT_ERR_INVALID;
+    PermArgs a;
+    a.rank = rank;
+    int64_t in_stride[6];
+    int64_t s = 1;
+    for (int ax = rank - 1; ax >= 0; --ax) {
+        in_stride[ax] = s;
+        s *= shape[ax];
+    }
+    a.n = s;
+    bool seen[6] = {false, false, false, false, false, false};
+    for (int ax = 0; ax < rank; ++ax) {
+        const int p = perm[ax];
+        if (p < 0 || p >= rank || seen[p]) return CT_ERR_INVALID;
+        seen[p] = true;
+        a.out_shape[ax] = shape[p];
+        a.in_stride_of_out_axis[ax] = in_stride[p];
+    }
+    if (a.n == 0) return CT_OK;
+    permute_kernel<<<elem_grid(h, a.n), 256, 0, h->stream>>>(in, out, a);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_vec_axpy_launch(ct_handle* h, int64_t n, double alpha, const double* x, double* y) {
+    axpy_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, alpha, x, y);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+int ct_vec_scale_launch(ct_handle* h, int64_t n, double alpha, double* x) {
+    scale_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, alpha, x);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_lanczos_init(ct_handle* h, int max_iter) {
+    init_lanczos_flags<<<1, 1, 0, h->stream>>>(h->d_flags, max_iter);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_lanczos_alpha(ct_handle* h, int64_t n, const double* vj, const double* w, int j, const int* skip) {
+    const int g = grid_for(h, n);
+    partial_kernel<0><<<g, RT, 0, h->stream>>>(n, vj, w, h->d_partials, skip);
+    lanczos_alpha_finish<<<1, RT, 0, h->stream>>>(h->d_partials, g, h->d_scalars, j, skip);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_lanczos_update(ct_handle* h, int64_t n, double* w, const double* vj, const double* vjm1, int j,
+                      double beta_threshold, const int* skip) {
+    const int g = grid_for(h, n);
+    lanczos_update_kernel<<<g, RT, 0, h->stream>>>(n, w, vj, vjm1, h->d_scalars, j, h->d_partials, skip);
+    lanczos_beta_finish<<<1, RT, 0, h->stream>>>(h->d_partials, g, h->d_scalars, h->d_flags, j,
+                                                 beta_threshold, skip);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+// Full reorthogonalisation of w against V[0..nvec) followed by the beta
+// decision.  Runs after ct_lanczos_update (whose beta it overwrites).
+int ct_lanczos_reorth_beta(ct_handle* h, int64_t n, double* w, const double* V, int64_t ldv, int nvec, int j,
+                           double beta_threshold, const int* skip) {
+    if (nvec > CT_MAX_KRYLOV) return CT_ERR_UNSUPPORTED;
+    int g = grid_for(h, n);
+    if ((int64_t)g * nvec > CT_NPARTIALS) g = CT_NPARTIALS / nvec;
+    double* coeff = h->d_scalars + SC_MISC;
+    multidot_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, h->d_partials, skip);
+    multidot_finish<<<1, RT, 0, h->stream>>>(h->d_partials, g, nvec, coeff, skip);
+    multiaxpy_norm_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, coeff, h->d_partials, skip);
+    lanczos_beta_finish<<<1, RT, 0, h->stream>>>(h->d_partials, g, h->d_scalars, h->d_flags, j,
+                                                 beta_threshold, skip);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_lanczos_next(ct_handle* h, int64_t n, const double* w, double* vnext, int j, const int* skip) {
+    lanczos_next_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, w, vnext, h->d_scalars, j, skip);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_tridiag_eig(ct_handle* h, int max_iter, double tol, int max_rotations) {
+    if (max_iter > 64) return CT_ERR_UNSUPPORTED;
+    const size_t smem = 2 * (size_t)max_iter * max_iter * sizeof(double);
+    static bool attr = false;
+    if (!attr) {
+        CT_CUDA(h, cudaFuncSetAttribute(tridiag_jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        2 * 64 * 64 * 8));
+        attr = true;
+    }
+    const int converged = (max_rotations <= 0);
+    const int cap = converged ? 200000 : max_rotations;
+    tridiag_jacobi_kernel<<<1, 32, smem, h->stream>>>(h->d_scalars, h->d_flags, h->d_status, tol, cap, converged);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_ritz(ct_handle* h, int64_t n, const double* V, int64_t ldv, double* out) {
+    ritz_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, V, ldv, h->d_scalars, h->d_flags, out);
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}

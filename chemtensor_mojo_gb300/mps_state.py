@@ -1,0 +1,231 @@
+"""MPS and MPO containers: the host side of src/state/mps_state.mojo and
+src/state/mpo_state.mojo, plus the seeded initial states.
+
+* ``MPSSite`` / ``MatrixProductState``          mps_state.mojo:13-167
+* ``create_product_mps``                        mps_state.mojo:258-304
+* ``create_uniform_mps``                        mps_state.mojo:220-255 (seeded here)
+* ``create_random_mps_c_compatible``            rng_c_compat.mojo:174-231, run natively
+* ``mps_right_normalize``                       device SVD sweep (no working
+                                                reference counterpart)
+* ``mps_to_statevector`` / ``mps_norm``         mps_state.mojo:454-508
+* ``MPOSite`` / ``MatrixProductOperator``       mpo_state.mojo:10-193
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import List, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+from .dense_tensor import (DenseTensor, DeviceContext, create_dense_tensor_from_data, dense_tensor_dot,
+                           create_dense_tensor, get_context, _ptr)
+
+
+class MPSSite:
+    """Rank-3 site tensor [left_bond, physical, right_bond]."""
+
+    def __init__(self, tensor: DenseTensor):
+        self.tensor = tensor
+
+    def _assert_rank3(self):
+        if len(self.tensor.shape) != 3:
+            raise ValueError(f"MPSSite expects rank-3 tensors [bond_left, physical, bond_right], got rank "
+                             f"{len(self.tensor.shape)}")
+
+    def rank(self) -> int:
+        return len(self.tensor.shape)
+
+    def shape(self) -> List[int]:
+        return list(self.tensor.shape)
+
+    def physical_dim(self) -> int:
+        self._assert_rank3()
+        return self.tensor.shape[1]
+
+    def left_bond_dim(self) -> int:
+        self._assert_rank3()
+        return self.tensor.shape[0]
+
+    def right_bond_dim(self) -> int:
+        self._assert_rank3()
+        return self.tensor.shape[2]
+
+
+class MatrixProductState:
+    def __init__(self, sites: Sequence[MPSSite]):
+        if len(sites) == 0:
+            raise ValueError("MatrixProductState requires at least one site tensor")
+        phys = sites[0].physical_dim()
+        bonds = [sites[0].left_bond_dim()]
+        for idx, site in enumerate(sites):
+            if site.physical_dim() != phys:
+                raise ValueError("All MPS sites must have the same physical dimension")
+            if idx > 0 and site.left_bond_dim() != sites[idx - 1].right_bond_dim():
+                raise ValueError(f"Bond mismatch between sites {idx - 1} and {idx}")
+            bonds.append(site.right_bond_dim())
+        self.sites = list(sites)
+        self.physical_dim = phys
+        self.length = len(self.sites)
+        self.bond_dims = bonds
+
+    def num_sites(self) -> int:
+        return self.length
+
+    def bond_dimension(self, index: int) -> int:
+        return self.bond_dims[index]
+
+    def site_shape(self, index: int) -> List[int]:
+        return self.sites[index].shape()
+
+    def describe(self) -> None:
+        print(f"MatrixProductState(length={self.length}, physical_dim={self.physical_dim})")
+        print("  bond_dims:", self.bond_dims)
+
+    def to_numpy(self) -> List[np.ndarray]:
+        return [s.tensor.to_numpy() for s in self.sites]
+
+
+class MPOSite:
+    """Rank-4 site tensor [Wl, d_in, d_out, Wr]."""
+
+    def __init__(self, tensor: DenseTensor):
+        if len(tensor.shape) != 4:
+            raise ValueError("MPOSite expects rank-4 tensors [Wl, d_in, d_out, Wr]")
+        self.tensor = tensor
+
+    def left_bond_dim(self) -> int:
+        return self.tensor.shape[0]
+
+    def right_bond_dim(self) -> int:
+        return self.tensor.shape[3]
+
+    def physical_in_dim(self) -> int:
+        return self.tensor.shape[1]
+
+    def physical_out_dim(self) -> int:
+        return self.tensor.shape[2]
+
+
+class MatrixProductOperator:
+    def __init__(self, sites: Sequence[MPOSite]):
+        if len(sites) == 0:
+            raise ValueError("MatrixProductOperator requires at least one site")
+        for i in range(1, len(sites)):
+            if sites[i].left_bond_dim() != sites[i - 1].right_bond_dim():
+                raise ValueError(f"MPO bond mismatch between sites {i - 1} and {i}")
+        self.sites = list(sites)
+        self.length = len(self.sites)
+        self.bond_dims = [sites[0].left_bond_dim()] + [s.right_bond_dim() for s in sites]
+
+    def num_sites(self) -> int:
+        return self.length
+
+    def bond_dimension(self, index: int) -> int:
+        return self.bond_dims[index]
+
+    def to_numpy(self) -> List[np.ndarray]:
+        return [s.tensor.to_numpy() for s in self.sites]
+
+
+def mpo_from_arrays(ctx, arrays: Sequence[np.ndarray]) -> MatrixProductOperator:
+    return MatrixProductOperator([MPOSite(create_dense_tensor_from_data(ctx, a, a.shape)) for a in arrays])
+
+
+def mps_from_arrays(ctx, arrays: Sequence[np.ndarray]) -> MatrixProductState:
+    return MatrixProductState([MPSSite(create_dense_tensor_from_data(ctx, a, a.shape)) for a in arrays])
+
+
+# -- creators ---------------------------------------------------------------------
+def create_product_mps(ctx, physical_dim: int, basis: Sequence[int]) -> MatrixProductState:
+    if len(basis) < 1:
+        raise ValueError("basis must contain at least one element")
+    if physical_dim < 1:
+        raise ValueError("physical_dim must be >= 1")
+    sites = []
+    for i, choice in enumerate(basis):
+        if choice < 0 or choice >= physical_dim:
+            raise ValueError(f"Invalid basis index {choice} at site {i} (must be in [0, physical_dim))")
+        data = np.zeros(physical_dim)
+        data[choice] = 1.0
+        sites.append(MPSSite(create_dense_tensor_from_data(ctx, data, [1, physical_dim, 1])))
+    return MatrixProductState(sites)
+
+
+def create_uniform_mps(ctx, num_sites: int, physical_dim: int, bond_dims: Sequence[int],
+                       init_value: float | None = None, seed: int = 0) -> MatrixProductState:
+    if num_sites < 1:
+        raise ValueError("num_sites must be >= 1")
+    if physical_dim < 1:
+        raise ValueError("physical_dim must be >= 1")
+    if len(bond_dims) != num_sites + 1:
+        raise ValueError("bond_dims must have length num_sites + 1")
+    g = np.random.default_rng(seed)
+    sites = []
+    for i in range(num_sites):
+        dl, dr = bond_dims[i], bond_dims[i + 1]
+        if dl < 1 or dr < 1:
+            raise ValueError("Bond dimensions must be >= 1")
+        shape = [dl, physical_dim, dr]
+        if init_value is None:
+            a = g.random(shape) / np.sqrt(dl * physical_dim * dr)
+        else:
+            a = np.full(shape, float(init_value))
+        sites.append(MPSSite(create_dense_tensor_from_data(ctx, a, shape)))
+    return MatrixProductState(sites)
+
+
+def random_mps_c_compatible_arrays(nsites: int, d: int, chi_max: int, seed: int):
+    """Host arrays of create_random_mps_c_compatible (native PCG32 + Box-Muller)."""
+    lib = _lib.load()
+    dims = (C.c_int64 * (nsites + 1))()
+    _lib.check(lib.ct_random_mps_host(nsites, d, chi_max, C.c_uint64(seed), dims, None), "ct_random_mps_host")
+    dims_l = [int(x) for x in dims]
+    arrays = [np.empty((dims_l[i], d, dims_l[i + 1]), dtype=np.float64) for i in range(nsites)]
+    pp, keep = _lib.ptr_array([a.ctypes.data for a in arrays])
+    _lib.check(lib.ct_random_mps_host(nsites, d, chi_max, C.c_uint64(seed), dims, pp), "ct_random_mps_host")
+    return arrays, dims_l
+
+
+def create_random_mps_c_compatible(ctx, nsites: int, d: int, chi_max: int, seed: int) -> MatrixProductState:
+    arrays, _ = random_mps_c_compatible_arrays(nsites, d, chi_max, seed)
+    return mps_from_arrays(ctx, arrays)
+
+
+def mps_right_normalize(ctx, mps: MatrixProductState) -> MatrixProductState:
+    """Right-canonical form on the device (SVD sweep from the right, no truncation)."""
+    ctx = ctx or get_context()
+    n = mps.num_sites()
+    bd = _lib.i64_array(mps.bond_dims)
+    tensors = [s.tensor.storage.clone() for s in mps.sites]
+    pp, keep = _lib.ptr_array([t.data_ptr() for t in tensors])
+    ctx.call("ct_mps_right_normalize", n, mps.physical_dim, bd, pp)
+    dims = [int(x) for x in bd]
+    sites = [MPSSite(DenseTensor(tensors[i], [dims[i], mps.physical_dim, dims[i + 1]])) for i in range(n)]
+    return MatrixProductState(sites)
+
+
+def mps_to_statevector(psi: MatrixProductState, ctx: DeviceContext | None = None) -> DenseTensor:
+    """Row-major contraction to the full vector (small L only), mps_state.mojo:454-492."""
+    ctx = ctx or get_context()
+    res = psi.sites[0].tensor
+    left = res.shape[0] * res.shape[1]
+    right = res.shape[2]
+    res = res.reshape([left, right])
+    for i in range(1, psi.num_sites()):
+        site = psi.sites[i].tensor
+        Di, di, Dn = site.shape
+        if right != Di:
+            raise ValueError("Bond dimension mismatch in mps_to_statevector")
+        out = create_dense_tensor(ctx, [left, di * Dn])
+        dense_tensor_dot(out, res, site.reshape([Di, di * Dn]), ctx)
+        left, right = left * di, Dn
+        res = out.reshape([left, right])
+    if right != 1:
+        raise ValueError("Expected trailing bond dimension 1 in mps_to_statevector")
+    return res.reshape([left])
+
+
+def mps_norm(psi: MatrixProductState, ctx: DeviceContext | None = None) -> float:
+    return mps_to_statevector(psi, ctx).norm(ctx)

@@ -1,0 +1,210 @@
+/*
+ * ctdmrg.h -- C ABI of libctdmrg.so, the GB300 (sm_103a) two-site DMRG path.
+ *
+ * Conventions (the same as the reference's native shim, native/svd_shim.c:1-23):
+ *   - every entry point returns an int status: CT_OK (0) or a negative CT_ERR_*;
+ *   - every tensor pointer is a caller-owned DEVICE pointer to a row-major,
+ *     contiguous FP64 array in the reference layouts
+ *         MPS site  A[Dl, d, Dr]            (src/state/mps_state.mojo:13-49)
+ *         MPO site  W[wl, d_in, d_out, wr]  (src/state/mpo_state.mojo:10-54)
+ *         env       E[w, D_ket, D_bra]      (src/state/environments.mojo:110-131)
+ *         theta     th[Dl, d, d, Dr]        (src/algorithms/dmrg.mojo:93-140)
+ *     unless a parameter says it is a host pointer (suffix _host);
+ *   - scratch memory is owned by the handle; a handle is not thread-safe,
+ *     use one handle per host thread;
+ *   - all work is enqueued on the handle's stream; entry points that return a
+ *     host scalar synchronise that stream.
+ *
+ * Precision forms (ct_prec):
+ *   CT_PREC_FP64    plain form, FP64 everywhere.
+ *   CT_PREC_TF32X3  contractions on tcgen05 tensor cores in TF32 with
+ *                   3xTF32 split compensation and FP32 accumulation; all
+ *                   storage, Lanczos, eigensolve, SVD and reductions FP64.
+ */
+#ifndef CTDMRG_H
+#define CTDMRG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CTDMRG_VERSION 1
+
+#if defined(__GNUC__)
+#define CT_API __attribute__((visibility("default")))
+#else
+#define CT_API
+#endif
+
+enum ct_status {
+    CT_OK = 0,
+    CT_ERR_INVALID = -1,     /* bad argument (null pointer, bad enum)            */
+    CT_ERR_CUDA = -2,        /* a CUDA runtime call failed                       */
+    CT_ERR_OOM = -3,         /* device allocation failed / allocation limit hit  */
+    CT_ERR_NOCONV = -4,      /* an iterative device solver hit its iteration cap */
+    CT_ERR_ZERO_NORM = -5,   /* Lanczos start vector has zero norm               */
+    CT_ERR_SHAPE = -6,       /* inconsistent shapes                              */
+    CT_ERR_UNSUPPORTED = -7, /* shape/precision not supported by this build      */
+    CT_ERR_NONFINITE = -8,   /* NaN/Inf met in a reduction                       */
+    CT_ERR_EMPTY = -9        /* truncation kept zero singular values             */
+};
+
+enum ct_prec { CT_PREC_FP64 = 0, CT_PREC_TF32X3 = 1 };
+
+typedef struct ct_handle ct_handle;
+
+/* ---- lifecycle (no reference counterpart: MAX's DeviceContext, dmrg.mojo:2) */
+CT_API int ct_create(int device, void* stream, ct_handle** out);
+CT_API int ct_destroy(ct_handle* h);
+CT_API int ct_set_stream(ct_handle* h, void* stream);
+CT_API int ct_synchronize(ct_handle* h);
+/* reads and clears the device status word (sticky first error of a kernel) */
+CT_API int ct_get_status(ct_handle* h, int* status_out);
+CT_API const char* ct_error_string(int status);
+CT_API const char* ct_last_error(ct_handle* h);
+CT_API int ct_version(void);
+/* bytes of handle-owned scratch currently reserved */
+CT_API int ct_workspace_bytes(ct_handle* h, int64_t* bytes_out);
+/* cap on handle-owned scratch in bytes (0 = unlimited); growth beyond it -> CT_ERR_OOM */
+CT_API int ct_set_workspace_limit(ct_handle* h, int64_t bytes);
+
+/* ---- dense tensor core (src/m_tensor/dense_tensor.mojo) --------------------
+ * Row-major C[m,n] = alpha * op(A) op(B) + beta * C, op = identity or transpose.
+ * The 2-D core of dense_tensor_dot (dense_tensor.mojo:963-1328); the axis
+ * bookkeeping of dense_tensor_dot lives in the host layer.               */
+CT_API int ct_gemm(ct_handle* h, int prec, int trans_a, int trans_b, int64_t m, int64_t n, int64_t k,
+            double alpha, const double* A, int64_t lda, const double* B, int64_t ldb,
+            double beta, double* C, int64_t ldc);
+/* out[i] = in[perm-index] : physical N-D permute, rank <= 6
+ * (DenseTensor.transpose, dense_tensor.mojo:460-545)                       */
+CT_API int ct_permute(ct_handle* h, const double* in, double* out, int rank, const int64_t* shape,
+               const int32_t* perm);
+/* vector ops (dense_tensor.mojo:637-754): FP64 reductions on the device   */
+CT_API int ct_vec_dot(ct_handle* h, int64_t n, const double* x, const double* y, double* result_host);
+CT_API int ct_vec_norm_sq(ct_handle* h, int64_t n, const double* x, double* result_host);
+CT_API int ct_vec_axpy(ct_handle* h, int64_t n, double alpha, const double* x, double* y);
+CT_API int ct_vec_scale(ct_handle* h, int64_t n, double alpha, double* x);
+/* identity boundary environment E[w, D, D] (dmrg.mojo:74-84)              */
+CT_API int ct_env_identity(ct_handle* h, double* E, int64_t w, int64_t D);
+
+/* ---- two-site DMRG building blocks (src/algorithms/dmrg.mojo) ------------ */
+/* theta[Dl,d,d,Dr] = A_i[Dl*d, Dm] . A_ip1[Dm, d*Dr]  (build_two_site_theta, dmrg.mojo:93-140) */
+CT_API int ct_theta2(ct_handle* h, int prec, const double* A_i, const double* A_ip1, double* theta,
+              int64_t Dl, int64_t d, int64_t Dm, int64_t Dr);
+/* out = H_eff theta (apply_two_site_heff, dmrg.mojo:254-374).
+ * L[wL,Dl,Dl], R[wR,Dr,Dr], W1[wL,d,d,wM], W2[wM,d,d,wR].                  */
+CT_API int ct_heff2_apply(ct_handle* h, int prec, const double* theta, const double* L, const double* R,
+                   const double* W1, const double* W2, double* out, int64_t Dl, int64_t d,
+                   int64_t Dr, int64_t wL, int64_t wM, int64_t wR);
+/* Lnext[wR,Dr,Dr] from Lprev[wL,Dl,Dl], A[Dl,d,Dr], W[wL,d,d,wR]
+ * (update_left_environment, environments.mojo:99-201)                      */
+CT_API int ct_env_left(ct_handle* h, int prec, const double* Lprev, const double* A, const double* W,
+                double* Lnext, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR);
+/* Rprev[wL,Dl,Dl] from Rnext[wR,Dr,Dr], A[Dl,d,Dr], W[wL,d,d,wR]
+ * (update_right_environment, environments.mojo:309-417)                    */
+CT_API int ct_env_right(ct_handle* h, int prec, const double* Rnext, const double* A, const double* W,
+                 double* Rprev, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR);
+/* Lanczos ground state of H_eff (lanczos_two_site_optimize, dmrg.mojo:486-756).
+ * theta_in is not modified; theta_out gets the normalised Ritz vector.
+ * max_rotations: Jacobi rotation cap of the tridiagonal eigensolve (the
+ * reference uses 200, dmrg.mojo:510); 0 = run the same Jacobi to convergence.
+ * reorth != 0 adds full FP64 reorthogonalisation against the Krylov basis.
+ * alpha_host/beta_host (may be NULL) receive max_iter / max_iter-1 values.  */
+CT_API int ct_lanczos2(ct_handle* h, int prec, const double* theta_in, double* theta_out,
+                const double* L, const double* R, const double* W1, const double* W2,
+                int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wM, int64_t wR,
+                int max_iter, double tol, int max_rotations, int reorth,
+                double* energy_host, int* numiter_host, double* alpha_host, double* beta_host);
+/* Truncated thin SVD of a row-major M[m,n] on the device
+ * (dense_tensor_svd_trunc_lapack_f64, dense_tensor.mojo:1483-1592).
+ * Writes the kept factors compactly: U[m, chi], S[chi], Vt[chi, n] (row-major,
+ * capacity k = min(m,n) for chi), chi chosen by the reference rule.         */
+CT_API int ct_svd_trunc(ct_handle* h, const double* M, int64_t m, int64_t n, int64_t chi_max,
+                 double eps_trunc, double* U, double* S, double* Vt, int64_t* chi_host);
+/* Two-site split (split_two_site_theta_svd, dmrg.mojo:143-252).
+ * A_out[Dl,d,chi], B_out[chi,d,Dr] (capacity min(Dl*d, d*Dr) for chi),
+ * S_out (may be NULL) gets the kept singular values, descending.          */
+CT_API int ct_svd_split(ct_handle* h, const double* theta, int64_t Dl, int64_t d, int64_t Dr,
+                 int64_t chi_max, double eps_trunc, int left_to_right, double* A_out,
+                 double* B_out, double* S_out, int64_t* chi_host, double* discarded_host);
+
+/* ---- sweep driver (dmrg_two_site, dmrg.mojo:377-483) ---------------------- */
+typedef struct ct_dmrg_params {
+    int num_sweeps;
+    int chi_max;
+    double eps_trunc;
+    int max_krylov_iter;
+    double krylov_tol;
+    double energy_tol;
+    int two_site;        /* must be 1 (dmrg.mojo:416-417)                      */
+    int verbose;
+    int prec;            /* ct_prec                                            */
+    int max_rotations;   /* 200 = reference Jacobi cap; 0 = converged          */
+    int reorth;          /* full FP64 reorthogonalisation                      */
+} ct_dmrg_params;
+
+typedef struct ct_dmrg_stats {
+    double seconds_total;      /* host wall clock of the call                   */
+    double seconds_lanczos;    /* summed device time (CUDA events) per phase    */
+    double seconds_svd;
+    double seconds_env;
+    double heff_flops;         /* algorithmic FLOPs of all H_eff applies        */
+    double env_flops;
+    int64_t heff_applies;
+    int64_t local_updates;
+    double max_discarded;      /* largest discarded weight over the run         */
+} ct_dmrg_stats;
+
+/* Runs the sweeps in place.  mps_sites[i] are caller-owned device buffers of
+ * capacity site_capacity[i] doubles; bond_dims (length nsites+1) is read and
+ * updated.  mpo_sites[i] are device pointers, mpo_dims (length nsites+1) the
+ * MPO bond dimensions.  sweep_energies_host (length num_sweeps, may be NULL)
+ * gets the energy of every sweep run; discarded_host (length
+ * num_sweeps*2*(nsites-1), may be NULL) every local discarded weight.      */
+CT_API int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* params, int nsites, int d,
+                     const int64_t* mpo_dims, const double* const* mpo_sites,
+                     int64_t* bond_dims, double* const* mps_sites,
+                     const int64_t* site_capacity, double* energy_host,
+                     double* sweep_energies_host, int* sweeps_done_host,
+                     double* discarded_host, ct_dmrg_stats* stats_host);
+
+/* Right-canonicalise an MPS in place with device SVD splits (no truncation);
+ * site 0 is normalised.  No reference counterpart that works
+ * (mps_state.mojo:170-217 is dead code); the configs ask for a
+ * right-normalised start.                                                   */
+CT_API int ct_mps_right_normalize(ct_handle* h, int nsites, int d, int64_t* bond_dims,
+                           double* const* mps_sites);
+
+/* <psi|H|psi> and <psi|psi> through left environments on the device
+ * (expectation_value, environments.mojo:475-532).                           */
+CT_API int ct_mps_expectation(ct_handle* h, int prec, int nsites, int d, const int64_t* mpo_dims,
+                       const double* const* mpo_sites, const int64_t* bond_dims,
+                       const double* const* mps_sites, double* energy_host, double* norm_sq_host);
+
+/* ---- host-side seeded initial state (rng_c_compat.mojo:14-231) ------------
+ * Fills HOST buffers: sites[i] gets dims[i]*d*dims[i+1] doubles holding the
+ * float32 values of create_random_mps_c_compatible; dims (length nsites+1)
+ * is written.  With sites_host == NULL only dims is computed.               */
+CT_API int ct_random_mps_host(int nsites, int d, int chi_max, uint64_t seed, int64_t* dims,
+                       double* const* sites_host);
+/* first n values of randnf() for a seed (used by tests)                    */
+CT_API int ct_rng_randnf_host(uint64_t seed, int64_t n, float* out);
+
+/* ---- adjoint (no reference counterpart; spec item) ------------------
+ * Gradient of E(A) = <psi|H|psi>/<psi|psi> with respect to every site tensor
+ * of a (not necessarily canonical) MPS, by the hand-written adjoint of the
+ * environment chain.  grad_sites[i] are caller-owned device buffers shaped
+ * like mps_sites[i].  checkpoint_every > 0 stores only every k-th left
+ * environment and recomputes the others (memory ~ L/k environments).      */
+CT_API int ct_energy_grad(ct_handle* h, int prec, int nsites, int d, const int64_t* mpo_dims,
+                   const double* const* mpo_sites, const int64_t* bond_dims,
+                   const double* const* mps_sites, double* const* grad_sites,
+                   int checkpoint_every, double* energy_host);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CTDMRG_H */

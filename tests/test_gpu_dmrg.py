@@ -1,0 +1,119 @@
+"""Sweep-level parity of the FP64 device DMRG against the oracle and exact diagonalisation.
+
+* TFIM L=12 (J=h=1, chi<=32, 6 sweeps, 20 Lanczos steps, eps 1e-10) from the
+  seed-0 right-normalised random MPS: per-sweep energies equal the oracle's to
+  1e-10 relative and the bond dimensions are identical, in the reference's
+  capped-Jacobi semantics; the converged eigensolve matches ED to 1e-8.
+* 4-site XXX (test_dmrg_exact_small.mojo:17-65): E0 = -3.
+* Small Bose-Hubbard and Jordan-Wigner Fermi-Hubbard chains against ED.
+"""
+import numpy as np
+import pytest
+
+from oracle import dmrg as od
+from oracle import ed
+from oracle import hamiltonians as oh
+from oracle import rng as orng
+
+pytestmark = pytest.mark.gpu
+
+
+def ct_mod():
+    import chemtensor_mojo_gb300 as ct
+    return ct
+
+
+def run_device(ctx, mpo_arrays, mps_arrays, params):
+    ct = ct_mod()
+    mps = ct.mps_from_arrays(ctx, mps_arrays)
+    mpo = ct.mpo_from_arrays(ctx, mpo_arrays)
+    stats = ct.DMRGStats()
+    E, out = ct.dmrg_two_site(ctx, mpo, mps, params, stats)
+    return E, out, stats
+
+
+@pytest.fixture(scope="module")
+def tfim12():
+    L = 12
+    mpo = oh.ising_1d(L, J=1.0, h_longitudinal=0.0, g_transverse=1.0)
+    sites, dims = orng.create_random_mps_c_compatible(L, 2, 32, 0)
+    mps = od.right_normalize(sites)
+    return mpo, mps
+
+
+@pytest.mark.parametrize("max_rot", [200, 0])
+def test_tfim12_matches_oracle(ctx, tfim12, max_rot):
+    ct = ct_mod()
+    mpo, mps = tfim12
+    p = ct.DMRGParams(num_sweeps=6, chi_max=32, eps_trunc=1e-10, max_krylov_iter=20, krylov_tol=1e-10,
+                      energy_tol=0.0, max_rotations=max_rot)
+    E, out, stats = run_device(ctx, mpo, mps, p)
+    pref = od.DMRGParams(6, 32, 1e-10, 20, 1e-10, 0.0)
+    log = od.SweepLog()
+    E_ref, mps_ref = od.dmrg_two_site(mpo, mps, pref, eig="jacobi" if max_rot else "exact", log=log)
+    assert out.bond_dims == [1] + [a.shape[2] for a in mps_ref]
+    np.testing.assert_allclose(stats.sweep_energies, log.energies, rtol=1e-10, atol=0)
+    assert abs(E - E_ref) <= 1e-10 * abs(E_ref)
+    np.testing.assert_allclose(stats.discarded, log.discarded, atol=1e-12)
+    if max_rot == 0:
+        assert abs(E - ed.ground_energy(mpo)) < 1e-8
+
+
+def test_xxx_4site_exact(ctx):
+    """test_dmrg_exact_small.mojo:17-65 (Neel start, chi=8, 6 sweeps): E0 = -3."""
+    ct = ct_mod()
+    mpo = oh.heisenberg_xxz(4, J=1.0, D=1.0, h=0.0)
+    neel = []
+    for i in range(4):
+        a = np.zeros((1, 2, 1))
+        a[0, i % 2, 0] = 1.0
+        neel.append(a)
+    p = ct.DMRGParams(num_sweeps=6, chi_max=8, eps_trunc=1e-10, max_krylov_iter=20, krylov_tol=1e-8,
+                      energy_tol=1e-8)
+    E, out, _ = run_device(ctx, mpo, neel, p)
+    assert abs(E - (-3.0)) < 1e-10
+
+
+@pytest.mark.parametrize("model", ["bose_hubbard", "fermi_hubbard", "xxz"])
+def test_small_models_vs_ed(ctx, model):
+    ct = ct_mod()
+    if model == "bose_hubbard":
+        L, d = 6, 3
+        mpo = oh.bose_hubbard(L, d, t=1.0, u=4.0, mu=0.0)
+    elif model == "fermi_hubbard":
+        L, d = 6, 4
+        mpo = oh.fermi_hubbard(L, t=1.0, U=8.0)
+    else:
+        L, d = 10, 2
+        mpo = oh.spin_half_xxz(L, 1.0)
+    sites, _ = orng.create_random_mps_c_compatible(L, d, 64, 1)
+    mps = od.right_normalize(sites)
+    p = ct.DMRGParams(num_sweeps=6, chi_max=64, eps_trunc=1e-12, max_krylov_iter=24, krylov_tol=1e-12,
+                      energy_tol=0.0, max_rotations=0)
+    E, out, _ = run_device(ctx, mpo, mps, p)
+    assert abs(E - ed.ground_energy(mpo)) < 1e-8 * max(1.0, abs(E))
+
+
+def test_expectation_matches_energy(ctx, tfim12):
+    """Tier A of test_dmrg_gauge_safe.mojo:52-88: E_dmrg equals <psi|H|psi>/<psi|psi>."""
+    ct = ct_mod()
+    mpo, mps = tfim12
+    p = ct.DMRGParams(num_sweeps=4, chi_max=32, eps_trunc=1e-10, max_krylov_iter=20, krylov_tol=1e-10,
+                      energy_tol=0.0, max_rotations=0)
+    E, out, _ = run_device(ctx, mpo, mps, p)
+    E2 = ct.expectation_value_normalized(out, ct.mpo_from_arrays(ctx, mpo), ctx)
+    assert abs(E - E2) < 1e-8
+    ref = od.expectation(out.to_numpy(), mpo) / od.norm_sq(out.to_numpy())
+    assert abs(E2 - ref) < 1e-12
+
+
+def test_right_normalize_on_device(ctx):
+    ct = ct_mod()
+    arrays, dims = ct.random_mps_c_compatible_arrays(10, 2, 16, 3)
+    mps = ct.mps_right_normalize(ctx, ct.mps_from_arrays(ctx, arrays))
+    for a in mps.to_numpy()[1:]:
+        m = a.reshape(a.shape[0], -1)
+        assert np.allclose(m @ m.T, np.eye(a.shape[0]), atol=1e-12)
+    psi = ct.mps_to_statevector(mps, ctx).to_numpy()
+    psi0 = od.mps_to_statevector(arrays)
+    assert abs(abs(psi @ psi0) / np.linalg.norm(psi0) - 1.0) < 1e-12
