@@ -1,0 +1,410 @@
+#!/usr/bin/env python
+"""Benchmark of the two-site DMRG sweep on one GB300.
+
+Workload: open spin-1/2 Heisenberg chain H = sum (Sx Sx + Sy Sy + Delta Sz Sz),
+L=64, Delta=1, d=2, MPO bond dimension 5; seeded Gaussian initial MPS (bond
+dimensions min(2^k, 2^(L-k), 64), right-normalised); chi_max ramped
+64 -> 256 -> 1024, 24 Lanczos steps per bond, truncation 1e-10.
+
+A "step" is one full sweep (L->R then R->L, 126 local updates) at chi_max=1024.
+The W warm-up steps are the ramp sweeps (chi 64, 256, then 1024); the K timed
+sweeps run in one dmrg_two_site call at chi_max=1024.  Inputs (environments,
+Krylov bases, MPS at chi=1024) are far larger than the 129 MB L2.
+
+Reported (one JSON line on rank 0):
+  value          seconds per sweep, device time (CUDA events), inputs resident
+  e2e            the same through the C ABI from pinned host buffers
+                 (MPS/MPO copied in and the final MPS + energy copied out
+                 inside the timed region)
+  heff_tflops    algorithmic H_eff FLOP/s inside the sweep (Lanczos phase)
+  roofline       tcgen05 TF32x3 GEMM (the dominant kernel) at the centre-bond
+                 shapes, algorithmic FLOP/s vs the measured-BF16-derived
+                 3xTF32 ceiling
+  fp64           the plain FP64 form: centre-bond H_eff apply time and an
+                 accuracy check |dE/E| (mixed vs FP64) on the same ramp to chi=256
+  cpu_baseline   the CPU FP64 oracle (NumPy/LAPACK, all host cores) on one
+                 centre-bond local update, extrapolated to a sweep by FLOPs
+
+``--impl reference`` times the CPU oracle port of the reference path instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+L_SITES = 64
+D_PHYS = 2
+MPO_D = 5
+LANCZOS = 24
+EPS = 1e-10
+RAMP = [64, 256, 1024]
+METRIC = "DMRG sweep s & H_eff TFLOP/s, mixed-prec vs FP64 on GPU at |dE/E|<=1e-9"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--prec", default="tf32x3", choices=["tf32x3", "fp64"])
+    ap.add_argument("--chi", type=int, default=1024)
+    ap.add_argument("--L", type=int, default=L_SITES)
+    ap.add_argument("--no-extras", action="store_true", help="skip the FP64/roofline/CPU side measurements")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def heff_flops(chi_l, chi_r, D=MPO_D, d=D_PHYS):
+    return (2.0 * chi_l * D * d * d * chi_r * chi_l + 2.0 * chi_l * d * chi_r * D * d * d * D
+            + 2.0 * chi_l * chi_r * d * D * d * d * D + 2.0 * chi_l * d * d * chi_r * D * chi_r)
+
+
+def bond_caps(L, chi):
+    return [min(chi, 2 ** k, 2 ** (L - k)) for k in range(L + 1)]
+
+
+def sweep_flop_weight(L, chi):
+    """sum over the 2(L-1) local updates of H_eff FLOPs relative to the centre bond."""
+    c = bond_caps(L, chi)
+    centre = heff_flops(chi, chi)
+    w = sum(heff_flops(c[i], c[i + 2]) for i in range(L - 1))
+    return 2.0 * w / centre
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=5)
+
+    def summary(self):
+        sm = []
+        mx = []
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def cpu_local_update_seconds(chi, seed=0):
+    """One centre-bond local update of the CPU FP64 oracle (theta, Lanczos, SVD, env)."""
+    from oracle import dmrg as od
+    from oracle import hamiltonians as oh
+    g = np.random.default_rng(seed)
+    mpo = oh.spin_half_xxz(8, 1.0)
+    W = mpo[3]
+    A = g.standard_normal((chi, D_PHYS, chi)) / np.sqrt(2 * chi * chi)
+    B = g.standard_normal((chi, D_PHYS, chi)) / np.sqrt(2 * chi * chi)
+    Lenv = g.standard_normal((MPO_D, chi, chi))
+    Lenv = 0.5 * (Lenv + Lenv.transpose(0, 2, 1))
+    Renv = g.standard_normal((MPO_D, chi, chi))
+    Renv = 0.5 * (Renv + Renv.transpose(0, 2, 1))
+    t0 = time.perf_counter()
+    th = od.build_two_site_theta(A, B)
+    E, tho = od.lanczos_two_site_optimize(th, Lenv, Renv, W, W, LANCZOS, 1e-10, eig="exact")
+    An, Bn, info = od.split_two_site_theta_svd(tho, chi, EPS, True)
+    od.update_left_environment(Lenv, An, W)
+    return time.perf_counter() - t0
+
+
+def reference_arm(args, rank):
+    """CPU oracle port of the reference path: sampled centre-bond updates, extrapolated."""
+    if rank != 0:
+        return
+    chi = args.chi
+    for _ in range(args.warmup):
+        cpu_local_update_seconds(min(chi, 256))
+    times = [cpu_local_update_seconds(chi, seed=s) for s in range(args.steps)]
+    weight = sweep_flop_weight(args.L, chi)
+    per_sweep = float(np.mean(times)) * weight
+    line = {
+        "impl": "reference", "metric": METRIC, "value": per_sweep, "unit": "s/sweep", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_sweep * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"heisenberg_xxz L={args.L} d=2 D=5 chi={chi} lanczos={LANCZOS}",
+                   "model": "spin-1/2 XXZ Delta=1 (reference XXZ MPO, J=-1/4)", "parallelism": "replicas"},
+        "cpu_baseline": {"value": per_sweep, "unit": "s/sweep", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"{args.steps} centre-bond local updates at chi={chi}, FLOP-weighted x{weight:.1f}"
+                                   " to a sweep (extrapolated)"},
+        "e2e": {"value": per_sweep, "unit": "s/sweep", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        reference_arm(args, rank)
+        return
+
+    import torch
+    import ctypes as C
+    import chemtensor_mojo_gb300 as ct
+    from chemtensor_mojo_gb300 import _lib
+    from chemtensor_mojo_gb300.dmrg import bond_capacities
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    ctx = ct.get_context(local_rank)
+    L = args.L
+    chi = args.chi
+    prec = args.prec
+
+    mpo = ct.create_spin_half_xxz_mpo(ctx, L, 1.0)
+    arrays, dims = ct.random_mps_c_compatible_arrays(L, D_PHYS, RAMP[0], 1000 + rank)
+    mps = ct.mps_right_normalize(ctx, ct.mps_from_arrays(ctx, arrays))
+
+    def params(c, nsweeps, pr=prec):
+        return ct.DMRGParams(num_sweeps=nsweeps, chi_max=c, eps_trunc=EPS, max_krylov_iter=LANCZOS,
+                             krylov_tol=1e-10, energy_tol=0.0, max_rotations=0, prec=pr)
+
+    # ---- warm-up: the chi ramp ----------------------------------------------
+    ramp = (RAMP + [chi] * 100)[:max(args.warmup, 0)]
+    ramp = [min(c, chi) for c in ramp]
+    E = None
+    warm_log = []
+    for c in ramp:
+        st = ct.DMRGStats()
+        E, mps = ct.dmrg_two_site(ctx, mpo, mps, params(c, 1), st)
+        warm_log.append({"chi_max": c, "energy": E, "seconds": st.seconds_total})
+
+    # ---- timed: K sweeps at chi, from pinned host buffers --------------------
+    d = D_PHYS
+    cap = bond_capacities(list(mps.bond_dims), d, chi)
+    host_sites = [torch.zeros(cap[i] * d * cap[i + 1], dtype=torch.float64).pin_memory() for i in range(L)]
+    for i, s in enumerate(mps.sites):
+        host_sites[i][:s.tensor.size].copy_(s.tensor.storage.cpu())
+    host_mpo = [s.tensor.storage.cpu().pin_memory() for s in mpo.sites]
+    dev_sites = [torch.empty_like(h, device=ctx.torch_device) for h in host_sites]
+    dev_mpo = [torch.empty_like(h, device=ctx.torch_device) for h in host_mpo]
+    bd = _lib.i64_array(mps.bond_dims)
+    mpo_pp, k1 = _lib.ptr_array([t.data_ptr() for t in dev_mpo])
+    mps_pp, k2 = _lib.ptr_array([t.data_ptr() for t in dev_sites])
+    capacity = _lib.i64_array([t.numel() for t in dev_sites])
+    Ec = C.c_double()
+    sweeps_e = (C.c_double * max(args.steps, 1))()
+    done = C.c_int()
+    stats = _lib.ct_dmrg_stats()
+    cp = params(chi, args.steps).to_c()
+    h2d = sum(h.numel() * 8 for h in host_sites) + sum(h.numel() * 8 for h in host_mpo)
+    d2h = sum(h.numel() * 8 for h in host_sites) + 8
+
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    clocks = ClockSampler(local_rank)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    launches0 = _lib.launch_count()
+    t_wall0 = time.perf_counter()
+    ev[0].record(stream)
+    for h, dv in zip(host_sites, dev_sites):
+        dv.copy_(h, non_blocking=True)
+    for h, dv in zip(host_mpo, dev_mpo):
+        dv.copy_(h, non_blocking=True)
+    ev[1].record(stream)
+    ctx.call("ct_dmrg_two_site", C.byref(cp), L, d, _lib.i64_array(mpo.bond_dims), mpo_pp, bd, mps_pp, capacity,
+             C.byref(Ec), sweeps_e, C.byref(done), None, C.byref(stats))
+    ev[2].record(stream)
+    for h, dv in zip(host_sites, dev_sites):
+        h.copy_(dv, non_blocking=True)
+    ev[3].record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    launches = _lib.launch_count() - launches0
+    clocks.stop()
+    if dist is not None:
+        dist.barrier()
+    K = max(args.steps, 1)
+    dev_s = ev[1].elapsed_time(ev[2]) * 1e-3
+    e2e_s = ev[0].elapsed_time(ev[3]) * 1e-3
+    if dist is not None:
+        t = torch.tensor([dev_s, e2e_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s, e2e_s = float(t[0]), float(t[1])
+    per_sweep = dev_s / K
+    heff_tflops = stats.heff_flops / max(stats.seconds_lanczos, 1e-12) / 1e12
+    final_dims = [int(x) for x in bd]
+
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        extras = side_measurements(ctx, ct, _lib, C, chi, prec, L, mpo)
+
+    if rank != 0:
+        return
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        peaks = {}
+    bf16 = peaks.get("bf16_tflops", 1900.0)
+    peak_src = "measured" if "bf16_tflops" in peaks else "fallback"
+    line = {
+        "metric": METRIC, "value": per_sweep, "unit": "s/sweep", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": per_sweep * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": prec, "storage_dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"heisenberg_xxz L={L} d=2 D=5 chi_max={chi} (ramp {ramp}) lanczos={LANCZOS} "
+                               f"eps={EPS}", "model": "spin-1/2 XXZ Delta=1 (reference XXZ MPO, J=-1/4)",
+                   "global_batch": 1, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (MPS + environments + Krylov basis >> 129 MB)",
+                   "eigensolver": "converged tridiagonal Jacobi"},
+        "energy": Ec.value, "sweep_energies": list(sweeps_e)[:done.value], "bond_dims_final": final_dims,
+        "heff_tflops": heff_tflops, "heff_applies": stats.heff_applies, "local_updates": stats.local_updates,
+        "phase_seconds": {"lanczos": stats.seconds_lanczos, "svd": stats.seconds_svd, "env": stats.seconds_env,
+                          "total_wall": stats.seconds_total},
+        "max_discarded": stats.max_discarded, "warmup_log": warm_log,
+        "e2e": {"value": e2e_s / K, "unit": "s/sweep", "h2d_bytes_per_step": h2d // K, "d2h_bytes_per_step": d2h // K,
+                "wall_s": t_wall},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+    }
+    line.update(extras)
+    if "tc_gemm_ms" in extras:
+        m, n, k = extras["tc_gemm_shape"]
+        ach = 2.0 * m * n * k / (extras["tc_gemm_ms"] * 1e-3) / 1e12
+        peak = bf16 / 6.0
+        line["roofline"] = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                            "traffic": extras.get("tc_gemm_traffic"),
+                            "kernel": "tc_gemm_kernel<128,3> (TF32x3, tcgen05)",
+                            "peak_note": f"{peak_src} bf16 {bf16} TFLOP/s / 2 (TF32 rate) / 3 (3 MMAs per product)"}
+    if "cpu_sweep_s" in extras:
+        line["cpu_baseline"] = {"value": extras["cpu_sweep_s"], "unit": "s/sweep", "cores": os.cpu_count(),
+                                "kind": "port", "sample": extras["cpu_sample"]}
+    print(json.dumps(line), flush=True)
+
+
+def side_measurements(ctx, ct, _lib, C, chi, prec, L, mpo):
+    import torch
+    out = {}
+    # dominant kernel: TF32x3 GEMM at the centre-bond H_eff shapes
+    if prec == "tf32x3":
+        m, n, k = MPO_D * chi, D_PHYS * D_PHYS * chi, chi
+        ms = C.c_double()
+        ctx.call("ct_tc_gemm_time", C.c_int64(m), C.c_int64(n), C.c_int64(k), 10, C.byref(ms))
+        out["tc_gemm_ms"] = ms.value
+        out["tc_gemm_shape"] = [m, n, k]
+        m4, n4, k4 = chi * D_PHYS * D_PHYS, chi, MPO_D * chi
+        ctx.call("ct_tc_gemm_time", C.c_int64(m4), C.c_int64(n4), C.c_int64(k4), 10, C.byref(ms))
+        out["tc_gemm4_ms"] = ms.value
+        out["tc_gemm4_shape"] = [m4, n4, k4]
+    # H_eff apply at the centre bond: mixed and FP64
+    g = torch.Generator(device="cpu").manual_seed(5)
+    dev = ctx.torch_device
+    th = ct.DenseTensor(torch.randn(chi * 4 * chi, generator=g, dtype=torch.float64).to(dev), [chi, 2, 2, chi])
+    Le = ct.DenseTensor(torch.randn(MPO_D * chi * chi, generator=g, dtype=torch.float64).to(dev), [MPO_D, chi, chi])
+    Re = ct.DenseTensor(torch.randn(MPO_D * chi * chi, generator=g, dtype=torch.float64).to(dev), [MPO_D, chi, chi])
+    W = mpo.sites[L // 2]
+    F = heff_flops(chi, chi)
+    for pr, reps in (("tf32x3", 10), ("fp64", 2)):
+        ct.apply_two_site_heff(th, Le, Re, W, W, ctx, prec=pr)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            o = ct.apply_two_site_heff(th, Le, Re, W, W, ctx, prec=pr)
+        e1.record()
+        torch.cuda.synchronize()
+        s = e0.elapsed_time(e1) * 1e-3 / reps
+        out[f"heff_apply_{pr}_s"] = s
+        out[f"heff_apply_{pr}_tflops"] = F / s / 1e12
+        if pr == "tf32x3":
+            o_mixed = o.to_numpy()
+        else:
+            o64 = o.to_numpy()
+    out["heff_apply_rel_err_tf32x3_vs_fp64"] = float(np.linalg.norm(o_mixed - o64) / np.linalg.norm(o64))
+    out["heff_apply_speedup_vs_fp64"] = out["heff_apply_fp64_s"] / out["heff_apply_tf32x3_s"]
+    # accuracy: mixed vs FP64 on the same ramp capped at chi=256 (FP64 affordable)
+    arrays, _ = ct.random_mps_c_compatible_arrays(L, D_PHYS, RAMP[0], 7)
+    res = {}
+    tsec = {}
+    for pr in ("tf32x3", "fp64"):
+        mps = ct.mps_right_normalize(ctx, ct.mps_from_arrays(ctx, arrays))
+        t0 = time.perf_counter()
+        for c in (64, 256, 256):
+            E, mps = ct.dmrg_two_site(ctx, mpo, mps, ct.DMRGParams(
+                num_sweeps=1, chi_max=c, eps_trunc=EPS, max_krylov_iter=LANCZOS, krylov_tol=1e-10,
+                energy_tol=0.0, max_rotations=0, prec=pr))
+        tsec[pr] = time.perf_counter() - t0
+        res[pr] = E
+    out["accuracy_check"] = {"workload": f"same chain, ramp 64,256,256 ({L} sites)", "E_fp64": res["fp64"],
+                             "E_tf32x3": res["tf32x3"],
+                             "dE_over_E": abs(res["tf32x3"] - res["fp64"]) / abs(res["fp64"]),
+                             "seconds_fp64": tsec["fp64"], "seconds_tf32x3": tsec["tf32x3"]}
+    # CPU baseline: one centre-bond local update of the FP64 oracle, extrapolated
+    t_cpu = cpu_local_update_seconds(chi)
+    w = sweep_flop_weight(L, chi)
+    out["cpu_sweep_s"] = t_cpu * w
+    out["cpu_sample"] = (f"1 centre-bond local update (theta, {LANCZOS} Lanczos H_eff applies, SVD, env) at chi={chi}"
+                         f" took {t_cpu:.2f} s; x{w:.1f} FLOP weight to a sweep (extrapolated)")
+    return out
+
+
+if __name__ == "__main__":
+    main()

@@ -87,9 +87,11 @@ SIGNATURES = {
     "ct_mps_expectation": [P, I32, I32, I32, C.POINTER(I64), PP, C.POINTER(I64), PP, C.POINTER(D), C.POINTER(D)],
     "ct_random_mps_host": [I32, I32, I32, C.c_uint64, C.POINTER(I64), PP],
     "ct_rng_randnf_host": [C.c_uint64, I64, C.POINTER(C.c_float)],
+    "ct_tc_gemm_time": [P, I64, I64, I64, I32, C.POINTER(D)],
     "ct_energy_grad": [P, I32, I32, I32, C.POINTER(I64), PP, C.POINTER(I64), PP, PP, I32, C.POINTER(D)],
 }
 STRING_FUNCS = {"ct_error_string": [I32], "ct_last_error": [P]}
+INT64_FUNCS = {"ct_launch_count": []}
 
 _lib = None
 _lock = threading.Lock()
@@ -111,12 +113,20 @@ def load() -> C.CDLL:
             f = getattr(lib, name)
             f.argtypes = args
             f.restype = C.c_int
+        for name, args in INT64_FUNCS.items():
+            f = getattr(lib, name)
+            f.argtypes = args
+            f.restype = C.c_int64
         for name, args in STRING_FUNCS.items():
             f = getattr(lib, name)
             f.argtypes = args
             f.restype = C.c_char_p
         _lib = lib
         return lib
+
+
+def launch_count() -> int:
+    return int(load().ct_launch_count())
 
 
 def error_string(status: int) -> str:

@@ -11,6 +11,8 @@
 // ---------------------------------------------------------------------------
 // errors, handle, arena
 // ---------------------------------------------------------------------------
+std::atomic<long long> g_ct_launches{0};
+
 void ct_seterr(ct_handle* h, const char* fmt, ...) {
     if (!h) return;
     char buf[1024];
@@ -88,6 +90,8 @@ static int check_prec(ct_handle* h, int prec) {
 extern "C" {
 
 int ct_version(void) { return CTDMRG_VERSION; }
+
+int64_t ct_launch_count(void) { return (int64_t)g_ct_launches.load(); }
 
 const char* ct_error_string(int s) {
     switch (s) {

@@ -6,6 +6,7 @@
 #include <stdint.h>
 #include <stdio.h>
 #include <string.h>
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -55,6 +56,10 @@ enum { FL_STOP = 0, FL_NUMITER = 1, FL_ROT = 2, FL_CHI = 3, FL_TMP = 4, FL_CNT =
 #define CT_MAX_KRYLOV 128
 
 void ct_seterr(ct_handle* h, const char* fmt, ...);
+
+// process-wide count of kernel launches issued by this library
+extern std::atomic<long long> g_ct_launches;
+static inline void ct_note_launch() { g_ct_launches.fetch_add(1, std::memory_order_relaxed); }
 
 #define CT_CUDA(h, x)                                                                      \
     do {                                                                                   \

@@ -99,10 +99,10 @@ int ct_gemm_f64_launch(ct_handle* h, const GemmDesc& g) {
     }
     const bool ak = (g.sAk == 1);
     const bool bn = (g.sBn == 1);
-    if (ak && bn) gemm_f64_kernel<true, true><<<grid, NT, 0, h->stream>>>(g);
-    else if (ak) gemm_f64_kernel<true, false><<<grid, NT, 0, h->stream>>>(g);
-    else if (bn) gemm_f64_kernel<false, true><<<grid, NT, 0, h->stream>>>(g);
-    else gemm_f64_kernel<false, false><<<grid, NT, 0, h->stream>>>(g);
+    if (ak && bn) { gemm_f64_kernel<true, true><<<grid, NT, 0, h->stream>>>(g); ct_note_launch(); }
+    else if (ak) { gemm_f64_kernel<true, false><<<grid, NT, 0, h->stream>>>(g); ct_note_launch(); }
+    else if (bn) { gemm_f64_kernel<false, true><<<grid, NT, 0, h->stream>>>(g); ct_note_launch(); }
+    else { gemm_f64_kernel<false, false><<<grid, NT, 0, h->stream>>>(g); ct_note_launch(); }
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }

@@ -101,7 +101,7 @@ int ct_mpo_apply_f64_launch(ct_handle* h, const MpoDesc& m) {
     }
     if (m.O > 65535) return CT_ERR_UNSUPPORTED;
     dim3 grid((unsigned)ct_cdiv(m.I, MPO_NT), (unsigned)m.O);
-    mpo_apply_f64_kernel<<<grid, MPO_NT, smem, h->stream>>>(m);
+    mpo_apply_f64_kernel<<<grid, MPO_NT, smem, h->stream>>>(m); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
@@ -109,21 +109,21 @@ int ct_mpo_apply_f64_launch(ct_handle* h, const MpoDesc& m) {
 int ct_build_w12(ct_handle* h, const double* W1, const double* W2, double* W12t, int64_t wL,
                  int64_t d, int64_t wM, int64_t wR) {
     const int64_t n = (d * d * wR) * (wL * d * d);
-    build_w12_kernel<<<(unsigned)ct_cdiv(n, 256), 256, 0, h->stream>>>(W1, W2, W12t, wL, d, wM, wR);
+    build_w12_kernel<<<(unsigned)ct_cdiv(n, 256), 256, 0, h->stream>>>(W1, W2, W12t, wL, d, wM, wR); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
 
 int ct_build_wt_left(ct_handle* h, const double* W, double* Wt, int64_t wL, int64_t d, int64_t wR) {
     const int64_t n = (d * wR) * (wL * d);
-    build_wt_left_kernel<<<(unsigned)ct_cdiv(n, 256), 256, 0, h->stream>>>(W, Wt, wL, d, wR);
+    build_wt_left_kernel<<<(unsigned)ct_cdiv(n, 256), 256, 0, h->stream>>>(W, Wt, wL, d, wR); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
 
 int ct_build_wt_right(ct_handle* h, const double* W, double* Wt, int64_t wL, int64_t d, int64_t wR) {
     const int64_t n = (wL * d) * (wR * d);
-    build_wt_right_kernel<<<(unsigned)ct_cdiv(n, 256), 256, 0, h->stream>>>(W, Wt, wL, d, wR);
+    build_wt_right_kernel<<<(unsigned)ct_cdiv(n, 256), 256, 0, h->stream>>>(W, Wt, wL, d, wR); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }

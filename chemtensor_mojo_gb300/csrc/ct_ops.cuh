@@ -10,8 +10,9 @@ struct HeffPlan {
     double* T1 = nullptr;
     double* T3 = nullptr;
     double* W12 = nullptr;
-    // mixed form (ct_tc.cu)
+    // mixed form (ct_tc.cu): operand planes of the bond, constructed in place
     void* tc = nullptr;
+    alignas(16) unsigned char tc_store[512];
 };
 
 struct LanczosResult {

@@ -19,6 +19,7 @@ namespace {
 
 constexpr int SVD_NT = 256;
 constexpr int SVD_MAX_SWEEPS = 60;
+constexpr double SVD_EPS2 = 2.2204460492503131e-16 * 2.2204460492503131e-16;
 
 __device__ __forceinline__ void tournament_pair(int P, int r, int k, int& p, int& q) {
     if (k == 0) {
@@ -31,7 +32,11 @@ __device__ __forceinline__ void tournament_pair(int P, int r, int k, int& p, int
 }
 
 // Rotation that orthogonalises two vectors with |x_p|^2=a, |x_q|^2=b, <x_p,x_q>=c.
-__device__ __forceinline__ bool jacobi_rot(double a, double b, double c, double tol, double& cs, double& sn) {
+// Vectors with |x|^2 <= floor (numerically zero next to |M|_F) are left alone:
+// rotating rounding noise never converges.
+__device__ __forceinline__ bool jacobi_rot(double a, double b, double c, double tol, double floor, double& cs,
+                                           double& sn) {
+    if (a <= floor || b <= floor) return false;
     if (c == 0.0 || !(fabs(c) > tol * sqrt(a * b))) return false;
     const double zeta = (b - a) / (2.0 * c);
     double t;
@@ -58,7 +63,8 @@ __global__ void svd_init_kernel(const double* M, int64_t m, int64_t n, int cols,
 
 // ---- large path: one round, one CTA per pair -------------------------------
 __global__ void __launch_bounds__(SVD_NT) svd_round_kernel(double* X, int64_t len, int64_t ldx, double* Q,
-                                                           int64_t nvec, int P, int r, double tol, int* rot_count) {
+                                                           int64_t nvec, int P, int r, double tol,
+                                                           const double* frob2, int* rot_count) {
     __shared__ double sm[32];
     __shared__ double rot[2];
     __shared__ int do_rot;
@@ -79,7 +85,8 @@ __global__ void __launch_bounds__(SVD_NT) svd_round_kernel(double* X, int64_t le
     c = ct_block_sum<SVD_NT>(c, sm);
     if (threadIdx.x == 0) {
         double cs, sn;
-        do_rot = jacobi_rot(a, b, c, tol, cs, sn) ? 1 : 0;
+        const double floor = SVD_EPS2 * (*frob2);
+        do_rot = jacobi_rot(a, b, c, tol, floor, cs, sn) ? 1 : 0;
         if (do_rot) {
             rot[0] = cs;
             rot[1] = sn;
@@ -112,6 +119,10 @@ __global__ void __launch_bounds__(SVD_NT) svd_small_kernel(double* Xg, int64_t l
     for (int64_t t = threadIdx.x; t < (int64_t)nvec * len; t += SVD_NT) X[t] = Xg[(t / len) * ldx + t % len];
     for (int64_t t = threadIdx.x; t < (int64_t)nvec * nvec; t += SVD_NT) Q[t] = Qg[t];
     __syncthreads();
+    __shared__ double red[32];
+    double f2 = 0.0;
+    for (int64_t t = threadIdx.x; t < (int64_t)nvec * len; t += SVD_NT) f2 = fma(X[t], X[t], f2);
+    const double floor = SVD_EPS2 * ct_block_sum<SVD_NT>(f2, red);
     const int P = nvec + (nvec & 1);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = SVD_NT / 32;
     bool converged = false;
@@ -135,7 +146,7 @@ __global__ void __launch_bounds__(SVD_NT) svd_small_kernel(double* Xg, int64_t l
                 b = ct_warp_sum(b);
                 c = ct_warp_sum(c);
                 double cs, sn;
-                if (jacobi_rot(a, b, c, tol, cs, sn)) {
+                if (jacobi_rot(a, b, c, tol, floor, cs, sn)) {
                     rotated = 1;
                     for (int64_t i = lane; i < len; i += 32) {
                         const double u = xp[i], v = xq[i];
@@ -317,7 +328,7 @@ int ct_svd_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, i
         int g = (int)ct_cdiv(tot, 256);
         if (g > h->num_sms * 16) g = h->num_sms * 16;
         if (g < 1) g = 1;
-        svd_init_kernel<<<g, 256, 0, h->stream>>>(M, m, n, cols, X, ldx, Q, nvec);
+        svd_init_kernel<<<g, 256, 0, h->stream>>>(M, m, n, cols, X, ldx, Q, nvec); ct_note_launch();
         CT_LAUNCH_CHECK(h);
     }
     const double tol = 2.2204460492503131e-16 * sqrt((double)(len > 1 ? len : 1)) * 4.0;
@@ -331,16 +342,18 @@ int ct_svd_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, i
                 attr = true;
             }
             svd_small_kernel<<<1, SVD_NT, small_bytes, h->stream>>>(X, len, ldx, Q, (int)nvec, tol, SVD_MAX_SWEEPS,
-                                                                    h->d_status);
+                                                                    h->d_status); ct_note_launch();
             CT_LAUNCH_CHECK(h);
         } else {
             const int P = (int)(nvec + (nvec & 1));
             int* d_rot = h->d_flags + FL_ROT;
+            double* d_frob2 = h->d_scalars + SC_TMP0;
+            CT_TRY(ct_reduce_nrm2sq(h, nvec * ldx, X, d_frob2, nullptr));
             bool converged = false;
             for (int sweep = 0; sweep < SVD_MAX_SWEEPS; ++sweep) {
                 CT_CUDA(h, cudaMemsetAsync(d_rot, 0, sizeof(int), h->stream));
                 for (int r = 0; r < P - 1; ++r) {
-                    svd_round_kernel<<<P / 2, SVD_NT, 0, h->stream>>>(X, len, ldx, Q, nvec, P, r, tol, d_rot);
+                    svd_round_kernel<<<P / 2, SVD_NT, 0, h->stream>>>(X, len, ldx, Q, nvec, P, r, tol, d_frob2, d_rot); ct_note_launch();
                 }
                 CT_LAUNCH_CHECK(h);
                 int rot = 0;
@@ -358,9 +371,9 @@ int ct_svd_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, i
             }
         }
     }
-    svd_norms_kernel<<<(unsigned)ct_cdiv(nvec * 32, 256), 256, 0, h->stream>>>(X, len, ldx, nvec, sig);
-    svd_rank_kernel<<<(unsigned)ct_cdiv(nvec, 256), 256, 0, h->stream>>>(sig, nvec, perm);
-    svd_trunc_kernel<<<1, 32, 0, h->stream>>>(sig, perm, k, chi_max, eps_trunc, h->d_scalars, h->d_flags);
+    svd_norms_kernel<<<(unsigned)ct_cdiv(nvec * 32, 256), 256, 0, h->stream>>>(X, len, ldx, nvec, sig); ct_note_launch();
+    svd_rank_kernel<<<(unsigned)ct_cdiv(nvec, 256), 256, 0, h->stream>>>(sig, nvec, perm); ct_note_launch();
+    svd_trunc_kernel<<<1, 32, 0, h->stream>>>(sig, perm, k, chi_max, eps_trunc, h->d_scalars, h->d_flags); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     int chi = 0;
     double sums[2];
@@ -383,7 +396,7 @@ int ct_svd_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, i
         if (g > h->num_sms * 16) g = h->num_sms * 16;
         if (g < 1) g = 1;
         svd_gather_kernel<<<g, 256, 0, h->stream>>>(X, ldx, Q, nvec, sig, perm, h->d_flags, m, n, cols, mode, A, B,
-                                                    S);
+                                                    S); ct_note_launch();
         CT_LAUNCH_CHECK(h);
     }
     return CT_OK;

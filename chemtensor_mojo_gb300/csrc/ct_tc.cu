@@ -1,16 +1,757 @@
-// Mixed-precision (TF32x3) tensor-core path: placeholder until the tcgen05
-// kernels land; every entry reports CT_ERR_UNSUPPORTED.
+// Mixed-precision form: TF32x3 contractions on the sm_103a tensor cores.
+//
+// GEMM: C[M,N] = sum_k A[m,k] B[n,k] with both operands K-major, each split
+// into two TF32 planes (x = hi + lo, both exactly representable in TF32) so
+// that hi*hi + hi*lo + lo*hi accumulated in FP32 recovers ~FP32 accuracy.
+//   * one CTA per 128 x BN output tile, 6 warps:
+//       warp 0      TMA producer (cp.async.bulk.tensor, 128B swizzle)
+//       warp 1      TMEM allocator + single-thread tcgen05.mma issuer
+//       warps 2..5  epilogue (tcgen05.ld 32x32b, one TMEM lane quadrant each)
+//   * STAGES-deep smem ring guarded by full/empty mbarriers; MMAs release a
+//     stage through tcgen05.commit; the accumulator lives in TMEM.
+//   * every mbarrier wait is bounded by %globaltimer (2 s); a timeout sets the
+//     device status word and the CTA falls through to TMEM release and exit.
+//
+// Contraction chains (see ct_ops.cu for the FP64 form) are the same, with the
+// permutes folded into the operand packers (FP64 -> split TF32, K-major,
+// K padded to 32) and into the GEMM epilogue's row mapping.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <new>
+
 #include "ct_ops.cuh"
 
-int ct_tc_available(ct_handle* h) { (void)h; return 0; }
-size_t ct_tc_heff_ws_bytes(int64_t, int64_t, int64_t, int64_t, int64_t, int64_t) { return 0; }
-int ct_tc_heff_prepare(ct_handle*, Arena&, HeffPlan&) { return CT_ERR_UNSUPPORTED; }
-int ct_tc_heff_run(ct_handle*, const HeffPlan&, const double*, double*, const int*) { return CT_ERR_UNSUPPORTED; }
-size_t ct_tc_env_ws_bytes(int64_t, int64_t, int64_t, int64_t, int64_t) { return 0; }
-int ct_tc_env_left_run(ct_handle*, Arena&, const double*, const double*, const double*, double*, int64_t, int64_t,
-                       int64_t, int64_t, int64_t) { return CT_ERR_UNSUPPORTED; }
-int ct_tc_env_right_run(ct_handle*, Arena&, const double*, const double*, const double*, double*, int64_t, int64_t,
-                        int64_t, int64_t, int64_t) { return CT_ERR_UNSUPPORTED; }
-int ct_tc_gemm(ct_handle*, Arena&, int, int, int64_t, int64_t, int64_t, double, const double*, int64_t,
-               const double*, int64_t, double, double*, int64_t) { return CT_ERR_UNSUPPORTED; }
-size_t ct_tc_gemm_ws_bytes(int64_t, int64_t, int64_t) { return 0; }
+namespace {
+
+constexpr int TC_BM = 128;
+constexpr int TC_BK = 32;             // fp32 elements per 128-byte swizzle row
+constexpr int TC_THREADS = 192;
+constexpr unsigned long long TC_WAIT_NS = 2000000000ull;
+
+// ---------------------------------------------------------------------------
+// PTX helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: false on timeout or when another role already aborted.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = gtimer();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (*abort_flag) return false;
+        if (gtimer() - t0 > TC_WAIT_NS) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(dst)), "l"(tm), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// K-major operand, 128-byte swizzle: rows of 128 B, 8-row groups 1024 B apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;               // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;     // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;               // descriptor version
+    d |= (uint64_t)2 << 61;               // SWIZZLE_128B
+    return d;
+}
+
+// kind::tf32 instruction descriptor: D f32, A/B tf32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t dtm, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
+        ::"r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// round-to-nearest-even to TF32 (10 explicit mantissa bits), kept in an fp32 container
+__device__ __forceinline__ float tf32_rne(float x) {
+    uint32_t u = __float_as_uint(x);
+    if ((u & 0x7F800000u) == 0x7F800000u) return x;   // inf / nan unchanged
+    u += 0xFFFu + ((u >> 13) & 1u);
+    u &= 0xFFFFE000u;
+    return __uint_as_float(u);
+}
+
+__device__ __forceinline__ void split_tf32(double x, float& hi, float& lo) {
+    hi = tf32_rne((float)x);
+    lo = tf32_rne((float)(x - (double)hi));
+}
+
+// ---------------------------------------------------------------------------
+// GEMM kernel
+// ---------------------------------------------------------------------------
+struct TcEpi {
+    void* C;
+    int out_fp64;        // 1: double, 0: float
+    int64_t M0;          // row m -> (m / M0) * sCm1 + (m % M0) * sCm0
+    int64_t sCm1, sCm0;
+    double alpha, beta;  // C = alpha * acc + beta * C
+};
+
+template <int BN, int STAGES>
+struct TcSmem {
+    static constexpr int A_BYTES = TC_BM * TC_BK * 4;       // 16 KB per plane
+    static constexpr int B_BYTES = BN * TC_BK * 4;
+    static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+    static constexpr int TILE_BYTES = STAGES * STAGE_BYTES;
+    static constexpr int TOTAL = TILE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+};
+
+template <int BN, int STAGES>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
+                   const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl, int M, int N,
+                   int Kpad, TcEpi epi, const int* skip, int* status) {
+    using L = TcSmem<BN, STAGES>;
+    if (ct_skip(skip)) return;
+    extern __shared__ uint8_t tc_smem_raw[];
+    // 128-byte swizzled tiles need 1024-byte alignment in the shared window
+    uint8_t* smem = tc_smem_raw + ((1024u - (smem_u32(tc_smem_raw) & 1023u)) & 1023u);
+    uint64_t* full = (uint64_t*)(smem + L::TILE_BYTES);
+    uint64_t* empty = full + STAGES;
+    uint64_t* done = empty + STAGES;
+    uint32_t* tmem_slot = (uint32_t*)(done + 1);
+    volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * BN;
+    const int nkb = Kpad / TC_BK;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"((uint32_t)BN)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            for (int kb = 0; kb < nkb; ++kb) {
+                const int s = kb % STAGES;
+                const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+                if (kb >= STAGES && !mbar_wait(&empty[s], ph ^ 1u, abort_flag)) {
+                    *abort_flag = 1;
+                    ct_set_status(status, CT_ERR_CUDA);
+                    break;
+                }
+                uint8_t* st = smem + s * L::STAGE_BYTES;
+                mbar_expect_tx(&full[s], L::STAGE_BYTES);
+                const int x = kb * TC_BK;
+                tma_load_2d(st, &tmAh, x, m0, &full[s]);
+                tma_load_2d(st + L::A_BYTES, &tmAl, x, m0, &full[s]);
+                tma_load_2d(st + 2 * L::A_BYTES, &tmBh, x, n0, &full[s]);
+                tma_load_2d(st + 2 * L::A_BYTES + L::B_BYTES, &tmBl, x, n0, &full[s]);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_tf32(TC_BM, BN);
+            bool ok = true;
+            for (int kb = 0; kb < nkb; ++kb) {
+                const int s = kb % STAGES;
+                const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+                if (!mbar_wait(&full[s], ph, abort_flag)) {
+                    *abort_flag = 1;
+                    ct_set_status(status, CT_ERR_CUDA);
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t a_hi = smem_u32(smem + s * L::STAGE_BYTES);
+                const uint32_t a_lo = a_hi + L::A_BYTES;
+                const uint32_t b_hi = a_hi + 2 * L::A_BYTES;
+                const uint32_t b_lo = b_hi + L::B_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < TC_BK / 8; ++kk) {
+                    const uint32_t off = kk * 32;   // 8 tf32 = 32 bytes of K per MMA
+                    const uint32_t acc0 = (kb > 0 || kk > 0) ? 1u : 0u;
+                    mma_tf32(tmem, sw128_desc(a_lo + off), sw128_desc(b_hi + off), idesc, acc0);
+                    mma_tf32(tmem, sw128_desc(a_hi + off), sw128_desc(b_lo + off), idesc, 1u);
+                    mma_tf32(tmem, sw128_desc(a_hi + off), sw128_desc(b_hi + off), idesc, 1u);
+                }
+                mma_commit(&empty[s]);
+            }
+            if (ok) mma_commit(done);
+        }
+    } else {
+        // epilogue warps 2..5 -> TMEM lane quadrants 2,3,0,1
+        const int q = warp & 3;
+        const bool ok = mbar_wait(done, 0, abort_flag);
+        if (!ok) {
+            *abort_flag = 1;
+            ct_set_status(status, CT_ERR_CUDA);
+        }
+        __syncwarp();
+        tc_fence_after();
+        if (ok) {
+            const int row = q * 32 + lane;
+            const int64_t m = (int64_t)m0 + row;
+            const bool mvalid = m < M;
+            int64_t rbase = 0;
+            if (mvalid) rbase = (m / epi.M0) * epi.sCm1 + (m % epi.M0) * epi.sCm0;
+            const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16);
+#pragma unroll 1
+            for (int c = 0; c < BN; c += 16) {
+                uint32_t r[16];
+                tmem_ld16(tq + (uint32_t)c, r);
+                if (!mvalid) continue;
+                if (epi.out_fp64) {
+                    double* Cd = (double*)epi.C + rbase;
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int64_t n = (int64_t)n0 + c + j;
+                        if (n < N) {
+                            double v = epi.alpha * (double)__uint_as_float(r[j]);
+                            if (epi.beta != 0.0) v = fma(epi.beta, Cd[n], v);
+                            Cd[n] = v;
+                        }
+                    }
+                } else {
+                    float* Cf = (float*)epi.C + rbase;
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int64_t n = (int64_t)n0 + c + j;
+                        if (n < N) Cf[n] = (float)epi.alpha * __uint_as_float(r[j]);
+                    }
+                }
+            }
+        }
+        tc_fence_before();
+    }
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN)
+                     : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// operand packer: FP64 source -> split TF32 planes [rows][ldk], K-major.
+// row r = r1 * R0 + r0 ; col k = k1 * K0p + k0 (k0 < K0 valid, K0..K0p zero)
+// src address = r1*s_r1 + r0*s_r0 + k1*s_k1 + k0*s_k0
+// ---------------------------------------------------------------------------
+struct PackDesc {
+    const double* src;
+    int64_t rows, R0, s_r1, s_r0;
+    int64_t K1, K0, K0p, s_k1, s_k0;
+    float* hi;
+    float* lo;
+    int64_t ldk;   // = K1 * K0p rounded up to 32
+    double scale;
+    const double* scale_ptr;   // optional device scalar multiplier
+};
+
+// 32 x 32 tiles through shared memory; K_FAST: source contiguous along k0.
+template <bool K_FAST>
+__global__ void pack_split_kernel(PackDesc p, const int* skip) {
+    if (ct_skip(skip)) return;
+    __shared__ double tile[32][33];
+    const int64_t rb = (int64_t)blockIdx.y * 32;
+    const int64_t kb = (int64_t)blockIdx.x * 32;   // in padded k space
+    const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+    double sc = p.scale;
+    if (p.scale_ptr) sc *= *p.scale_ptr;
+    for (int i = ty; i < 32; i += 8) {
+        int64_t r, k;
+        if (K_FAST) { r = rb + i; k = kb + tx; }
+        else        { r = rb + tx; k = kb + i; }
+        double v = 0.0;
+        if (r < p.rows && k < p.ldk) {
+            const int64_t k1 = k / p.K0p, k0 = k % p.K0p;
+            if (k1 < p.K1 && k0 < p.K0) {
+                const int64_t r1 = r / p.R0, r0 = r % p.R0;
+                v = p.src[r1 * p.s_r1 + r0 * p.s_r0 + k1 * p.s_k1 + k0 * p.s_k0];
+            }
+        }
+        if (K_FAST) tile[i][tx] = v;
+        else tile[tx][i] = v;
+    }
+    __syncthreads();
+    for (int i = ty; i < 32; i += 8) {
+        const int64_t r = rb + i, k = kb + tx;
+        if (r < p.rows && k < p.ldk) {
+            float h, l;
+            split_tf32(tile[i][tx] * sc, h, l);
+            p.hi[r * p.ldk + k] = h;
+            p.lo[r * p.ldk + k] = l;
+        }
+    }
+}
+
+// MPO leg in FP32 with split-TF32 output: out(o, j, i) = sum_k Wt[j,k] in(o,k,i)
+struct MpoTcDesc {
+    int64_t O, K, J, I;
+    const float* in; int64_t sIo, sIk, sIi;
+    float* hi; float* lo; int64_t sOo, sOi, J0, sOj1, sOj0;
+    const double* Wt;
+    const int* skip;
+};
+
+constexpr int MPOT_NT = 128, MPOT_JC = 16;
+
+__global__ void __launch_bounds__(MPOT_NT) mpo_tc_kernel(MpoTcDesc m) {
+    if (ct_skip(m.skip)) return;
+    extern __shared__ float wsf[];
+    const int64_t JK = m.J * m.K;
+    for (int64_t t = threadIdx.x; t < JK; t += MPOT_NT) wsf[t] = (float)m.Wt[t];
+    __syncthreads();
+    const int64_t o = blockIdx.y;
+    const int64_t i = (int64_t)blockIdx.x * MPOT_NT + threadIdx.x;
+    if (i >= m.I) return;
+    const float* in = m.in + o * m.sIo + i * m.sIi;
+    for (int64_t j0 = 0; j0 < m.J; j0 += MPOT_JC) {
+        float acc[MPOT_JC];
+#pragma unroll
+        for (int jj = 0; jj < MPOT_JC; ++jj) acc[jj] = 0.f;
+        const int nj = (int)((m.J - j0) < MPOT_JC ? (m.J - j0) : MPOT_JC);
+        for (int64_t k = 0; k < m.K; ++k) {
+            const float x = in[k * m.sIk];
+#pragma unroll
+            for (int jj = 0; jj < MPOT_JC; ++jj)
+                if (jj < nj) acc[jj] = fmaf(wsf[(j0 + jj) * m.K + k], x, acc[jj]);
+        }
+#pragma unroll
+        for (int jj = 0; jj < MPOT_JC; ++jj) {
+            if (jj >= nj) break;
+            const int64_t j = j0 + jj;
+            const int64_t off = o * m.sOo + i * m.sOi + (j / m.J0) * m.sOj1 + (j % m.J0) * m.sOj0;
+            float h, l;
+            split_tf32((double)acc[jj], h, l);
+            m.hi[off] = h;
+            m.lo[off] = l;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+bool get_encoder() {
+    if (g_encode) return true;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || fn == nullptr) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    return true;
+}
+
+int make_map(ct_handle* h, CUtensorMap* m, const float* base, int64_t rows, int64_t ldk, int box_rows) {
+    if (((uintptr_t)base & 15) || (ldk % TC_BK)) {
+        ct_seterr(h, "TMA operand misaligned (base %p, ldk %lld)", (const void*)base, (long long)ldk);
+        return CT_ERR_INVALID;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)ldk, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(ldk * 4)};
+    cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        ct_seterr(h, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return CT_ERR_CUDA;
+    }
+    return CT_OK;
+}
+
+constexpr int GEMM_BN = 128;
+constexpr int GEMM_STAGES = 3;
+
+struct SplitOperand {
+    float* hi = nullptr;
+    float* lo = nullptr;
+    int64_t rows = 0, ldk = 0;
+};
+
+int tc_gemm_launch(ct_handle* h, const SplitOperand& A, const SplitOperand& B, int64_t M, int64_t N,
+                   const TcEpi& epi, const int* skip) {
+    if (A.ldk != B.ldk) return CT_ERR_SHAPE;
+    if (M <= 0 || N <= 0) return CT_OK;
+    if (M > (1ll << 31) || N > (1ll << 31)) return CT_ERR_UNSUPPORTED;
+    CUtensorMap ta_h, ta_l, tb_h, tb_l;
+    CT_TRY(make_map(h, &ta_h, A.hi, A.rows, A.ldk, TC_BM));
+    CT_TRY(make_map(h, &ta_l, A.lo, A.rows, A.ldk, TC_BM));
+    CT_TRY(make_map(h, &tb_h, B.hi, B.rows, B.ldk, GEMM_BN));
+    CT_TRY(make_map(h, &tb_l, B.lo, B.rows, B.ldk, GEMM_BN));
+    using L = TcSmem<GEMM_BN, GEMM_STAGES>;
+    static int attr_dev = -1;
+    if (attr_dev != h->device) {
+        CT_CUDA(h, cudaFuncSetAttribute(tc_gemm_kernel<GEMM_BN, GEMM_STAGES>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, L::TOTAL));
+        attr_dev = h->device;
+    }
+    dim3 grid((unsigned)ct_cdiv(N, GEMM_BN), (unsigned)ct_cdiv(M, TC_BM));
+    if (grid.y > 65535) return CT_ERR_UNSUPPORTED;
+    tc_gemm_kernel<GEMM_BN, GEMM_STAGES><<<grid, TC_THREADS, L::TOTAL, h->stream>>>(
+        ta_h, ta_l, tb_h, tb_l, (int)M, (int)N, (int)A.ldk, epi, skip, h->d_status); ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int pack_launch(ct_handle* h, const PackDesc& p, bool k_fast, const int* skip) {
+    if (p.rows <= 0 || p.ldk <= 0) return CT_OK;
+    dim3 grid((unsigned)ct_cdiv(p.ldk, 32), (unsigned)ct_cdiv(p.rows, 32));
+    if (grid.y > 65535) return CT_ERR_UNSUPPORTED;
+    dim3 block(32, 8);
+    if (k_fast) { pack_split_kernel<true><<<grid, block, 0, h->stream>>>(p, skip); ct_note_launch(); }
+    else { pack_split_kernel<false><<<grid, block, 0, h->stream>>>(p, skip); ct_note_launch(); }
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+// Plain 2-level-row, 1-level-k pack helper.
+PackDesc pack_desc(const double* src, int64_t rows, int64_t R0, int64_t s_r1, int64_t s_r0, int64_t K, int64_t s_k,
+                   const SplitOperand& dst) {
+    PackDesc p{};
+    p.src = src;
+    p.rows = rows; p.R0 = R0; p.s_r1 = s_r1; p.s_r0 = s_r0;
+    p.K1 = 1; p.K0 = K; p.K0p = dst.ldk; p.s_k1 = 0; p.s_k0 = s_k;
+    p.hi = dst.hi; p.lo = dst.lo; p.ldk = dst.ldk;
+    p.scale = 1.0; p.scale_ptr = nullptr;
+    return p;
+}
+
+int mpo_tc_launch(ct_handle* h, const MpoTcDesc& m) {
+    if (m.O <= 0 || m.I <= 0 || m.J <= 0) return CT_OK;
+    const size_t smem = (size_t)(m.J * m.K) * sizeof(float);
+    if (smem > 200 * 1024 || m.O > 65535) return CT_ERR_UNSUPPORTED;
+    static int attr_dev = -1;
+    if (attr_dev != h->device) {
+        CT_CUDA(h, cudaFuncSetAttribute(mpo_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        attr_dev = h->device;
+    }
+    dim3 grid((unsigned)ct_cdiv(m.I, MPOT_NT), (unsigned)m.O);
+    mpo_tc_kernel<<<grid, MPOT_NT, smem, h->stream>>>(m); ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+SplitOperand take_split(Arena& ar, int64_t rows, int64_t ldk) {
+    SplitOperand s;
+    s.rows = rows;
+    s.ldk = ldk;
+    s.hi = ar.take<float>((size_t)(rows * ldk));
+    s.lo = ar.take<float>((size_t)(rows * ldk));
+    return s;
+}
+size_t split_bytes(int64_t rows, int64_t ldk) { return 2 * ct_bytes((size_t)(rows * ldk), 4); }
+
+struct TcHeff {
+    SplitOperand Lp;   // [wL*Dl][Dl_pad]
+    SplitOperand R4;   // [Dr][wR*Dr_pad]
+    SplitOperand th;   // [d*d*Dr][Dl_pad]
+    SplitOperand A4;   // [Dl*d*d][wR*Dr_pad]
+    float* T1 = nullptr;
+    double* W12 = nullptr;
+    int64_t Dl_pad = 0, Dr_pad = 0;
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// entry points used by ct_ops.cu / ct_api.cu
+// ---------------------------------------------------------------------------
+int ct_tc_available(ct_handle* h) {
+    if (!h->tc_checked) {
+        h->tc_checked = true;
+        int major = 0, minor = 0;
+        cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, h->device);
+        cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, h->device);
+        h->tc_ok = (major == 10 && minor == 3) && get_encoder();
+    }
+    return h->tc_ok ? 1 : 0;
+}
+
+size_t ct_tc_heff_ws_bytes(int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wM, int64_t wR) {
+    (void)wM;
+    const int64_t Dlp = ct_round_up(Dl, TC_BK), Drp = ct_round_up(Dr, TC_BK);
+    return split_bytes(wL * Dl, Dlp) + split_bytes(Dr, wR * Drp) + split_bytes(d * d * Dr, Dlp) +
+           split_bytes(Dl * d * d, wR * Drp) + ct_bytes((size_t)(Dl * wL * d * d * Dr), 4) +
+           ct_bytes((size_t)((d * d * wR) * (wL * d * d)), 8) + 256;
+}
+
+int ct_tc_heff_prepare(ct_handle* h, Arena& ar, HeffPlan& p) {
+    static_assert(sizeof(TcHeff) <= sizeof(p.tc_store), "HeffPlan::tc_store too small");
+    TcHeff& q = *new (p.tc_store) TcHeff();
+    const int64_t Dl = p.Dl, d = p.d, Dr = p.Dr, wL = p.wL, wM = p.wM, wR = p.wR;
+    q.Dl_pad = ct_round_up(Dl, TC_BK);
+    q.Dr_pad = ct_round_up(Dr, TC_BK);
+    q.Lp = take_split(ar, wL * Dl, q.Dl_pad);
+    q.R4 = take_split(ar, Dr, wR * q.Dr_pad);
+    q.th = take_split(ar, d * d * Dr, q.Dl_pad);
+    q.A4 = take_split(ar, Dl * d * d, wR * q.Dr_pad);
+    q.T1 = ar.take<float>((size_t)(Dl * wL * d * d * Dr));
+    q.W12 = ar.take<double>((size_t)((d * d * wR) * (wL * d * d)));
+    if (!q.Lp.lo || !q.R4.lo || !q.th.lo || !q.A4.lo || !q.T1 || !q.W12) return CT_ERR_OOM;
+    CT_TRY(ct_build_w12(h, p.W1, p.W2, q.W12, wL, d, wM, wR));
+    // L[wL, Dl, Dl'] -> Lp[(wL, Dl')][Dl]
+    CT_TRY(pack_launch(h, pack_desc(p.L, wL * Dl, Dl, Dl * Dl, 1, Dl, Dl, q.Lp), false, nullptr));
+    // R[wR, Dr, Dr'] -> R4[Dr'][(wR, Dr)] with per-wR padding
+    {
+        PackDesc pd{};
+        pd.src = p.R;
+        pd.rows = Dr; pd.R0 = Dr; pd.s_r1 = 0; pd.s_r0 = 1;
+        pd.K1 = wR; pd.K0 = Dr; pd.K0p = q.Dr_pad; pd.s_k1 = Dr * Dr; pd.s_k0 = Dr;
+        pd.hi = q.R4.hi; pd.lo = q.R4.lo; pd.ldk = wR * q.Dr_pad;
+        pd.scale = 1.0;
+        CT_TRY(pack_launch(h, pd, false, nullptr));
+    }
+    // padding columns of A4 are never written by the MPO leg: zero them once
+    CT_CUDA(h, cudaMemsetAsync(q.A4.hi, 0, (size_t)(q.A4.rows * q.A4.ldk) * 4, h->stream));
+    CT_CUDA(h, cudaMemsetAsync(q.A4.lo, 0, (size_t)(q.A4.rows * q.A4.ldk) * 4, h->stream));
+    p.tc = &q;
+    return CT_OK;
+}
+
+int ct_tc_heff_run(ct_handle* h, const HeffPlan& p, const double* theta, double* out, const int* skip) {
+    const TcHeff& q = *(const TcHeff*)p.tc;
+    const int64_t Dl = p.Dl, d = p.d, Dr = p.Dr, wL = p.wL, wR = p.wR;
+    const int64_t n1 = d * d * Dr;
+    // theta[Dl, n1] -> th[n1][Dl]
+    CT_TRY(pack_launch(h, pack_desc(theta, n1, n1, 0, 1, Dl, n1, q.th), false, skip));
+    {   // T1[Dl'][wL][n1] (fp32) = Lp . th^T
+        TcEpi e{};
+        e.C = q.T1; e.out_fp64 = 0; e.M0 = Dl; e.sCm1 = n1; e.sCm0 = wL * n1; e.alpha = 1.0; e.beta = 0.0;
+        CT_TRY(tc_gemm_launch(h, q.Lp, q.th, wL * Dl, n1, e, skip));
+    }
+    {   // A4[(Dl' t1 t2)][(wR, Dr)] = W12 . T1
+        MpoTcDesc m{};
+        m.O = Dl; m.K = wL * d * d; m.J = d * d * wR; m.I = Dr;
+        m.in = q.T1; m.sIo = wL * d * d * Dr; m.sIk = Dr; m.sIi = 1;
+        const int64_t K4 = wR * q.Dr_pad;
+        m.hi = q.A4.hi; m.lo = q.A4.lo; m.sOo = d * d * K4; m.sOi = 1; m.J0 = wR; m.sOj1 = K4; m.sOj0 = q.Dr_pad;
+        m.Wt = q.W12; m.skip = skip;
+        CT_TRY(mpo_tc_launch(h, m));
+    }
+    {   // out[(Dl' t1 t2)][Dr'] = A4 . R4^T  (fp64)
+        TcEpi e{};
+        e.C = out; e.out_fp64 = 1; e.M0 = Dl * d * d; e.sCm1 = 0; e.sCm0 = Dr; e.alpha = 1.0; e.beta = 0.0;
+        CT_TRY(tc_gemm_launch(h, q.A4, q.R4, Dl * d * d, Dr, e, skip));
+    }
+    return CT_OK;
+}
+
+size_t ct_tc_env_ws_bytes(int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR) {
+    const int64_t Dlp = ct_round_up(Dl, TC_BK), Drp = ct_round_up(Dr, TC_BK);
+    const int64_t K3l = ct_round_up(Dl * d, TC_BK), K3r = ct_round_up(d * Dr, TC_BK);
+    const size_t wt = ct_bytes((size_t)((wL * d) * (wR * d)), 8);
+    const size_t left = split_bytes(wL * Dl, Dlp) + split_bytes(d * Dr, Dlp) +
+                        ct_bytes((size_t)(Dl * wL * d * Dr), 4) + split_bytes(wR * Dr, K3l) + split_bytes(Dr, K3l) +
+                        wt;
+    const size_t right = split_bytes(wR * Dr, Drp) + split_bytes(d * Dl, Drp) +
+                         ct_bytes((size_t)(Dr * wR * d * Dl), 4) + split_bytes(wL * Dl, K3r) +
+                         split_bytes(Dl, K3r) + wt;
+    return std::max(left, right) + 1024;
+}
+
+int ct_tc_env_left_run(ct_handle* h, Arena& ar, const double* Lp, const double* A, const double* W, double* Ln,
+                       int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR) {
+    const int64_t Dlp = ct_round_up(Dl, TC_BK);
+    const int64_t K3 = ct_round_up(Dl * d, TC_BK);
+    const int64_t n1 = d * Dr;
+    SplitOperand La = take_split(ar, wL * Dl, Dlp);
+    SplitOperand Ab = take_split(ar, n1, Dlp);
+    float* T1 = ar.take<float>((size_t)(Dl * wL * n1));
+    SplitOperand A3 = take_split(ar, wR * Dr, K3);
+    SplitOperand B3 = take_split(ar, Dr, K3);
+    double* Wt = ar.take<double>((size_t)((d * wR) * (wL * d)));
+    if (!La.lo || !Ab.lo || !T1 || !A3.lo || !B3.lo || !Wt) return CT_ERR_OOM;
+    CT_TRY(ct_build_wt_left(h, W, Wt, wL, d, wR));
+    CT_TRY(pack_launch(h, pack_desc(Lp, wL * Dl, Dl, Dl * Dl, 1, Dl, Dl, La), false, nullptr));
+    CT_TRY(pack_launch(h, pack_desc(A, n1, n1, 0, 1, Dl, n1, Ab), false, nullptr));
+    {   // T1[Dl'][wL][(s Dr)]
+        TcEpi e{};
+        e.C = T1; e.out_fp64 = 0; e.M0 = Dl; e.sCm1 = n1; e.sCm0 = wL * n1; e.alpha = 1.0;
+        CT_TRY(tc_gemm_launch(h, La, Ab, wL * Dl, n1, e, nullptr));
+    }
+    CT_CUDA(h, cudaMemsetAsync(A3.hi, 0, (size_t)(A3.rows * A3.ldk) * 4, h->stream));
+    CT_CUDA(h, cudaMemsetAsync(A3.lo, 0, (size_t)(A3.rows * A3.ldk) * 4, h->stream));
+    {   // A3[(wR Dr)][(Dl' s')] = Wt . T1
+        MpoTcDesc m{};
+        m.O = Dl; m.K = wL * d; m.J = d * wR; m.I = Dr;
+        m.in = T1; m.sIo = wL * d * Dr; m.sIk = Dr; m.sIi = 1;
+        m.hi = A3.hi; m.lo = A3.lo; m.sOo = d; m.sOi = K3; m.J0 = wR; m.sOj1 = 1; m.sOj0 = Dr * K3;
+        m.Wt = Wt;
+        CT_TRY(mpo_tc_launch(h, m));
+    }
+    // B3[Dr'][(Dl' s')] = A[Dl', s', Dr']
+    CT_TRY(pack_launch(h, pack_desc(A, Dr, Dr, 0, 1, Dl * d, Dr, B3), false, nullptr));
+    TcEpi e{};
+    e.C = Ln; e.out_fp64 = 1; e.M0 = wR * Dr; e.sCm1 = 0; e.sCm0 = Dr; e.alpha = 1.0;
+    return tc_gemm_launch(h, A3, B3, wR * Dr, Dr, e, nullptr);
+}
+
+int ct_tc_env_right_run(ct_handle* h, Arena& ar, const double* Rn, const double* A, const double* W, double* Rp,
+                        int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR) {
+    const int64_t Drp = ct_round_up(Dr, TC_BK);
+    const int64_t K3 = ct_round_up(d * Dr, TC_BK);
+    SplitOperand Ra = take_split(ar, wR * Dr, Drp);
+    SplitOperand Ab = take_split(ar, d * Dl, Drp);
+    float* T1 = ar.take<float>((size_t)(Dr * wR * d * Dl));
+    SplitOperand A3 = take_split(ar, wL * Dl, K3);
+    SplitOperand B3 = take_split(ar, Dl, K3);
+    double* Wt = ar.take<double>((size_t)((wL * d) * (wR * d)));
+    if (!Ra.lo || !Ab.lo || !T1 || !A3.lo || !B3.lo || !Wt) return CT_ERR_OOM;
+    CT_TRY(ct_build_wt_right(h, W, Wt, wL, d, wR));
+    // R[wR, Dr, Dr'] -> Ra[(wR, Dr')][Dr]
+    CT_TRY(pack_launch(h, pack_desc(Rn, wR * Dr, Dr, Dr * Dr, 1, Dr, Dr, Ra), false, nullptr));
+    // A[Dl, s, Dr] -> Ab[(s, Dl)][Dr]   (row n' = s*Dl + Dl_idx)
+    CT_TRY(pack_launch(h, pack_desc(A, d * Dl, Dl, Dr, d * Dr, Dr, 1, Ab), true, nullptr));
+    {   // T1[Dr'][wR][s][Dl]
+        TcEpi e{};
+        e.C = T1; e.out_fp64 = 0; e.M0 = Dr; e.sCm1 = d * Dl; e.sCm0 = wR * d * Dl; e.alpha = 1.0;
+        CT_TRY(tc_gemm_launch(h, Ra, Ab, wR * Dr, d * Dl, e, nullptr));
+    }
+    CT_CUDA(h, cudaMemsetAsync(A3.hi, 0, (size_t)(A3.rows * A3.ldk) * 4, h->stream));
+    CT_CUDA(h, cudaMemsetAsync(A3.lo, 0, (size_t)(A3.rows * A3.ldk) * 4, h->stream));
+    {   // A3[(wL Dl)][(s' Dr')] = Wt . T1
+        MpoTcDesc m{};
+        m.O = Dr; m.K = wR * d; m.J = wL * d; m.I = Dl;
+        m.in = T1; m.sIo = wR * d * Dl; m.sIk = Dl; m.sIi = 1;
+        m.hi = A3.hi; m.lo = A3.lo; m.sOo = 1; m.sOi = K3; m.J0 = d; m.sOj1 = Dl * K3; m.sOj0 = Dr;
+        m.Wt = Wt;
+        CT_TRY(mpo_tc_launch(h, m));
+    }
+    // B3[Dl'][(s' Dr')] = A natural layout
+    CT_TRY(pack_launch(h, pack_desc(A, Dl, Dl, 0, d * Dr, d * Dr, 1, B3), true, nullptr));
+    TcEpi e{};
+    e.C = Rp; e.out_fp64 = 1; e.M0 = wL * Dl; e.sCm1 = 0; e.sCm0 = Dl; e.alpha = 1.0;
+    return tc_gemm_launch(h, A3, B3, wL * Dl, Dl, e, nullptr);
+}
+
+size_t ct_tc_gemm_ws_bytes(int64_t m, int64_t n, int64_t k) {
+    const int64_t kp = ct_round_up(k, TC_BK);
+    return split_bytes(m, kp) + split_bytes(n, kp) + 512;
+}
+
+int ct_tc_gemm(ct_handle* h, Arena& ar, int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha,
+               const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc) {
+    const int64_t kp = ct_round_up(k, TC_BK);
+    SplitOperand a = take_split(ar, m, kp);
+    SplitOperand b = take_split(ar, n, kp);
+    if (!a.lo || !b.lo) return CT_ERR_OOM;
+    // op(A)[i, p]: trans_a=0 -> A[i*lda + p] (k contiguous), 1 -> A[p*lda + i]
+    CT_TRY(pack_launch(h, trans_a ? pack_desc(A, m, m, 0, 1, k, lda, a) : pack_desc(A, m, m, 0, lda, k, 1, a),
+                       !trans_a, nullptr));
+    // op(B)[p, j]: trans_b=0 -> B[p*ldb + j] -> rows j, k stride ldb; 1 -> B[j*ldb + p]
+    CT_TRY(pack_launch(h, trans_b ? pack_desc(B, n, n, 0, ldb, k, 1, b) : pack_desc(B, n, n, 0, 1, k, ldb, b),
+                       trans_b != 0, nullptr));
+    TcEpi e{};
+    e.C = C; e.out_fp64 = 1; e.M0 = m; e.sCm1 = 0; e.sCm0 = ldc; e.alpha = alpha; e.beta = beta;
+    return tc_gemm_launch(h, a, b, m, n, e, nullptr);
+}
+
+// Times launches of the raw TF32x3 GEMM kernel (operands already split and
+// resident) with CUDA events on the handle's stream.
+extern "C" CT_API int ct_tc_gemm_time(ct_handle* h, int64_t m, int64_t n, int64_t k, int reps, double* ms_per_launch) {
+    if (!h || !ms_per_launch || m <= 0 || n <= 0 || k <= 0 || reps <= 0) return CT_ERR_INVALID;
+    if (!ct_tc_available(h)) return CT_ERR_UNSUPPORTED;
+    const int64_t kp = ct_round_up(k, TC_BK);
+    float* C = nullptr;
+    CT_TRY(ct_reserve(h, split_bytes(m, kp) + split_bytes(n, kp) + ct_bytes((size_t)(m * n), 4) + 1024));
+    Arena ar(h);
+    SplitOperand a = take_split(ar, m, kp);
+    SplitOperand b = take_split(ar, n, kp);
+    C = ar.take<float>((size_t)(m * n));
+    if (!a.lo || !b.lo || !C) return CT_ERR_OOM;
+    CT_CUDA(h, cudaMemsetAsync(a.hi, 0, (size_t)(m * kp) * 4, h->stream));
+    CT_CUDA(h, cudaMemsetAsync(a.lo, 0, (size_t)(m * kp) * 4, h->stream));
+    CT_CUDA(h, cudaMemsetAsync(b.hi, 0, (size_t)(n * kp) * 4, h->stream));
+    CT_CUDA(h, cudaMemsetAsync(b.lo, 0, (size_t)(n * kp) * 4, h->stream));
+    TcEpi e{};
+    e.C = C; e.out_fp64 = 0; e.M0 = m; e.sCm1 = 0; e.sCm0 = n; e.alpha = 1.0;
+    for (int i = 0; i < 2; ++i) CT_TRY(tc_gemm_launch(h, a, b, m, n, e, nullptr));
+    cudaEvent_t e0, e1;
+    CT_CUDA(h, cudaEventCreate(&e0));
+    CT_CUDA(h, cudaEventCreate(&e1));
+    CT_CUDA(h, cudaEventRecord(e0, h->stream));
+    for (int i = 0; i < reps; ++i) CT_TRY(tc_gemm_launch(h, a, b, m, n, e, nullptr));
+    CT_CUDA(h, cudaEventRecord(e1, h->stream));
+    CT_CUDA(h, cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CT_CUDA(h, cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms_per_launch = (double)ms / reps;
+    return CT_OK;
+}

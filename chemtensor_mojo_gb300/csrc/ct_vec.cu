@@ -353,30 +353,30 @@ int elem_grid(ct_handle* h, int64_t n) {
 
 int ct_reduce_dot(ct_handle* h, int64_t n, const double* x, const double* y, double* d_out, const int* skip) {
     const int g = grid_for(h, n);
-    partial_kernel<0><<<g, RT, 0, h->stream>>>(n, x, y, h->d_partials, skip);
-    finish_store_kernel<<<1, RT, 0, h->stream>>>(h->d_partials, g, d_out, skip);
+    partial_kernel<0><<<g, RT, 0, h->stream>>>(n, x, y, h->d_partials, skip); ct_note_launch();
+    finish_store_kernel<<<1, RT, 0, h->stream>>>(h->d_partials, g, d_out, skip); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
 
 int ct_reduce_nrm2sq(ct_handle* h, int64_t n, const double* x, double* d_out, const int* skip) {
     const int g = grid_for(h, n);
-    partial_kernel<1><<<g, RT, 0, h->stream>>>(n, x, nullptr, h->d_partials, skip);
-    finish_store_kernel<<<1, RT, 0, h->stream>>>(h->d_partials, g, d_out, skip);
+    partial_kernel<1><<<g, RT, 0, h->stream>>>(n, x, nullptr, h->d_partials, skip); ct_note_launch();
+    finish_store_kernel<<<1, RT, 0, h->stream>>>(h->d_partials, g, d_out, skip); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
 
 int ct_scale_by_inv_sqrt(ct_handle* h, int64_t n, const double* x, double* y, const double* d_nsq,
                          const int* skip, int zero_code) {
-    scale_inv_sqrt_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, x, y, d_nsq, skip, h->d_status, zero_code);
+    scale_inv_sqrt_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, x, y, d_nsq, skip, h->d_status, zero_code); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
 
 int ct_fill(ct_handle* h, double* x, int64_t n, double v) {
     if (n <= 0) return CT_OK;
-    fill_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(x, n, v);
+    fill_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(x, n, v); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
@@ -390,7 +390,7 @@ int ct_copy(ct_handle* h, double* dst, const double* src, int64_t n) {
 int ct_identity_env(ct_handle* h, double* E, int64_t w, int64_t D) {
     const int64_t n = w * D * D;
     if (n <= 0) return CT_OK;
-    identity_env_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(E, w, D);
+    identity_env_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(E, w, D); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
@@ -416,32 +416,32 @@ int ct_permute_launch(ct_handle* h, const double* in, double* out, int rank, con
         a.in_stride_of_out_axis[ax] = in_stride[p];
     }
     if (a.n == 0) return CT_OK;
-    permute_kernel<<<elem_grid(h, a.n), 256, 0, h->stream>>>(in, out, a);
+    permute_kernel<<<elem_grid(h, a.n), 256, 0, h->stream>>>(in, out, a); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
 
 int ct_vec_axpy_launch(ct_handle* h, int64_t n, double alpha, const double* x, double* y) {
-    axpy_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, alpha, x, y);
+    axpy_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, alpha, x, y); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
 int ct_vec_scale_launch(ct_handle* h, int64_t n, double alpha, double* x) {
-    scale_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, alpha, x);
+    scale_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, alpha, x); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
 
 int ct_lanczos_init(ct_handle* h, int max_iter) {
-    init_lanczos_flags<<<1, 1, 0, h->stream>>>(h->d_flags, max_iter);
+    init_lanczos_flags<<<1, 1, 0, h->stream>>>(h->d_flags, max_iter); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
 
 int ct_lanczos_alpha(ct_handle* h, int64_t n, const double* vj, const double* w, int j, const int* skip) {
     const int g = grid_for(h, n);
-    partial_kernel<0><<<g, RT, 0, h->stream>>>(n, vj, w, h->d_partials, skip);
-    lanczos_alpha_finish<<<1, RT, 0, h->stream>>>(h->d_partials, g, h->d_scalars, j, skip);
+    partial_kernel<0><<<g, RT, 0, h->stream>>>(n, vj, w, h->d_partials, skip); ct_note_launch();
+    lanczos_alpha_finish<<<1, RT, 0, h->stream>>>(h->d_partials, g, h->d_scalars, j, skip); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
@@ -449,9 +449,9 @@ int ct_lanczos_alpha(ct_handle* h, int64_t n, const double* vj, const double* w,
 int ct_lanczos_update(ct_handle* h, int64_t n, double* w, const double* vj, const double* vjm1, int j,
                       double beta_threshold, const int* skip) {
     const int g = grid_for(h, n);
-    lanczos_update_kernel<<<g, RT, 0, h->stream>>>(n, w, vj, vjm1, h->d_scalars, j, h->d_partials, skip);
+    lanczos_update_kernel<<<g, RT, 0, h->stream>>>(n, w, vj, vjm1, h->d_scalars, j, h->d_partials, skip); ct_note_launch();
     lanczos_beta_finish<<<1, RT, 0, h->stream>>>(h->d_partials, g, h->d_scalars, h->d_flags, j,
-                                                 beta_threshold, skip);
+                                                 beta_threshold, skip); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
@@ -464,17 +464,17 @@ int ct_lanczos_reorth_beta(ct_handle* h, int64_t n, double* w, const double* V, 
     int g = grid_for(h, n);
     if ((int64_t)g * nvec > CT_NPARTIALS) g = CT_NPARTIALS / nvec;
     double* coeff = h->d_scalars + SC_MISC;
-    multidot_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, h->d_partials, skip);
-    multidot_finish<<<1, RT, 0, h->stream>>>(h->d_partials, g, nvec, coeff, skip);
-    multiaxpy_norm_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, coeff, h->d_partials, skip);
+    multidot_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, h->d_partials, skip); ct_note_launch();
+    multidot_finish<<<1, RT, 0, h->stream>>>(h->d_partials, g, nvec, coeff, skip); ct_note_launch();
+    multiaxpy_norm_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, coeff, h->d_partials, skip); ct_note_launch();
     lanczos_beta_finish<<<1, RT, 0, h->stream>>>(h->d_partials, g, h->d_scalars, h->d_flags, j,
-                                                 beta_threshold, skip);
+                                                 beta_threshold, skip); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
 
 int ct_lanczos_next(ct_handle* h, int64_t n, const double* w, double* vnext, int j, const int* skip) {
-    lanczos_next_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, w, vnext, h->d_scalars, j, skip);
+    lanczos_next_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, w, vnext, h->d_scalars, j, skip); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
@@ -490,13 +490,13 @@ int ct_tridiag_eig(ct_handle* h, int max_iter, double tol, int max_rotations) {
     }
     const int converged = (max_rotations <= 0);
     const int cap = converged ? 200000 : max_rotations;
-    tridiag_jacobi_kernel<<<1, 32, smem, h->stream>>>(h->d_scalars, h->d_flags, h->d_status, tol, cap, converged);
+    tridiag_jacobi_kernel<<<1, 32, smem, h->stream>>>(h->d_scalars, h->d_flags, h->d_status, tol, cap, converged); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
 
 int ct_ritz(ct_handle* h, int64_t n, const double* V, int64_t ldv, double* out) {
-    ritz_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, V, ldv, h->d_scalars, h->d_flags, out);
+    ritz_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, V, ldv, h->d_scalars, h->d_flags, out); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }

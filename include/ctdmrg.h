@@ -65,6 +65,8 @@ CT_API int ct_get_status(ct_handle* h, int* status_out);
 CT_API const char* ct_error_string(int status);
 CT_API const char* ct_last_error(ct_handle* h);
 CT_API int ct_version(void);
+/* number of kernels this library has launched in the process (all handles) */
+CT_API int64_t ct_launch_count(void);
 /* bytes of handle-owned scratch currently reserved */
 CT_API int ct_workspace_bytes(ct_handle* h, int64_t* bytes_out);
 /* cap on handle-owned scratch in bytes (0 = unlimited); growth beyond it -> CT_ERR_OOM */
@@ -202,6 +204,11 @@ CT_API int ct_energy_grad(ct_handle* h, int prec, int nsites, int d, const int64
                    const double* const* mpo_sites, const int64_t* bond_dims,
                    const double* const* mps_sites, double* const* grad_sites,
                    int checkpoint_every, double* energy_host);
+
+/* ---- measurement hook (no reference counterpart) --------------------------
+ * Average device time of one launch of the TF32x3 tcgen05 GEMM kernel on an
+ * m x n x k problem with operands already split and resident in HBM.       */
+CT_API int ct_tc_gemm_time(ct_handle* h, int64_t m, int64_t n, int64_t k, int reps, double* ms_per_launch);
 
 #ifdef __cplusplus
 }

@@ -41,22 +41,55 @@ def tfim12():
     return mpo, mps
 
 
-@pytest.mark.parametrize("max_rot", [200, 0])
-def test_tfim12_matches_oracle(ctx, tfim12, max_rot):
+def test_tfim12_trajectory_matches_oracle(ctx, tfim12):
+    """Converged eigensolve: whole 6-sweep trajectory equals the oracle's."""
     ct = ct_mod()
     mpo, mps = tfim12
     p = ct.DMRGParams(num_sweeps=6, chi_max=32, eps_trunc=1e-10, max_krylov_iter=20, krylov_tol=1e-10,
-                      energy_tol=0.0, max_rotations=max_rot)
+                      energy_tol=0.0, max_rotations=0)
     E, out, stats = run_device(ctx, mpo, mps, p)
     pref = od.DMRGParams(6, 32, 1e-10, 20, 1e-10, 0.0)
     log = od.SweepLog()
-    E_ref, mps_ref = od.dmrg_two_site(mpo, mps, pref, eig="jacobi" if max_rot else "exact", log=log)
+    E_ref, mps_ref = od.dmrg_two_site(mpo, mps, pref, eig="exact", log=log)
     assert out.bond_dims == [1] + [a.shape[2] for a in mps_ref]
     np.testing.assert_allclose(stats.sweep_energies, log.energies, rtol=1e-10, atol=0)
     assert abs(E - E_ref) <= 1e-10 * abs(E_ref)
     np.testing.assert_allclose(stats.discarded, log.discarded, atol=1e-12)
-    if max_rot == 0:
-        assert abs(E - ed.ground_energy(mpo)) < 1e-8
+    assert abs(E - ed.ground_energy(mpo)) < 1e-8
+
+
+def test_tfim12_reference_jacobi_local_parity(ctx, tfim12):
+    """Reference semantics (Jacobi capped at 200 rotations, dmrg.mojo:507-598).
+
+    The capped eigensolve is ill-conditioned: a 1e-15 relative perturbation of
+    H_eff moves single local energies by up to ~4e-7 and whole trajectories by
+    ~1e-3 (tests/test_oracle.py::test_capped_jacobi_is_chaotic).  Parity is
+    therefore checked per local update along the device's own trajectory:
+    every device Lanczos result equals the oracle's on the same inputs to
+    1e-6, and both runs end in the same energy band.
+    """
+    ct = ct_mod()
+    mpo_a, mps_a = tfim12
+    mps = ct.mps_from_arrays(ctx, mps_a)
+    mpo = ct.mpo_from_arrays(ctx, mpo_a)
+    p = ct.DMRGParams(num_sweeps=2, chi_max=32, eps_trunc=1e-10, max_krylov_iter=20, krylov_tol=1e-10,
+                      energy_tol=0.0)
+    ws = ct.DMRGWorkspace(mps, mpo, ctx)
+    N = mps.num_sites()
+    worst = 0.0
+    for sweep in range(2):
+        for l2r, order in ((True, range(N - 1)), (False, range(N - 2, -1, -1))):
+            for i in order:
+                th = od.build_two_site_theta(mps.sites[i].tensor.to_numpy(), mps.sites[i + 1].tensor.to_numpy())
+                E_ref, _ = od.lanczos_two_site_optimize(th, ws.L_env[i].to_numpy(), ws.R_env[i + 2].to_numpy(),
+                                                        mpo_a[i], mpo_a[i + 1], 20, 1e-10)
+                E = ct.dmrg_local_update_two_site(i, mps, mpo, ws, p, ctx, l2r)
+                worst = max(worst, abs(E - E_ref))
+    assert worst < 1e-6
+    E_full, _, _ = run_device(ctx, mpo_a, mps_a, ct.DMRGParams(num_sweeps=6, chi_max=32, eps_trunc=1e-10,
+                                                               max_krylov_iter=20, krylov_tol=1e-10,
+                                                               energy_tol=0.0))
+    assert abs(E_full - ed.ground_energy(mpo_a)) < 2e-2
 
 
 def test_xxx_4site_exact(ctx):

@@ -23,7 +23,7 @@ def lib():
 
 def header_symbols():
     text = (ROOT / "include" / "ctdmrg.h").read_text()
-    return re.findall(r"^CT_API\s+(?:const\s+char\s*\*|int)\s+(ct_\w+)\s*\(", text, flags=re.M)
+    return re.findall(r"^CT_API\s+(?:const\s+char\s*\*|int64_t|int)\s+(ct_\w+)\s*\(", text, flags=re.M)
 
 
 def test_library_exports_every_header_symbol(lib):
@@ -35,7 +35,7 @@ def test_library_exports_every_header_symbol(lib):
 
 def test_bindings_cover_header(lib):
     from chemtensor_mojo_gb300 import _lib
-    bound = set(_lib.SIGNATURES) | set(_lib.STRING_FUNCS)
+    bound = set(_lib.SIGNATURES) | set(_lib.STRING_FUNCS) | set(_lib.INT64_FUNCS)
     assert set(header_symbols()) == bound
 
 
