@@ -63,7 +63,41 @@ def parse():
     ap.add_argument("--chi", type=int, default=1024)
     ap.add_argument("--L", type=int, default=L_SITES)
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64/roofline/CPU side measurements")
+    ap.add_argument("--mode", default="sweep", choices=["sweep", "heff"],
+                    help="heff: only centre-bond H_eff applies (a small, fixed workload for profilers)")
     return ap.parse_args()
+
+
+def heff_mode(args):
+    """W + K centre-bond H_eff applies at (chi, D=5, d=2); one JSON line (profiling workload)."""
+    import torch
+    import chemtensor_mojo_gb300 as ct
+    from chemtensor_mojo_gb300 import _lib
+    ctx = ct.get_context(0)
+    chi = args.chi
+    mpo = ct.create_spin_half_xxz_mpo(ctx, 8, 1.0)
+    W = mpo.sites[3]
+    g = torch.Generator(device="cpu").manual_seed(5)
+    dev = ctx.torch_device
+    th = ct.DenseTensor(torch.randn(chi * 4 * chi, generator=g, dtype=torch.float64).to(dev), [chi, 2, 2, chi])
+    Le = ct.DenseTensor(torch.randn(MPO_D * chi * chi, generator=g, dtype=torch.float64).to(dev), [MPO_D, chi, chi])
+    Re = ct.DenseTensor(torch.randn(MPO_D * chi * chi, generator=g, dtype=torch.float64).to(dev), [MPO_D, chi, chi])
+    for _ in range(args.warmup):
+        ct.apply_two_site_heff(th, Le, Re, W, W, ctx, prec=args.prec)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = _lib.launch_count()
+    e0.record()
+    for _ in range(args.steps):
+        ct.apply_two_site_heff(th, Le, Re, W, W, ctx, prec=args.prec)
+    e1.record()
+    torch.cuda.synchronize()
+    s = e0.elapsed_time(e1) * 1e-3 / max(args.steps, 1)
+    F = heff_flops(chi, chi)
+    print(json.dumps({"metric": "H_eff apply seconds", "value": s, "unit": "s/apply", "tflops": F / s / 1e12,
+                      "dtype": args.prec, "config": {"workload": f"centre-bond H_eff chi={chi} D=5 d=2"},
+                      "steps": args.steps, "warmup": args.warmup,
+                      "gpu_launches": _lib.launch_count() - n0}), flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -196,6 +230,9 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         reference_arm(args, rank)
+        return
+    if args.mode == "heff":
+        heff_mode(args)
         return
 
     import torch

@@ -40,13 +40,14 @@ class ct_dmrg_params(C.Structure):
     _fields_ = [("num_sweeps", C.c_int), ("chi_max", C.c_int), ("eps_trunc", C.c_double),
                 ("max_krylov_iter", C.c_int), ("krylov_tol", C.c_double), ("energy_tol", C.c_double),
                 ("two_site", C.c_int), ("verbose", C.c_int), ("prec", C.c_int), ("max_rotations", C.c_int),
-                ("reorth", C.c_int)]
+                ("reorth", C.c_int), ("final_rayleigh", C.c_int)]
 
 
 class ct_dmrg_stats(C.Structure):
     _fields_ = [("seconds_total", C.c_double), ("seconds_lanczos", C.c_double), ("seconds_svd", C.c_double),
                 ("seconds_env", C.c_double), ("heff_flops", C.c_double), ("env_flops", C.c_double),
-                ("heff_applies", C.c_int64), ("local_updates", C.c_int64), ("max_discarded", C.c_double)]
+                ("heff_applies", C.c_int64), ("local_updates", C.c_int64), ("max_discarded", C.c_double),
+                ("energy_rayleigh", C.c_double)]
 
 
 P = C.c_void_p
@@ -79,7 +80,7 @@ SIGNATURES = {
     "ct_lanczos2": [P, I32, P, P, P, P, P, P, I64, I64, I64, I64, I64, I64, I32, D, I32, I32,
                     C.POINTER(D), C.POINTER(I32), C.POINTER(D), C.POINTER(D)],
     "ct_svd_trunc": [P, P, I64, I64, I64, D, P, P, P, C.POINTER(I64)],
-    "ct_svd_split": [P, P, I64, I64, I64, I64, D, I32, P, P, P, C.POINTER(I64), C.POINTER(D)],
+    "ct_svd_split": [P, I32, P, I64, I64, I64, I64, D, I32, P, P, P, C.POINTER(I64), C.POINTER(D)],
     "ct_dmrg_two_site": [P, C.POINTER(ct_dmrg_params), I32, I32, C.POINTER(I64), PP, C.POINTER(I64), PP,
                          C.POINTER(I64), C.POINTER(D), C.POINTER(D), C.POINTER(I32), C.POINTER(D),
                          C.POINTER(ct_dmrg_stats)],

@@ -456,10 +456,11 @@ int ct_svd_trunc(ct_handle* h, const double* M, int64_t m, int64_t n, int64_t ch
     return CT_OK;
 }
 
-int ct_svd_split(ct_handle* h, const double* theta, int64_t Dl, int64_t d, int64_t Dr, int64_t chi_max,
+int ct_svd_split(ct_handle* h, int prec, const double* theta, int64_t Dl, int64_t d, int64_t Dr, int64_t chi_max,
                  double eps_trunc, int left_to_right, double* A_out, double* B_out, double* S_out, int64_t* chi_host,
                  double* discarded_host) {
     CT_NULLCHK(h, h);
+    CT_TRY(check_prec(h, prec));
     CT_NULLCHK(h, theta);
     CT_NULLCHK(h, A_out);
     CT_NULLCHK(h, B_out);
@@ -470,14 +471,15 @@ int ct_svd_split(ct_handle* h, const double* theta, int64_t Dl, int64_t d, int64
     if (chi_max < 0) return CT_ERR_SHAPE;
     const int64_t m = Dl * d, n = d * Dr;
     const int mode = left_to_right ? 0 : 1;
-    CT_TRY(ct_reserve(h, ct_svd_ws_bytes(m, n, mode)));
+    CT_TRY(ct_reserve(h, ct_split_ws_bytes(prec, m, n, chi_max, mode)));
     Arena ar(h);
     // |theta|^2 in FP64 on the device (dmrg.mojo:176)
     CT_TRY(ct_reduce_nrm2sq(h, m * n, theta, h->d_scalars + SC_THETA_NSQ, nullptr));
     double tn = 0.0;
     CT_CUDA(h, cudaMemcpyAsync(&tn, h->d_scalars + SC_THETA_NSQ, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     SvdOut o;
-    CT_TRY(ct_svd_run(h, ar, theta, m, n, chi_max, eps_trunc, mode, A_out, B_out, S_out, &o));
+    CT_TRY(ct_split_run(h, ar, prec, theta, m, n, chi_max, eps_trunc, mode, A_out, B_out, S_out,
+                        h->d_scalars + SC_THETA_NSQ, &o));
     CT_TRY(check_status(h));
     *chi_host = o.chi;
     if (discarded_host) *discarded_host = (tn > 0.0) ? (tn - o.sum_s2_kept) / tn : 0.0;

@@ -151,7 +151,7 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         const int64_t wL = mpo_dims[i], wM = mpo_dims[i + 1], wR = mpo_dims[i + 2];
         const int64_t m = Dl * d, n = d * Dr;
         size_t need = ct_lanczos_ws_bytes(prec, Dl, d, Dr, wL, wM, wR, P->max_krylov_iter);
-        need = std::max(need, ct_svd_ws_bytes(m, n, l2r ? 0 : 1));
+        need = std::max(need, ct_split_ws_bytes(prec, m, n, P->chi_max, l2r ? 0 : 1));
         const int64_t chi_ub = std::min<int64_t>(std::min(m, n), P->chi_max);
         need = std::max(need, l2r ? ct_env_ws_bytes(prec, Dl, d, chi_ub, wL, wM)
                                   : ct_env_ws_bytes(prec, chi_ub, d, Dr, wM, wR));
@@ -189,8 +189,8 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         {
             Arena ar(h);
             // kept bond bound by the capacity of the sites it is written into
-            CT_TRY(ct_svd_run(h, ar, th_opt.p, m, n, P->chi_max, P->eps_trunc, l2r ? 0 : 1, mps_sites[i],
-                              mps_sites[i + 1], nullptr, &so));
+            CT_TRY(ct_split_run(h, ar, prec, th_opt.p, m, n, P->chi_max, P->eps_trunc, l2r ? 0 : 1, mps_sites[i],
+                                mps_sites[i + 1], nullptr, h->d_scalars + SC_THETA_NSQ, &so));
         }
         CT_CUDA(h, cudaEventRecord(ev_s.b, h->stream));
         const int64_t chi = so.chi;
@@ -253,6 +253,13 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         prev = energy;
     }
     *energy_host = energy;
+    st.energy_rayleigh = NAN;
+    if (P->final_rayleigh) {
+        double e = 0.0, nsq = 0.0;
+        CT_TRY(ct_mps_expectation(h, CT_PREC_FP64, N, d, mpo_dims, mpo_sites, bd, (const double* const*)mps_sites,
+                                  &e, &nsq));
+        st.energy_rayleigh = e / nsq;
+    }
     if (sweeps_done_host) *sweeps_done_host = sweeps_done;
     if (discarded_host)
         for (size_t k = 0; k < disc_all.size(); ++k) discarded_host[k] = disc_all[k];
@@ -294,7 +301,10 @@ int ct_mps_right_normalize(ct_handle* h, int N, int d, int64_t* bd, double* cons
         g.C = tmp.p; g.sCm = m; g.sCn = 1;
         g.alpha = 1.0; g.beta = 0.0; g.nb1 = 1; g.nb0 = 1;
         CT_TRY(ct_gemm_f64_launch(h, g));
-        CT_TRY(ct_copy(h, sites[i - 1], tmp.p, Dp * d * m));
+        // keep the running norm O(1): a long random chain's norm under- or overflows
+        CT_TRY(ct_reduce_nrm2sq(h, Dp * d * m, tmp.p, h->d_scalars + SC_NORM, nullptr));
+        CT_TRY(ct_scale_by_inv_sqrt(h, Dp * d * m, tmp.p, sites[i - 1], h->d_scalars + SC_NORM, nullptr,
+                                    CT_ERR_ZERO_NORM));
     }
     const int64_t n0 = bd[0] * d * bd[1];
     CT_TRY(ct_reduce_nrm2sq(h, n0, sites[0], h->d_scalars + SC_NORM, nullptr));
@@ -450,12 +460,3 @@ int ct_random_mps_host(int N, int d, int chi_max, uint64_t seed, int64_t* dims, 
 
 }  // extern "C"
 
-extern "C" int ct_energy_grad(ct_handle* h, int prec, int nsites, int d, const int64_t* mpo_dims,
-                              const double* const* mpo_sites, const int64_t* bond_dims,
-                              const double* const* mps_sites, double* const* grad_sites, int checkpoint_every,
-                              double* energy_host) {
-    (void)prec; (void)nsites; (void)d; (void)mpo_dims; (void)mpo_sites; (void)bond_dims; (void)mps_sites;
-    (void)grad_sites; (void)checkpoint_every; (void)energy_host;
-    if (h) ct_seterr(h, "ct_energy_grad: not built yet");
-    return CT_ERR_UNSUPPORTED;
-}

@@ -10,7 +10,21 @@ struct HeffPlan {
     double* T1 = nullptr;
     double* T3 = nullptr;
     double* W12 = nullptr;
-    // mixed form (ct_tc.cu): operand planes of the bond, constructed in place
+    // mixed-form SVD (ct_svd_mixed.cu); d_total = device |theta|^2
+size_t ct_svd_mixed_ws_bytes(int64_t m, int64_t n, int64_t chi_max, int mode);
+int ct_svd_mixed_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t chi_max,
+                     double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out);
+// the FP64 Jacobi runs in one CTA below this many doubles of X and Q
+static inline bool ct_svd_is_small(int64_t m, int64_t n, int mode) {
+    const int64_t nvec = mode ? n : m, len = mode ? m : n;
+    return (nvec * len + nvec * nvec) * 8 <= 200 * 1024;
+}
+// split dispatcher: FP64 Jacobi, or the mixed SVD for large TF32x3 problems
+size_t ct_split_ws_bytes(int prec, int64_t m, int64_t n, int64_t chi_max, int mode);
+int ct_split_run(ct_handle* h, Arena& ar, int prec, const double* M, int64_t m, int64_t n, int64_t chi_max,
+                 double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out);
+
+// mixed form (ct_tc.cu): operand planes of the bond, constructed in place
     void* tc = nullptr;
     alignas(16) unsigned char tc_store[512];
 };
@@ -53,6 +67,20 @@ int ct_lanczos_reorth_beta(ct_handle* h, int64_t n, double* w, const double* V, 
 size_t ct_svd_ws_bytes(int64_t m, int64_t n, int mode);
 int ct_svd_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t chi_max,
                double eps_trunc, int mode, double* A, double* B, double* S, SvdOut* out);
+
+// mixed-form SVD (ct_svd_mixed.cu); d_total = device |theta|^2
+size_t ct_svd_mixed_ws_bytes(int64_t m, int64_t n, int64_t chi_max, int mode);
+int ct_svd_mixed_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t chi_max,
+                     double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out);
+// the FP64 Jacobi runs in one CTA below this many doubles of X and Q
+static inline bool ct_svd_is_small(int64_t m, int64_t n, int mode) {
+    const int64_t nvec = mode ? n : m, len = mode ? m : n;
+    return (nvec * len + nvec * nvec) * 8 <= 200 * 1024;
+}
+// split dispatcher: FP64 Jacobi, or the mixed SVD for large TF32x3 problems
+size_t ct_split_ws_bytes(int prec, int64_t m, int64_t n, int64_t chi_max, int mode);
+int ct_split_run(ct_handle* h, Arena& ar, int prec, const double* M, int64_t m, int64_t n, int64_t chi_max,
+                 double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out);
 
 // mixed form (ct_tc.cu)
 size_t ct_tc_heff_ws_bytes(int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wM, int64_t wR);

@@ -43,12 +43,13 @@ class DMRGParams:
     prec: str = "fp64"
     max_rotations: int = REFERENCE_JACOBI_ROTATIONS
     reorth: bool = False
+    final_rayleigh: bool = False
 
     def to_c(self) -> _lib.ct_dmrg_params:
         return _lib.ct_dmrg_params(int(self.num_sweeps), int(self.chi_max), float(self.eps_trunc),
                                    int(self.max_krylov_iter), float(self.krylov_tol), float(self.energy_tol),
                                    int(bool(self.two_site)), int(bool(self.verbose)), _lib.PRECISIONS[self.prec],
-                                   int(self.max_rotations), int(bool(self.reorth)))
+                                   int(self.max_rotations), int(bool(self.reorth)), int(bool(self.final_rayleigh)))
 
 
 @dataclass
@@ -62,6 +63,7 @@ class DMRGStats:
     heff_applies: int = 0
     local_updates: int = 0
     max_discarded: float = 0.0
+    energy_rayleigh: float = float("nan")
     sweep_energies: List[float] = field(default_factory=list)
     discarded: List[float] = field(default_factory=list)
 
@@ -137,7 +139,7 @@ def lanczos_two_site_optimize(initial_theta: DenseTensor, L_env: DenseTensor, R_
 
 
 def split_two_site_theta_svd(theta: DenseTensor, chi_max: int, eps_trunc: float, ctx: DeviceContext | None = None,
-                             left_to_right: bool = True, return_spectrum: bool = False):
+                             left_to_right: bool = True, return_spectrum: bool = False, prec: str = "fp64"):
     """-> (A_i, A_ip1, discarded_weight[, S])."""
     ctx = ctx or get_context()
     Dl, d, _, Dr = theta.shape
@@ -148,7 +150,7 @@ def split_two_site_theta_svd(theta: DenseTensor, chi_max: int, eps_trunc: float,
     S = torch.empty(k, dtype=torch.float64, device=dev)
     chi = C.c_int64()
     disc = C.c_double()
-    ctx.call("ct_svd_split", _ptr(theta.storage), C.c_int64(Dl), C.c_int64(d), C.c_int64(Dr), C.c_int64(chi_max),
+    ctx.call("ct_svd_split", _p(prec), _ptr(theta.storage), C.c_int64(Dl), C.c_int64(d), C.c_int64(Dr), C.c_int64(chi_max),
              C.c_double(eps_trunc), int(bool(left_to_right)), _ptr(A), _ptr(B), _ptr(S), C.byref(chi),
              C.byref(disc))
     c = chi.value
@@ -183,7 +185,7 @@ def dmrg_local_update_two_site(site_index: int, mps: MatrixProductState, mpo: Ma
     E, th = lanczos_two_site_optimize(theta, workspace.L_env[i], workspace.R_env[i + 2], mpo.sites[i],
                                       mpo.sites[i + 1], ctx, params.max_krylov_iter, params.krylov_tol,
                                       params.prec, params.max_rotations, params.reorth)
-    A, B, _ = split_two_site_theta_svd(th, params.chi_max, params.eps_trunc, ctx, left_to_right)
+    A, B, _ = split_two_site_theta_svd(th, params.chi_max, params.eps_trunc, ctx, left_to_right, prec=params.prec)
     mps.sites[i] = A
     mps.sites[i + 1] = B
     mps.bond_dims[i + 1] = A.right_bond_dim()
@@ -251,7 +253,7 @@ def dmrg_two_site(ctx: DeviceContext | None, mpo: MatrixProductOperator, mps: Ma
              for i in range(N)]
     if stats is not None:
         for f in ("seconds_total", "seconds_lanczos", "seconds_svd", "seconds_env", "heff_flops", "env_flops",
-                  "heff_applies", "local_updates", "max_discarded"):
+                  "heff_applies", "local_updates", "max_discarded", "energy_rayleigh"):
             setattr(stats, f, getattr(st, f))
         stats.sweep_energies = list(sweeps)[:done.value]
         stats.discarded = list(disc)[:done.value * 2 * (N - 1)]

@@ -127,8 +127,11 @@ CT_API int ct_svd_trunc(ct_handle* h, const double* M, int64_t m, int64_t n, int
                  double eps_trunc, double* U, double* S, double* Vt, int64_t* chi_host);
 /* Two-site split (split_two_site_theta_svd, dmrg.mojo:143-252).
  * A_out[Dl,d,chi], B_out[chi,d,Dr] (capacity min(Dl*d, d*Dr) for chi),
- * S_out (may be NULL) gets the kept singular values, descending.          */
-CT_API int ct_svd_split(ct_handle* h, const double* theta, int64_t Dl, int64_t d, int64_t Dr,
+ * S_out (may be NULL) gets the kept singular values, descending.
+ * prec CT_PREC_FP64: one-sided Jacobi in FP64.  CT_PREC_TF32X3 (problems too
+ * large for one CTA): FP32 Jacobi for the subspace, FP64 re-orthonormalised
+ * canonical factor, tensor-core projection for the centre factor.         */
+CT_API int ct_svd_split(ct_handle* h, int prec, const double* theta, int64_t Dl, int64_t d, int64_t Dr,
                  int64_t chi_max, double eps_trunc, int left_to_right, double* A_out,
                  double* B_out, double* S_out, int64_t* chi_host, double* discarded_host);
 
@@ -145,6 +148,8 @@ typedef struct ct_dmrg_params {
     int prec;            /* ct_prec                                            */
     int max_rotations;   /* 200 = reference Jacobi cap; 0 = converged          */
     int reorth;          /* full FP64 reorthogonalisation                      */
+    int final_rayleigh;  /* also return <psi|H|psi>/<psi|psi> of the final MPS,
+                            contracted in FP64 (stats.energy_rayleigh)          */
 } ct_dmrg_params;
 
 typedef struct ct_dmrg_stats {
@@ -157,6 +162,7 @@ typedef struct ct_dmrg_stats {
     int64_t heff_applies;
     int64_t local_updates;
     double max_discarded;      /* largest discarded weight over the run         */
+    double energy_rayleigh;    /* FP64 Rayleigh quotient (NaN unless requested)  */
 } ct_dmrg_stats;
 
 /* Runs the sweeps in place.  mps_sites[i] are caller-owned device buffers of
