@@ -206,6 +206,13 @@ int ct_workspace_bytes(ct_handle* h, int64_t* bytes_out) {
     return CT_OK;
 }
 
+int ct_svd_sweeps(ct_handle* h, int* last_host, int64_t* total_host) {
+    CT_NULLCHK(h, h);
+    if (last_host) *last_host = h->last_svd_sweeps;
+    if (total_host) *total_host = h->total_svd_sweeps;
+    return CT_OK;
+}
+
 int ct_set_workspace_limit(ct_handle* h, int64_t bytes) {
     CT_NULLCHK(h, h);
     if (bytes < 0) return CT_ERR_INVALID;

@@ -29,6 +29,9 @@ struct ct_handle {
     size_t ws_cap = 0;
     size_t ws_limit = 0;            // 0 = unlimited
     std::string err;
+    // diagnostics: Jacobi sweeps of the last SVD split, and the running total
+    int last_svd_sweeps = 0;
+    int64_t total_svd_sweeps = 0;
     // tensor-core path state
     bool tc_checked = false;
     bool tc_ok = false;

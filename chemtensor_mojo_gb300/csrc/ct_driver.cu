@@ -123,6 +123,18 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
     CT_CUDA(h, cudaMalloc((void**)&th.p, (size_t)th_cap * sizeof(double)));
     CT_CUDA(h, cudaMalloc((void**)&th_opt.p, (size_t)th_cap * sizeof(double)));
 
+    // mixed form: rotations of the last split per (bond, direction), FP32, to
+    // warm-start the next sweep's Jacobi at the same bond
+    struct QCache {
+        float* p = nullptr;
+        int64_t cap = 0;     // elements
+        int64_t m = -1, n = -1;
+        ~QCache() {
+            if (p) cudaFree(p);
+        }
+    };
+    std::vector<QCache> qcache((size_t)(2 * N));
+
     EventTimer ev_l, ev_s, ev_e;
     ct_dmrg_stats st{};
     std::vector<double> disc_all;
@@ -189,8 +201,25 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         {
             Arena ar(h);
             // kept bond bound by the capacity of the sites it is written into
+            float* qc = nullptr;
+            int warm = 0;
+            if (prec == CT_PREC_TF32X3 && !ct_svd_is_small(m, n, l2r ? 0 : 1)) {
+                QCache& c = qcache[(size_t)(2 * i + (l2r ? 0 : 1))];
+                const int64_t nv = l2r ? m : n;
+                if (c.cap < nv * nv) {
+                    if (c.p) cudaFree(c.p);
+                    c.p = nullptr;
+                    CT_CUDA(h, cudaMalloc((void**)&c.p, (size_t)(nv * nv) * sizeof(float)));
+                    c.cap = nv * nv;
+                    c.m = c.n = -1;
+                }
+                warm = (c.m == m && c.n == n) ? 1 : 0;
+                qc = c.p;
+                c.m = m;
+                c.n = n;
+            }
             CT_TRY(ct_split_run(h, ar, prec, th_opt.p, m, n, P->chi_max, P->eps_trunc, l2r ? 0 : 1, mps_sites[i],
-                                mps_sites[i + 1], nullptr, h->d_scalars + SC_THETA_NSQ, &so));
+                                mps_sites[i + 1], nullptr, h->d_scalars + SC_THETA_NSQ, &so, qc, warm));
         }
         CT_CUDA(h, cudaEventRecord(ev_s.b, h->stream));
         const int64_t chi = so.chi;

@@ -12,8 +12,11 @@ struct HeffPlan {
     double* W12 = nullptr;
     // mixed-form SVD (ct_svd_mixed.cu); d_total = device |theta|^2
 size_t ct_svd_mixed_ws_bytes(int64_t m, int64_t n, int64_t chi_max, int mode);
+// qcache (nvec x nvec FP32, may be null): rotations of the previous split of the
+// same bond; warm != 0 starts the Jacobi from them and the cache is refreshed.
 int ct_svd_mixed_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t chi_max,
-                     double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out);
+                     double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out,
+                     float* qcache = nullptr, int warm = 0);
 // the FP64 Jacobi runs in one CTA below this many doubles of X and Q
 static inline bool ct_svd_is_small(int64_t m, int64_t n, int mode) {
     const int64_t nvec = mode ? n : m, len = mode ? m : n;
@@ -22,7 +25,8 @@ static inline bool ct_svd_is_small(int64_t m, int64_t n, int mode) {
 // split dispatcher: FP64 Jacobi, or the mixed SVD for large TF32x3 problems
 size_t ct_split_ws_bytes(int prec, int64_t m, int64_t n, int64_t chi_max, int mode);
 int ct_split_run(ct_handle* h, Arena& ar, int prec, const double* M, int64_t m, int64_t n, int64_t chi_max,
-                 double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out);
+                 double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out,
+                 float* qcache = nullptr, int warm = 0);
 
 // mixed form (ct_tc.cu): operand planes of the bond, constructed in place
     void* tc = nullptr;
@@ -70,8 +74,11 @@ int ct_svd_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, i
 
 // mixed-form SVD (ct_svd_mixed.cu); d_total = device |theta|^2
 size_t ct_svd_mixed_ws_bytes(int64_t m, int64_t n, int64_t chi_max, int mode);
+// qcache (nvec x nvec FP32, may be null): rotations of the previous split of the
+// same bond; warm != 0 starts the Jacobi from them and the cache is refreshed.
 int ct_svd_mixed_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t chi_max,
-                     double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out);
+                     double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out,
+                     float* qcache = nullptr, int warm = 0);
 // the FP64 Jacobi runs in one CTA below this many doubles of X and Q
 static inline bool ct_svd_is_small(int64_t m, int64_t n, int mode) {
     const int64_t nvec = mode ? n : m, len = mode ? m : n;
@@ -80,7 +87,8 @@ static inline bool ct_svd_is_small(int64_t m, int64_t n, int mode) {
 // split dispatcher: FP64 Jacobi, or the mixed SVD for large TF32x3 problems
 size_t ct_split_ws_bytes(int prec, int64_t m, int64_t n, int64_t chi_max, int mode);
 int ct_split_run(ct_handle* h, Arena& ar, int prec, const double* M, int64_t m, int64_t n, int64_t chi_max,
-                 double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out);
+                 double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out,
+                 float* qcache = nullptr, int warm = 0);
 
 // mixed form (ct_tc.cu)
 size_t ct_tc_heff_ws_bytes(int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wM, int64_t wR);
@@ -94,3 +102,7 @@ int ct_tc_env_right_run(ct_handle* h, Arena& ar, const double* Rn, const double*
 int ct_tc_gemm(ct_handle* h, Arena& ar, int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha,
                const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc);
 size_t ct_tc_gemm_ws_bytes(int64_t m, int64_t n, int64_t k);
+// same, with C in FP64 (out_fp64=1) or FP32 (beta must be 0 for FP32)
+int ct_tc_gemm_ex(ct_handle* h, Arena& ar, int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha,
+                  const double* A, int64_t lda, const double* B, int64_t ldb, double beta, void* C, int out_fp64,
+                  int64_t ldc);

@@ -14,6 +14,7 @@
 // round trip); large ones run one launch per round-robin round, n/2 pairs in
 // parallel, with a rotation counter read back once per sweep.
 #include "ct_ops.cuh"
+#include "ct_jacobi_coop.cuh"
 
 namespace {
 
@@ -345,30 +346,9 @@ int ct_svd_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, i
                                                                     h->d_status); ct_note_launch();
             CT_LAUNCH_CHECK(h);
         } else {
-            const int P = (int)(nvec + (nvec & 1));
-            int* d_rot = h->d_flags + FL_ROT;
             double* d_frob2 = h->d_scalars + SC_TMP0;
             CT_TRY(ct_reduce_nrm2sq(h, nvec * ldx, X, d_frob2, nullptr));
-            bool converged = false;
-            for (int sweep = 0; sweep < SVD_MAX_SWEEPS; ++sweep) {
-                CT_CUDA(h, cudaMemsetAsync(d_rot, 0, sizeof(int), h->stream));
-                for (int r = 0; r < P - 1; ++r) {
-                    svd_round_kernel<<<P / 2, SVD_NT, 0, h->stream>>>(X, len, ldx, Q, nvec, P, r, tol, d_frob2, d_rot); ct_note_launch();
-                }
-                CT_LAUNCH_CHECK(h);
-                int rot = 0;
-                CT_CUDA(h, cudaMemcpyAsync(&rot, d_rot, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-                CT_CUDA(h, cudaStreamSynchronize(h->stream));
-                if (rot == 0) {
-                    converged = true;
-                    break;
-                }
-            }
-            if (!converged) {
-                ct_seterr(h, "Jacobi SVD did not converge in %d sweeps (%lld x %lld)", SVD_MAX_SWEEPS,
-                          (long long)m, (long long)n);
-                return CT_ERR_NOCONV;
-            }
+            CT_TRY(ct_jacobi::run<double>(h, X, len, Q, nvec, tol, SVD_EPS2, d_frob2, nullptr));
         }
     }
     svd_norms_kernel<<<(unsigned)ct_cdiv(nvec * 32, 256), 256, 0, h->stream>>>(X, len, ldx, nvec, sig); ct_note_launch();

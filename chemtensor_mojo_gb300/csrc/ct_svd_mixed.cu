@@ -19,6 +19,7 @@
 //   4. singular values = FP64 norms of the projected rows/columns, descending;
 //      chi by the reference rule with the total weight |theta|^2 in FP64.
 #include "ct_ops.cuh"
+#include "ct_jacobi_coop.cuh"
 
 namespace {
 
@@ -133,6 +134,11 @@ __global__ void lift_kernel(const float* Q, int64_t nvec, const int* perm, int64
     }
 }
 
+__global__ void f32_to_f64_kernel(const float* a, double* b, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (double)a[i];
+}
+
 __global__ void sub_identity_kernel(double* G, int64_t c) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < c; i += (int64_t)gridDim.x * blockDim.x)
         G[i * c + i] -= 1.0;
@@ -221,16 +227,19 @@ size_t ct_svd_mixed_ws_bytes(int64_t m, int64_t n, int64_t chi_max, int mode) {
     const int64_t c = k < chi_max ? k : chi_max;
     size_t b = ct_bytes(nvec * len, 4) + ct_bytes(nvec * nvec, 4) + ct_bytes(nvec, 8) + ct_bytes(nvec, 4);
     b += ct_bytes(c * nvec, 8) + ct_bytes(c * c, 8) + ct_bytes(c * (m > n ? m : n), 8) + ct_bytes(c, 8) +
-         ct_bytes(c, 4) + 4096;
+         ct_bytes(c, 4) + ct_bytes(nvec * nvec, 8) + 4096;
     // tensor-core operand planes: Newton-Schulz (c x c by c x nvec) and projection
     const size_t ns = ct_tc_gemm_ws_bytes(c, nvec, c);
     const size_t pj = (mode == 0) ? ct_tc_gemm_ws_bytes(c, n, m) : ct_tc_gemm_ws_bytes(m, c, n);
-    return b + (ns > pj ? ns : pj);
+    const size_t wm = (mode == 0) ? ct_tc_gemm_ws_bytes(nvec, n, m) : ct_tc_gemm_ws_bytes(nvec, m, n);
+    size_t mx = ns > pj ? ns : pj;
+    mx = mx > wm ? mx : wm;
+    return b + mx;
 }
 
 int ct_svd_mixed_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t chi_max,
                      double eps_trunc, int mode, double* Aout, double* Bout, double* Sout, const double* d_total,
-                     SvdOut* out) {
+                     SvdOut* out, float* qcache, int warm) {
     const int cols = mode ? 1 : 0;
     const int64_t nvec = cols ? n : m, len = cols ? m : n;
     const int64_t k = m < n ? m : n;
@@ -251,36 +260,31 @@ int ct_svd_mixed_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_
     if (!X || !Q || !sig32 || !perm32 || !Qt || !G || !Pj || !sig || !perm) return CT_ERR_OOM;
     const size_t mark = ar.off;
 
-    to_f32_kernel<<<grid_elems(h, nvec * (len > nvec ? len : nvec)), 256, 0, h->stream>>>(M, m, n, cols, X, Q, nvec); ct_note_launch();
-    CT_LAUNCH_CHECK(h);
+    if (warm && qcache) {
+        // X0 = Qprev . M (rows) or Qprev . M^T (columns); Q0 = Qprev
+        double* Qp64 = ar.take<double>(nvec * nvec);
+        if (!Qp64) return CT_ERR_OOM;
+        const size_t mark2 = ar.off;
+        f32_to_f64_kernel<<<grid_elems(h, nvec * nvec), 256, 0, h->stream>>>(qcache, Qp64, nvec * nvec); ct_note_launch();
+        CT_LAUNCH_CHECK(h);
+        if (!cols) CT_TRY(ct_tc_gemm_ex(h, ar, 0, 0, nvec, n, m, 1.0, Qp64, nvec, M, n, 0.0, X, 0, n));
+        else CT_TRY(ct_tc_gemm_ex(h, ar, 0, 1, nvec, m, n, 1.0, Qp64, nvec, M, n, 0.0, X, 0, m));
+        ar.off = mark2;
+        CT_CUDA(h, cudaMemcpyAsync(Q, qcache, (size_t)(nvec * nvec) * sizeof(float), cudaMemcpyDeviceToDevice,
+                                   h->stream));
+    } else {
+        to_f32_kernel<<<grid_elems(h, nvec * (len > nvec ? len : nvec)), 256, 0, h->stream>>>(M, m, n, cols, X, Q, nvec); ct_note_launch();
+        CT_LAUNCH_CHECK(h);
+    }
     // 1. FP32 one-sided Jacobi
     if (nvec >= 2) {
-        const int P = (int)(nvec + (nvec & 1));
-        int* d_rot = h->d_flags + FL_ROT;
         double* d_f2 = h->d_scalars + SC_MISC + 200;
         CT_TRY(ct_reduce_nrm2sq(h, m * n, M, d_f2, nullptr));
-        const double tol = 1e-6;
-        bool converged = false;
-        for (int sweep = 0; sweep < MAX_SWEEPS32; ++sweep) {
-            CT_CUDA(h, cudaMemsetAsync(d_rot, 0, sizeof(int), h->stream));
-            for (int r = 0; r < P - 1; ++r) {
-                round32_kernel<<<P / 2, NT, 0, h->stream>>>(X, len, Q, nvec, P, r, tol, d_f2, d_rot); ct_note_launch();
-            }
-            CT_LAUNCH_CHECK(h);
-            int rot = 0;
-            CT_CUDA(h, cudaMemcpyAsync(&rot, d_rot, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-            CT_CUDA(h, cudaStreamSynchronize(h->stream));
-            if (rot == 0) {
-                converged = true;
-                break;
-            }
-        }
-        if (!converged) {
-            ct_seterr(h, "FP32 Jacobi SVD did not converge in %d sweeps (%lld x %lld)", MAX_SWEEPS32, (long long)m,
-                      (long long)n);
-            return CT_ERR_NOCONV;
-        }
+        CT_TRY(ct_jacobi::run<float>(h, X, len, Q, nvec, 1e-6, 1.4210854715202004e-14, d_f2, nullptr));
     }
+    if (qcache)
+        CT_CUDA(h, cudaMemcpyAsync(qcache, Q, (size_t)(nvec * nvec) * sizeof(float), cudaMemcpyDeviceToDevice,
+                                   h->stream));
     norms32_kernel<<<(unsigned)ct_cdiv(nvec * 32, 256), 256, 0, h->stream>>>(X, len, nvec, sig32); ct_note_launch();
     rank_desc_kernel<<<(unsigned)ct_cdiv(nvec, 256), 256, 0, h->stream>>>(sig32, nvec, perm32); ct_note_launch();
     lift_kernel<<<grid_elems(h, c * nvec), 256, 0, h->stream>>>(Q, nvec, perm32, c, Qt); ct_note_launch();
@@ -335,8 +339,9 @@ size_t ct_split_ws_bytes(int prec, int64_t m, int64_t n, int64_t chi_max, int mo
 }
 
 int ct_split_run(ct_handle* h, Arena& ar, int prec, const double* M, int64_t m, int64_t n, int64_t chi_max,
-                 double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out) {
+                 double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out,
+                 float* qcache, int warm) {
     if (prec == CT_PREC_TF32X3 && !ct_svd_is_small(m, n, mode))
-        return ct_svd_mixed_run(h, ar, M, m, n, chi_max, eps_trunc, mode, A, B, S, d_total, out);
+        return ct_svd_mixed_run(h, ar, M, m, n, chi_max, eps_trunc, mode, A, B, S, d_total, out, qcache, warm);
     return ct_svd_run(h, ar, M, m, n, chi_max, eps_trunc, mode, A, B, S, out);
 }

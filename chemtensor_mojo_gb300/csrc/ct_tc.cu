@@ -706,6 +706,12 @@ size_t ct_tc_gemm_ws_bytes(int64_t m, int64_t n, int64_t k) {
 
 int ct_tc_gemm(ct_handle* h, Arena& ar, int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha,
                const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc) {
+    return ct_tc_gemm_ex(h, ar, trans_a, trans_b, m, n, k, alpha, A, lda, B, ldb, beta, C, 1, ldc);
+}
+
+int ct_tc_gemm_ex(ct_handle* h, Arena& ar, int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha,
+                  const double* A, int64_t lda, const double* B, int64_t ldb, double beta, void* C, int out_fp64,
+                  int64_t ldc) {
     const int64_t kp = ct_round_up(k, TC_BK);
     SplitOperand a = take_split(ar, m, kp);
     SplitOperand b = take_split(ar, n, kp);
@@ -717,7 +723,7 @@ int ct_tc_gemm(ct_handle* h, Arena& ar, int trans_a, int trans_b, int64_t m, int
     CT_TRY(pack_launch(h, trans_b ? pack_desc(B, n, n, 0, ldb, k, 1, b) : pack_desc(B, n, n, 0, 1, k, ldb, b),
                        trans_b != 0, nullptr));
     TcEpi e{};
-    e.C = C; e.out_fp64 = 1; e.M0 = m; e.sCm1 = 0; e.sCm0 = ldc; e.alpha = alpha; e.beta = beta;
+    e.C = C; e.out_fp64 = out_fp64; e.M0 = m; e.sCm1 = 0; e.sCm0 = ldc; e.alpha = alpha; e.beta = beta;
     return tc_gemm_launch(h, a, b, m, n, e, nullptr);
 }
 

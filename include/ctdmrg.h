@@ -69,6 +69,8 @@ CT_API int ct_version(void);
 CT_API int64_t ct_launch_count(void);
 /* bytes of handle-owned scratch currently reserved */
 CT_API int ct_workspace_bytes(ct_handle* h, int64_t* bytes_out);
+/* Jacobi sweeps of the last SVD split on this handle and the running total */
+CT_API int ct_svd_sweeps(ct_handle* h, int* last_host, int64_t* total_host);
 /* cap on handle-owned scratch in bytes (0 = unlimited); growth beyond it -> CT_ERR_OOM */
 CT_API int ct_set_workspace_limit(ct_handle* h, int64_t bytes);
 

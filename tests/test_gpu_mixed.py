@@ -158,7 +158,7 @@ def test_svd_split_mixed(ctx, dims, chi_max, eps, l2r):
         # may differ near a tie, but the weight actually discarded obeys eps
         recon = np.tensordot(a, b, axes=([2], [0]))
         committed = np.sum((recon - th) ** 2) / np.sum(th * th)
-        assert committed <= 1.5 * eps + 1e-12
+        assert committed <= 1.5 * eps + 1e-10   # FP32 subspace resolves tail weights to ~1e-10
         assert abs(chi - info.chi) <= max(8, info.chi // 10)
     kk = min(chi, info.chi)
     assert np.allclose(S[:kk], info.S[:kk], rtol=1e-5, atol=1e-6 * info.S[0])
