@@ -47,7 +47,7 @@ class ct_dmrg_stats(C.Structure):
     _fields_ = [("seconds_total", C.c_double), ("seconds_lanczos", C.c_double), ("seconds_svd", C.c_double),
                 ("seconds_env", C.c_double), ("heff_flops", C.c_double), ("env_flops", C.c_double),
                 ("heff_applies", C.c_int64), ("local_updates", C.c_int64), ("max_discarded", C.c_double),
-                ("energy_rayleigh", C.c_double)]
+                ("energy_rayleigh", C.c_double), ("subspace_splits", C.c_int64), ("exact_splits", C.c_int64)]
 
 
 P = C.c_void_p

@@ -157,6 +157,7 @@ int ct_destroy(ct_handle* h) {
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     cudaFree(h->ws);
+    for (auto& b : h->basis_cache) cudaFree(b.p);
     cudaFree(h->d_status);
     cudaFree(h->d_scalars);
     cudaFree(h->d_partials);

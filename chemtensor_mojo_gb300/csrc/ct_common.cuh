@@ -29,6 +29,13 @@ struct ct_handle {
     size_t ws_cap = 0;
     size_t ws_limit = 0;            // 0 = unlimited
     std::string err;
+    // kept bases of the last mixed-form split per (bond, direction), to warm-start
+    // the next sweep's subspace split; FP64 rows, freed by ct_destroy
+    struct BasisCache {
+        double* p = nullptr;
+        int64_t cap = 0, m = -1, n = -1, c = -1;
+    };
+    std::vector<BasisCache> basis_cache;
     // diagnostics: Jacobi sweeps of the last SVD split, and the running total
     int last_svd_sweeps = 0;
     int64_t total_svd_sweeps = 0;

@@ -164,6 +164,9 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         const int64_t m = Dl * d, n = d * Dr;
         size_t need = ct_lanczos_ws_bytes(prec, Dl, d, Dr, wL, wM, wR, P->max_krylov_iter);
         need = std::max(need, ct_split_ws_bytes(prec, m, n, P->chi_max, l2r ? 0 : 1));
+        const bool use_subspace = (prec == CT_PREC_TF32X3) && !ct_svd_is_small(m, n, l2r ? 0 : 1) &&
+                                  (int64_t)P->chi_max < std::min(m, n);
+        if (use_subspace) need = std::max(need, ct_split_subspace_ws_bytes(m, n, P->chi_max));
         const int64_t chi_ub = std::min<int64_t>(std::min(m, n), P->chi_max);
         need = std::max(need, l2r ? ct_env_ws_bytes(prec, Dl, d, chi_ub, wL, wM)
                                   : ct_env_ws_bytes(prec, chi_ub, d, Dr, wM, wR));
@@ -201,9 +204,33 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         {
             Arena ar(h);
             // kept bond bound by the capacity of the sites it is written into
+            bool done_split = false;
+            ct_handle::BasisCache* bc = nullptr;
+            if (use_subspace) {
+                const size_t key = (size_t)(2 * i + (l2r ? 0 : 1));
+                if (h->basis_cache.size() < (size_t)(2 * N)) h->basis_cache.resize((size_t)(2 * N));
+                bc = &h->basis_cache[key];
+                const int64_t c = P->chi_max, nv = l2r ? m : n;
+                if (bc->cap < c * nv) {
+                    if (bc->p) cudaFree(bc->p);
+                    bc->p = nullptr;
+                    CT_CUDA(h, cudaMalloc((void**)&bc->p, (size_t)(c * nv) * sizeof(double)));
+                    bc->cap = c * nv;
+                    bc->m = bc->n = bc->c = -1;
+                }
+                if (bc->m == m && bc->n == n && bc->c == c) {
+                    bool ok = false;
+                    CT_TRY(ct_split_subspace(h, ar, th_opt.p, m, n, c, l2r ? 0 : 1, bc->p, mps_sites[i],
+                                             mps_sites[i + 1], h->d_scalars + SC_THETA_NSQ, P->eps_trunc, 2, &so,
+                                             &ok));
+                    done_split = ok;
+                    if (ok) st.subspace_splits++;
+                }
+                if (!done_split) bc->m = bc->n = bc->c = -1;
+            }
             float* qc = nullptr;
             int warm = 0;
-            if (prec == CT_PREC_TF32X3 && !ct_svd_is_small(m, n, l2r ? 0 : 1)) {
+            if (!done_split && prec == CT_PREC_TF32X3 && !ct_svd_is_small(m, n, l2r ? 0 : 1)) {
                 QCache& c = qcache[(size_t)(2 * i + (l2r ? 0 : 1))];
                 const int64_t nv = l2r ? m : n;
                 if (c.cap < nv * nv) {
@@ -218,8 +245,19 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
                 c.m = m;
                 c.n = n;
             }
-            CT_TRY(ct_split_run(h, ar, prec, th_opt.p, m, n, P->chi_max, P->eps_trunc, l2r ? 0 : 1, mps_sites[i],
-                                mps_sites[i + 1], nullptr, h->d_scalars + SC_THETA_NSQ, &so, qc, warm));
+            if (!done_split) {
+                Arena ar2(h);
+                CT_TRY(ct_split_run(h, ar2, prec, th_opt.p, m, n, P->chi_max, P->eps_trunc, l2r ? 0 : 1,
+                                    mps_sites[i], mps_sites[i + 1], nullptr, h->d_scalars + SC_THETA_NSQ, &so, qc,
+                                    warm));
+                st.exact_splits++;
+                if (bc && so.chi == P->chi_max) {
+                    CT_TRY(ct_basis_from_split(h, l2r ? 0 : 1, mps_sites[i], mps_sites[i + 1], m, n, so.chi, bc->p));
+                    bc->m = m;
+                    bc->n = n;
+                    bc->c = so.chi;
+                }
+            }
         }
         CT_CUDA(h, cudaEventRecord(ev_s.b, h->stream));
         const int64_t chi = so.chi;

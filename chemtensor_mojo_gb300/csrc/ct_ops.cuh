@@ -10,25 +10,7 @@ struct HeffPlan {
     double* T1 = nullptr;
     double* T3 = nullptr;
     double* W12 = nullptr;
-    // mixed-form SVD (ct_svd_mixed.cu); d_total = device |theta|^2
-size_t ct_svd_mixed_ws_bytes(int64_t m, int64_t n, int64_t chi_max, int mode);
-// qcache (nvec x nvec FP32, may be null): rotations of the previous split of the
-// same bond; warm != 0 starts the Jacobi from them and the cache is refreshed.
-int ct_svd_mixed_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t chi_max,
-                     double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out,
-                     float* qcache = nullptr, int warm = 0);
-// the FP64 Jacobi runs in one CTA below this many doubles of X and Q
-static inline bool ct_svd_is_small(int64_t m, int64_t n, int mode) {
-    const int64_t nvec = mode ? n : m, len = mode ? m : n;
-    return (nvec * len + nvec * nvec) * 8 <= 200 * 1024;
-}
-// split dispatcher: FP64 Jacobi, or the mixed SVD for large TF32x3 problems
-size_t ct_split_ws_bytes(int prec, int64_t m, int64_t n, int64_t chi_max, int mode);
-int ct_split_run(ct_handle* h, Arena& ar, int prec, const double* M, int64_t m, int64_t n, int64_t chi_max,
-                 double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out,
-                 float* qcache = nullptr, int warm = 0);
-
-// mixed form (ct_tc.cu): operand planes of the bond, constructed in place
+    // mixed form (ct_tc.cu): operand planes of the bond, constructed in place
     void* tc = nullptr;
     alignas(16) unsigned char tc_store[512];
 };
@@ -89,6 +71,14 @@ size_t ct_split_ws_bytes(int prec, int64_t m, int64_t n, int64_t chi_max, int mo
 int ct_split_run(ct_handle* h, Arena& ar, int prec, const double* M, int64_t m, int64_t n, int64_t chi_max,
                  double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out,
                  float* qcache = nullptr, int warm = 0);
+
+// warm-started subspace split (ct_svd_subspace.cu)
+size_t ct_split_subspace_ws_bytes(int64_t m, int64_t n, int64_t c);
+int ct_split_subspace(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t c, int mode,
+                      double* basis, double* Aout, double* Bout, const double* d_total, double eps_trunc,
+                      int power_steps, SvdOut* out, bool* accepted);
+int ct_basis_from_split(ct_handle* h, int mode, const double* Aout, const double* Bout, int64_t m, int64_t n,
+                        int64_t c, double* basis);
 
 // mixed form (ct_tc.cu)
 size_t ct_tc_heff_ws_bytes(int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wM, int64_t wR);

@@ -165,6 +165,8 @@ typedef struct ct_dmrg_stats {
     int64_t local_updates;
     double max_discarded;      /* largest discarded weight over the run         */
     double energy_rayleigh;    /* FP64 Rayleigh quotient (NaN unless requested)  */
+    int64_t subspace_splits;   /* mixed form: warm-started subspace splits      */
+    int64_t exact_splits;      /* Jacobi-SVD splits                              */
 } ct_dmrg_stats;
 
 /* Runs the sweeps in place.  mps_sites[i] are caller-owned device buffers of

@@ -171,3 +171,29 @@ def test_svd_split_mixed(ctx, dims, chi_max, eps, l2r):
         prod = np.tensordot(a, b, axes=([2], [0]))
         prod_ref = np.tensordot(A_ref, B_ref, axes=([2], [0]))
         assert rel(prod, prod_ref) < 1e-5
+
+
+def test_dmrg_warm_subspace_split(ctx):
+    """Heisenberg L=16, chi_max=64 (bonds of 128 x 128, chi_max binding), 4 sweeps in one call:
+    after the first sweep the mixed form splits large bonds by the warm-started subspace
+    iteration; its FP64 Rayleigh energy matches the FP64 form (exact Jacobi splits) to 1e-9."""
+    ct = ct_mod()
+    L = 16
+    mpo_a = oh.spin_half_xxz(L, 1.0)
+    sites, _ = orng.create_random_mps_c_compatible(L, 2, 64, 2)
+    mps_a = od.right_normalize(sites)
+    out = {}
+    for prec in ("fp64", "tf32x3"):
+        st = ct.DMRGStats()
+        p = ct.DMRGParams(num_sweeps=4, chi_max=64, eps_trunc=0.0, max_krylov_iter=20, krylov_tol=1e-10,
+                          energy_tol=0.0, max_rotations=0, prec=prec, final_rayleigh=True)
+        E, mps = ct.dmrg_two_site(ctx, ct.mpo_from_arrays(ctx, mpo_a), ct.mps_from_arrays(ctx, mps_a), p, st)
+        out[prec] = st
+        if prec == "tf32x3":
+            # the run ends right-to-left: sites 1.. are right-canonical to FP64 accuracy
+            for a in mps.to_numpy()[1:]:
+                mat = a.reshape(a.shape[0], -1)
+                assert np.abs(mat @ mat.T - np.eye(a.shape[0])).max() < 1e-12
+    assert out["tf32x3"].subspace_splits > 0
+    e64 = out["fp64"].energy_rayleigh
+    assert abs(out["tf32x3"].energy_rayleigh - e64) <= 1e-9 * abs(e64)
