@@ -24,6 +24,8 @@ CT_ERR_SHAPE = -6
 CT_ERR_UNSUPPORTED = -7
 CT_ERR_NONFINITE = -8
 CT_ERR_EMPTY = -9
+CT_ERR_TOO_LARGE = -10
+NOALLOC_SCRATCH_DOUBLES = 1 << 21
 
 CT_PREC_FP64 = 0
 CT_PREC_TF32X3 = 1
@@ -90,6 +92,7 @@ SIGNATURES = {
     "ct_random_mps_host": [I32, I32, I32, C.c_uint64, C.POINTER(I64), PP],
     "ct_rng_randnf_host": [C.c_uint64, I64, C.POINTER(C.c_float)],
     "ct_tc_gemm_time": [P, I64, I64, I64, I32, C.POINTER(D)],
+    "ct_heff2_apply_noalloc": [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, I64],
     "ct_energy_grad": [P, I32, I32, I32, C.POINTER(I64), PP, C.POINTER(I64), PP, PP, I32, C.POINTER(D)],
 }
 STRING_FUNCS = {"ct_error_string": [I32], "ct_last_error": [P]}

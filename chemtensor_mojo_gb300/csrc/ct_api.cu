@@ -105,6 +105,7 @@ const char* ct_error_string(int s) {
         case CT_ERR_UNSUPPORTED: return "unsupported";
         case CT_ERR_NONFINITE: return "non-finite value";
         case CT_ERR_EMPTY: return "truncation kept no singular values";
+        case CT_ERR_TOO_LARGE: return "problem exceeds the static scratch of the no-alloc entry point";
         default: return "unknown status";
     }
 }

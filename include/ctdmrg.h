@@ -48,7 +48,8 @@ enum ct_status {
     CT_ERR_SHAPE = -6,       /* inconsistent shapes                              */
     CT_ERR_UNSUPPORTED = -7, /* shape/precision not supported by this build      */
     CT_ERR_NONFINITE = -8,   /* NaN/Inf met in a reduction                       */
-    CT_ERR_EMPTY = -9        /* truncation kept zero singular values             */
+    CT_ERR_EMPTY = -9,       /* truncation kept zero singular values             */
+    CT_ERR_TOO_LARGE = -10   /* problem exceeds the static scratch of a no-alloc entry */
 };
 
 enum ct_prec { CT_PREC_FP64 = 0, CT_PREC_TF32X3 = 1 };
@@ -214,6 +215,23 @@ CT_API int ct_energy_grad(ct_handle* h, int prec, int nsites, int d, const int64
                    const double* const* mpo_sites, const int64_t* bond_dims,
                    const double* const* mps_sites, double* const* grad_sites,
                    int checkpoint_every, double* energy_host);
+
+/* ---- allocation-free H_eff apply (no counterpart in the reference) --------
+ * For callers that cannot let a library allocate device memory, e.g. a Mojo/MAX
+ * host whose DeviceContext allocator owns every buffer, or a caller under a
+ * fixed device-memory budget.  Same FP64 result as ct_heff2_apply (same
+ * kernels), enqueued on `stream`; takes no handle and calls no cudaMalloc.
+ * Its intermediates live in one static device array of
+ * CT_NOALLOC_SCRATCH_DOUBLES doubles (16 MiB) held by every GPU that loads the
+ * library until exit; sizes that need more than that
+ * (T1 + T3 = 2 * Dl*d*d*Dr*max(wL,wR) doubles, plus the fused MPO matrix)
+ * return CT_ERR_TOO_LARGE.  The first call on a device looks up the array's
+ * address (make it before any stream capture).  All calls share the array:
+ * calls that overlap on the GPU race.                                       */
+#define CT_NOALLOC_SCRATCH_DOUBLES (1u << 21)
+CT_API int ct_heff2_apply_noalloc(void* stream, const double* theta, const double* L, const double* R,
+                                  const double* W1, const double* W2, double* out, int64_t Dl, int64_t d,
+                                  int64_t Dr, int64_t wL, int64_t wM, int64_t wR);
 
 /* ---- measurement hook (no reference counterpart) --------------------------
  * Average device time of one launch of the TF32x3 tcgen05 GEMM kernel on an
