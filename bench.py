@@ -52,6 +52,9 @@ MPO_D = 5
 LANCZOS = 24
 EPS = 0.0
 RAMP = [64, 256, 1024]
+# dram__bytes_read.sum + dram__bytes_write.sum of one centre-bond H_eff GEMM launch
+# (5120 x 4096 x 1024, chi=1024) from ncu; profiles/tc_gemm_kernel_heff_chi1024.md
+TC_GEMM_TRAFFIC_BYTES = (78.5 + 55.7) * 1e6
 METRIC = "DMRG sweep s & H_eff TFLOP/s, mixed-prec vs FP64 on GPU at |dE/E|<=1e-9"
 
 
@@ -65,7 +68,7 @@ def parse():
     ap.add_argument("--chi", type=int, default=1024)
     ap.add_argument("--L", type=int, default=L_SITES)
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64/roofline/CPU side measurements")
-    ap.add_argument("--mode", default="sweep", choices=["sweep", "heff"],
+    ap.add_argument("--mode", default="sweep", choices=["sweep", "heff", "heff-grid"],
                     help="heff: only centre-bond H_eff applies (a small, fixed workload for profilers)")
     return ap.parse_args()
 
@@ -100,6 +103,55 @@ def heff_mode(args):
                       "dtype": args.prec, "config": {"workload": f"centre-bond H_eff chi={chi} D=5 d=2"},
                       "steps": args.steps, "warmup": args.warmup,
                       "gpu_launches": _lib.launch_count() - n0}), flush=True)
+
+
+def heff_grid_mode(args):
+    """H_eff kernel grid: chi in {256, 512, 1024, 2048} x D in {5, 16, 32} x d in {2, 4}.
+
+    Random L, R [D, chi, chi], W [D, d, d, D] symmetrised in (s, t), theta
+    [chi, d, d, chi], all N(0, 1) from a fixed seed.  Each point: one warm-up
+    and ``--steps`` timed applies (CUDA events).  The FP64 form runs where one
+    apply stays under ~2 s (algorithmic FLOPs <= 2.5 TFLOP).  One JSON line.
+    """
+    import torch
+    import chemtensor_mojo_gb300 as ct
+    ctx = ct.get_context(0)
+    dev = ctx.torch_device
+    g = torch.Generator(device="cpu").manual_seed(11)
+    rows = []
+    for chi in (256, 512, 1024, 2048):
+        for D in (5, 16, 32):
+            for d in (2, 4):
+                F = heff_flops(chi, chi, D, d)
+                w = torch.randn(D, d, d, D, generator=g, dtype=torch.float64)
+                w = 0.5 * (w + w.transpose(1, 2))
+                mpo = ct.mpo_from_arrays(ctx, [w.numpy(), w.numpy()])
+                th = ct.DenseTensor(torch.randn(chi * d * d * chi, generator=g, dtype=torch.float64).to(dev),
+                                    [chi, d, d, chi])
+                Le = ct.DenseTensor(torch.randn(D * chi * chi, generator=g, dtype=torch.float64).to(dev),
+                                    [D, chi, chi])
+                Re = ct.DenseTensor(torch.randn(D * chi * chi, generator=g, dtype=torch.float64).to(dev),
+                                    [D, chi, chi])
+                row = {"chi": chi, "D": D, "d": d, "gflop": F / 1e9}
+                for prec in ("tf32x3", "fp64"):
+                    if prec == "fp64" and F > 2.5e12:
+                        continue
+                    ct.apply_two_site_heff(th, Le, Re, mpo.sites[0], mpo.sites[1], ctx, prec=prec)
+                    torch.cuda.synchronize()
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    for _ in range(max(args.steps, 1)):
+                        ct.apply_two_site_heff(th, Le, Re, mpo.sites[0], mpo.sites[1], ctx, prec=prec)
+                    e1.record()
+                    torch.cuda.synchronize()
+                    sec = e0.elapsed_time(e1) * 1e-3 / max(args.steps, 1)
+                    row[prec] = {"s": sec, "tflops": F / sec / 1e12}
+                rows.append(row)
+                del th, Le, Re, mpo
+                torch.cuda.empty_cache()
+    print(json.dumps({"metric": "H_eff apply TFLOP/s (kernel grid)", "unit": "TFLOP/s", "data": "synthetic",
+                      "config": {"workload": "H_eff grid chi x D x d, random L/R/W/theta"}, "grid": rows}),
+          flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -233,6 +285,9 @@ def main():
     if args.impl == "reference":
         reference_arm(args, rank)
         return
+    if args.mode == "heff-grid":
+        heff_grid_mode(args)
+        return
     if args.mode == "heff":
         heff_mode(args)
         return
@@ -288,13 +343,21 @@ def main():
     sweeps_e = (C.c_double * max(args.steps, 1))()
     done = C.c_int()
     stats = _lib.ct_dmrg_stats()
-    cp = params(chi, args.steps).to_c()
+    # the timed sweeps continue the warm-up's MPS on the same handle, so the
+    # large splits of the first half-sweep start from the kept bond bases
+    tp = params(chi, args.steps)
+    tp.keep_bases = True
+    cp = tp.to_c()
     h2d = sum(h.numel() * 8 for h in host_sites) + sum(h.numel() * 8 for h in host_mpo)
     d2h = sum(h.numel() * 8 for h in host_sites) + 8
 
     stream = torch.cuda.current_stream()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     clocks = ClockSampler(local_rank)
+    # event pair around every tensor-core GEMM launch of the timed sweeps
+    kt_on = prec == "tf32x3"
+    if kt_on:
+        ctx.call("ct_kernel_timing", 1)
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
@@ -317,6 +380,12 @@ def main():
     t_wall = time.perf_counter() - t_wall0
     launches = _lib.launch_count() - launches0
     clocks.stop()
+    kt = None
+    if kt_on:
+        n_kt, ms_kt, fl_kt = C.c_int64(), C.c_double(), C.c_double()
+        ctx.call("ct_kernel_timing_read", C.byref(n_kt), C.byref(ms_kt), C.byref(fl_kt))
+        ctx.call("ct_kernel_timing", 0)
+        kt = {"launches": n_kt.value, "ms": ms_kt.value, "flops": fl_kt.value}
     if dist is not None:
         dist.barrier()
     K = max(args.steps, 1)
@@ -365,20 +434,26 @@ def main():
         "phase_seconds": {"lanczos": stats.seconds_lanczos, "svd": stats.seconds_svd, "env": stats.seconds_env,
                           "total_wall": stats.seconds_total},
         "max_discarded": stats.max_discarded, "warmup_log": warm_log,
+        "splits": {"subspace": stats.subspace_splits, "exact": stats.exact_splits},
         "e2e": {"value": e2e_s / K, "unit": "s/sweep", "h2d_bytes_per_step": h2d // K, "d2h_bytes_per_step": d2h // K,
                 "wall_s": t_wall},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
     line.update(extras)
-    if "tc_gemm_ms" in extras:
-        m, n, k = extras["tc_gemm_shape"]
-        ach = 2.0 * m * n * k / (extras["tc_gemm_ms"] * 1e-3) / 1e12
+    if kt and kt["launches"] > 0 and kt["ms"] > 0:
+        # live: every TF32x3 GEMM launch of the timed sweeps, CUDA events on the launching stream
+        ach = kt["flops"] / (kt["ms"] * 1e-3) / 1e12
         peak = bf16 / 6.0
         line["roofline"] = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                            "traffic": extras.get("tc_gemm_traffic"),
-                            "kernel": "tc_gemm_kernel<128,3> (TF32x3, tcgen05)",
-                            "peak_note": f"{peak_src} bf16 {bf16} TFLOP/s / 2 (TF32 rate) / 3 (3 MMAs per product)"}
+                            "traffic": TC_GEMM_TRAFFIC_BYTES,
+                            "kernel": "tc_gemm_persist_kernel<128,3> (TF32x3, tcgen05)",
+                            "launches": kt["launches"], "avg_launch_ms": kt["ms"] / kt["launches"],
+                            "flops_per_launch": kt["flops"] / kt["launches"],
+                            "share_of_timed_region": kt["ms"] * 1e-3 / max(dev_s, 1e-12),
+                            "peak_note": f"{peak_src} bf16 {bf16} TFLOP/s / 2 (TF32 rate) / 3 (3 MMAs per product)",
+                            "traffic_note": "DRAM read+write bytes of one centre-bond H_eff GEMM "
+                                            "(5120x4096x1024) from an ncu capture, per launch"}
     if "cpu_sweep_s" in extras:
         line["cpu_baseline"] = {"value": extras["cpu_sweep_s"], "unit": "s/sweep", "cores": os.cpu_count(),
                                 "kind": "port", "sample": extras["cpu_sample"]}

@@ -159,6 +159,7 @@ int ct_destroy(ct_handle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     cudaFree(h->ws);
     for (auto& b : h->basis_cache) cudaFree(b.p);
+    for (auto e : h->ktime_ev) cudaEventDestroy(e);
     cudaFree(h->d_status);
     cudaFree(h->d_scalars);
     cudaFree(h->d_partials);

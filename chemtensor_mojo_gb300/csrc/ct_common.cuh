@@ -29,11 +29,13 @@ struct ct_handle {
     size_t ws_cap = 0;
     size_t ws_limit = 0;            // 0 = unlimited
     std::string err;
-    // kept bases of the last mixed-form split per (bond, direction), to warm-start
-    // the next sweep's subspace split; FP64 rows, freed by ct_destroy
+    // bond bases kept by the mixed-form splits, to warm-start the subspace split
+    // of the next visit of the bond: entry 2i holds the c rows over (a_{i-1}, s_i)
+    // of the last left-to-right split of bond i, entry 2i+1 the c rows over
+    // (s_{i+1}, a_{i+1}) of the last right-to-left one.  FP64, freed by ct_destroy.
     struct BasisCache {
         double* p = nullptr;
-        int64_t cap = 0, m = -1, n = -1, c = -1;
+        int64_t cap = 0, len = -1, c = -1;
     };
     std::vector<BasisCache> basis_cache;
     // diagnostics: Jacobi sweeps of the last SVD split, and the running total
@@ -42,9 +44,17 @@ struct ct_handle {
     // tensor-core path state
     bool tc_checked = false;
     bool tc_ok = false;
+    // optional live timing of every tensor-core GEMM launch: an event pair per
+    // launch on the handle's stream, read back when the pool fills or on request
+    bool ktime_on = false;
+    std::vector<cudaEvent_t> ktime_ev;   // 2 per slot
+    std::vector<double> ktime_slot_flops;
+    int ktime_pending = 0;
+    int64_t ktime_launches = 0;
+    double ktime_ms = 0.0, ktime_flops = 0.0;
 };
 
-enum { CT_NSCALARS = 1024, CT_NPARTIALS = 8192, CT_NFLAGS = 256 };
+enum { CT_NSCALARS = 1024, CT_NPARTIALS = 8192, CT_NFLAGS = 256, CT_MAX_KRYLOV_SLOTS = 128 };
 
 // scalar slots inside d_scalars
 enum {
@@ -58,8 +68,12 @@ enum {
     SC_RITZ = 64,          // Ritz coefficients (<= 128)
     SC_ALPHA = 256,        // Lanczos alpha (<= 128)
     SC_BETA = 512,         // Lanczos beta (<= 128)
-    SC_MISC = 768
+    SC_MISC = 768,         // scratch (<= 128): Thomas coefficients, reorthogonalisation
+    SC_SVD_FROB2 = 968,    // mixed SVD: |M|_F^2
+    SC_SPLIT_PIV = 970     // subspace split: smallest Cholesky pivot of each pass (2)
 };
+static_assert(SC_MISC + CT_MAX_KRYLOV_SLOTS <= SC_SVD_FROB2 && SC_SPLIT_PIV + 2 <= CT_NSCALARS,
+              "scalar slots overlap or overflow d_scalars");
 // int slots inside d_flags
 enum { FL_STOP = 0, FL_NUMITER = 1, FL_ROT = 2, FL_CHI = 3, FL_TMP = 4, FL_CNT = 8 };
 
@@ -162,6 +176,8 @@ struct GemmDesc {
     int64_t nb1, nb0;                      // batch = nb1 x nb0
     int64_t sA1, sA0, sB1, sB0, sC1, sC0;  // batch strides
     const int* skip;
+    int tri;   // 0: full; 1: write only C tiles on or below the diagonal (symmetric C);
+               // 2: A is lower triangular (A(m, k) = 0 for k > m), skip those k
 };
 int ct_gemm_f64_launch(ct_handle* h, const GemmDesc& g);
 
@@ -209,6 +225,9 @@ struct SvdOut {
     int64_t chi = 0;
     double sum_s2_all = 0.0;  // sum of all min(m,n) s^2 (sorted order)
     double sum_s2_kept = 0.0;
+    double min_pivot = 0.0;   // subspace split: smallest Cholesky pivot of the first pass,
+    double min_pivot2 = 0.0;  // of the second pass,
+    int chol_fail = 0;        // and whether a pivot was not positive
 };
 // tensor-core path (ct_tc.cu)
 struct TcGemm;

@@ -134,6 +134,9 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         }
     };
     std::vector<QCache> qcache((size_t)(2 * N));
+    if (h->basis_cache.size() < (size_t)(2 * N)) h->basis_cache.resize((size_t)(2 * N));
+    if (!P->keep_bases)
+        for (auto& b : h->basis_cache) b.len = b.c = -1;
 
     EventTimer ev_l, ev_s, ev_e;
     ct_dmrg_stats st{};
@@ -207,26 +210,37 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
             bool done_split = false;
             ct_handle::BasisCache* bc = nullptr;
             if (use_subspace) {
-                const size_t key = (size_t)(2 * i + (l2r ? 0 : 1));
-                if (h->basis_cache.size() < (size_t)(2 * N)) h->basis_cache.resize((size_t)(2 * N));
-                bc = &h->basis_cache[key];
-                const int64_t c = P->chi_max, nv = l2r ? m : n;
-                if (bc->cap < c * nv) {
-                    if (bc->p) cudaFree(bc->p);
-                    bc->p = nullptr;
-                    CT_CUDA(h, cudaMalloc((void**)&bc->p, (size_t)(c * nv) * sizeof(double)));
-                    bc->cap = c * nv;
-                    bc->m = bc->n = bc->c = -1;
+                // this split keeps its far-side basis in `own`; it starts from the
+                // basis the last split of the bond in the other direction kept
+                const int64_t c = P->chi_max, own_len = l2r ? m : n, src_len = l2r ? n : m;
+                ct_handle::BasisCache& own = h->basis_cache[(size_t)(2 * i + (l2r ? 0 : 1))];
+                const ct_handle::BasisCache& src = h->basis_cache[(size_t)(2 * i + (l2r ? 1 : 0))];
+                bc = &own;
+                if (own.cap < c * own_len) {
+                    if (own.p) cudaFree(own.p);
+                    own.p = nullptr;
+                    own.cap = 0;
+                    CT_CUDA(h, cudaMalloc((void**)&own.p, (size_t)(c * own_len) * sizeof(double)));
+                    own.cap = c * own_len;
                 }
-                if (bc->m == m && bc->n == n && bc->c == c) {
+                own.len = own.c = -1;
+                if (src.p && src.len == src_len && src.c == c) {
                     bool ok = false;
-                    CT_TRY(ct_split_subspace(h, ar, th_opt.p, m, n, c, l2r ? 0 : 1, bc->p, mps_sites[i],
-                                             mps_sites[i + 1], h->d_scalars + SC_THETA_NSQ, P->eps_trunc, 2, &so,
+                    CT_TRY(ct_split_subspace(h, ar, th_opt.p, m, n, c, l2r ? 0 : 1, src.p, own.p, mps_sites[i],
+                                             mps_sites[i + 1], h->d_scalars + SC_THETA_NSQ, P->eps_trunc, 0, &so,
                                              &ok));
                     done_split = ok;
-                    if (ok) st.subspace_splits++;
+                    if (P->verbose >= 2)
+                        fprintf(stderr,
+                                "bond %d %s: subspace split %s (pivots %.3g %.3g%s, kept %.12g of %.12g)\n", i,
+                                l2r ? "L->R" : "R->L", ok ? "accepted" : "refused", so.min_pivot, so.min_pivot2,
+                                so.chol_fail ? ", Cholesky failed" : "", so.sum_s2_kept, so.sum_s2_all);
+                    if (ok) {
+                        st.subspace_splits++;
+                        own.len = own_len;
+                        own.c = c;
+                    }
                 }
-                if (!done_split) bc->m = bc->n = bc->c = -1;
             }
             float* qc = nullptr;
             int warm = 0;
@@ -253,8 +267,7 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
                 st.exact_splits++;
                 if (bc && so.chi == P->chi_max) {
                     CT_TRY(ct_basis_from_split(h, l2r ? 0 : 1, mps_sites[i], mps_sites[i + 1], m, n, so.chi, bc->p));
-                    bc->m = m;
-                    bc->n = n;
+                    bc->len = l2r ? m : n;
                     bc->c = so.chi;
                 }
             }

@@ -28,6 +28,8 @@ __global__ void __launch_bounds__(NT) gemm_f64_kernel(GemmDesc g) {
 
     const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    if (g.tri == 1 && n0 >= m0 + BM) return;   // tile strictly above the diagonal
+    const int64_t kend = (g.tri == 2 && m0 + BM < g.K) ? m0 + BM : g.K;
 
     double acc[4][4];
 #pragma unroll
@@ -35,7 +37,7 @@ __global__ void __launch_bounds__(NT) gemm_f64_kernel(GemmDesc g) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
 
-    for (int64_t k0 = 0; k0 < g.K; k0 += BK) {
+    for (int64_t k0 = 0; k0 < kend; k0 += BK) {
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
             const int e = tid + NT * r;

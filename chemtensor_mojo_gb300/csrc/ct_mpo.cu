@@ -6,7 +6,7 @@
 // into one (d^2 wR) x (wL d^2) matrix W12 (sum over the middle MPO bond, once
 // per bond) and applied in a single pass over the intermediate: each thread
 // owns one column i of in(o, :, i), streams its K inputs once per chunk of 8
-// outputs and keeps the weights in shared memory.
+// outputs and keeps the weights (or a chunk of their rows) in shared memory.
 #include "ct_common.cuh"
 
 namespace {
@@ -14,22 +14,31 @@ namespace {
 constexpr int MPO_NT = 128;
 constexpr int MPO_JC = 8;
 
-__global__ void __launch_bounds__(MPO_NT) mpo_apply_f64_kernel(MpoDesc m) {
+// Block (x, o, z) handles columns i of slab o for output rows j in chunk z
+// ([z * jch, z * jch + jch) of J); shared memory holds that chunk of Wt and
+// its output offsets.
+__global__ void __launch_bounds__(MPO_NT) mpo_apply_f64_kernel(MpoDesc m, int64_t jch) {
     if (ct_skip(m.skip)) return;
     extern __shared__ double wsm[];
-    const int64_t JK = m.J * m.K;
-    for (int64_t t = threadIdx.x; t < JK; t += MPO_NT) wsm[t] = m.Wt[t];
+    const int64_t jbeg = (int64_t)blockIdx.z * jch;
+    const int64_t jn = (m.J - jbeg) < jch ? (m.J - jbeg) : jch;
+    int64_t* joff = reinterpret_cast<int64_t*>(wsm + jch * m.K);
+    for (int64_t t = threadIdx.x; t < jn * m.K; t += MPO_NT) wsm[t] = m.Wt[jbeg * m.K + t];
+    for (int64_t j = threadIdx.x; j < jn; j += MPO_NT) {
+        const int64_t jj = jbeg + j;
+        joff[j] = (jj / m.J0) * m.sOj1 + (jj % m.J0) * m.sOj0;
+    }
     __syncthreads();
     const int64_t o = blockIdx.y;
     const int64_t i = (int64_t)blockIdx.x * MPO_NT + threadIdx.x;
     if (i >= m.I) return;
     const double* in = m.in + o * m.sIo + i * m.sIi;
     double* out = m.out + o * m.sOo + i * m.sOi;
-    for (int64_t j0 = 0; j0 < m.J; j0 += MPO_JC) {
+    for (int64_t j0 = 0; j0 < jn; j0 += MPO_JC) {
         double acc[MPO_JC];
 #pragma unroll
         for (int jj = 0; jj < MPO_JC; ++jj) acc[jj] = 0.0;
-        const int nj = (int)((m.J - j0) < MPO_JC ? (m.J - j0) : MPO_JC);
+        const int nj = (int)((jn - j0) < MPO_JC ? (jn - j0) : MPO_JC);
         for (int64_t k = 0; k < m.K; ++k) {
             const double x = in[k * m.sIk];
 #pragma unroll
@@ -39,9 +48,7 @@ __global__ void __launch_bounds__(MPO_NT) mpo_apply_f64_kernel(MpoDesc m) {
 #pragma unroll
         for (int jj = 0; jj < MPO_JC; ++jj) {
             if (jj >= nj) break;
-            const int64_t j = j0 + jj;
-            const int64_t j1 = j / m.J0, jr = j % m.J0;
-            out[j1 * m.sOj1 + jr * m.sOj0] = acc[jj];
+            out[joff[j0 + jj]] = acc[jj];
         }
     }
 }
@@ -88,20 +95,29 @@ __global__ void build_wt_right_kernel(const double* W, double* Wt, int64_t wL, i
 
 int ct_mpo_apply_f64_launch(ct_handle* h, const MpoDesc& m) {
     if (m.O <= 0 || m.I <= 0 || m.J <= 0) return CT_OK;
-    const size_t smem = (size_t)(m.J * m.K) * sizeof(double);
-    if (smem > 200 * 1024) {
-        ct_seterr(h, "MPO weight matrix too large (%lld x %lld)", (long long)m.J, (long long)m.K);
-        return CT_ERR_UNSUPPORTED;
+    // the whole of Wt in shared memory when it fits in 96 KB, else chunks of rows
+    constexpr size_t kBudget = 96 * 1024;
+    const size_t per_row = (size_t)m.K * sizeof(double) + sizeof(int64_t);
+    int64_t jch = m.J;
+    if ((size_t)m.J * per_row > kBudget) {
+        jch = (int64_t)(kBudget / per_row);
+        if (jch >= MPO_JC) jch -= jch % MPO_JC;
+        if (jch < 1) {
+            ct_seterr(h, "MPO weight row too long (K = %lld)", (long long)m.K);
+            return CT_ERR_UNSUPPORTED;
+        }
     }
-    static bool attr_set = false;
-    if (!attr_set) {
+    const size_t smem = (size_t)jch * per_row;
+    const int64_t nz = ct_cdiv(m.J, jch);
+    if (m.O > 65535 || nz > 65535) return CT_ERR_UNSUPPORTED;
+    static int attr_dev = -1;
+    if (attr_dev != h->device) {
         CT_CUDA(h, cudaFuncSetAttribute(mpo_apply_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        200 * 1024));
-        attr_set = true;
+                                        (int)kBudget));
+        attr_dev = h->device;
     }
-    if (m.O > 65535) return CT_ERR_UNSUPPORTED;
-    dim3 grid((unsigned)ct_cdiv(m.I, MPO_NT), (unsigned)m.O);
-    mpo_apply_f64_kernel<<<grid, MPO_NT, smem, h->stream>>>(m); ct_note_launch();
+    dim3 grid((unsigned)ct_cdiv(m.I, MPO_NT), (unsigned)m.O, (unsigned)nz);
+    mpo_apply_f64_kernel<<<grid, MPO_NT, smem, h->stream>>>(m, jch); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }

@@ -62,55 +62,6 @@ __global__ void svd_init_kernel(const double* M, int64_t m, int64_t n, int cols,
         Q[t] = ((t / nvec) == (t % nvec)) ? 1.0 : 0.0;
 }
 
-// ---- large path: one round, one CTA per pair -------------------------------
-__global__ void __launch_bounds__(SVD_NT) svd_round_kernel(double* X, int64_t len, int64_t ldx, double* Q,
-                                                           int64_t nvec, int P, int r, double tol,
-                                                           const double* frob2, int* rot_count) {
-    __shared__ double sm[32];
-    __shared__ double rot[2];
-    __shared__ int do_rot;
-    int p, q;
-    tournament_pair(P, r, blockIdx.x, p, q);
-    if (p >= nvec || q >= nvec) return;
-    double* xp = X + (int64_t)p * ldx;
-    double* xq = X + (int64_t)q * ldx;
-    double a = 0.0, b = 0.0, c = 0.0;
-    for (int64_t i = threadIdx.x; i < len; i += SVD_NT) {
-        const double u = xp[i], v = xq[i];
-        a = fma(u, u, a);
-        b = fma(v, v, b);
-        c = fma(u, v, c);
-    }
-    a = ct_block_sum<SVD_NT>(a, sm);
-    b = ct_block_sum<SVD_NT>(b, sm);
-    c = ct_block_sum<SVD_NT>(c, sm);
-    if (threadIdx.x == 0) {
-        double cs, sn;
-        const double floor = SVD_EPS2 * (*frob2);
-        do_rot = jacobi_rot(a, b, c, tol, floor, cs, sn) ? 1 : 0;
-        if (do_rot) {
-            rot[0] = cs;
-            rot[1] = sn;
-            atomicAdd(rot_count, 1);
-        }
-    }
-    __syncthreads();
-    if (!do_rot) return;
-    const double cs = rot[0], sn = rot[1];
-    for (int64_t i = threadIdx.x; i < len; i += SVD_NT) {
-        const double u = xp[i], v = xq[i];
-        xp[i] = cs * u - sn * v;
-        xq[i] = sn * u + cs * v;
-    }
-    double* qp = Q + (int64_t)p * nvec;
-    double* qq = Q + (int64_t)q * nvec;
-    for (int64_t i = threadIdx.x; i < nvec; i += SVD_NT) {
-        const double u = qp[i], v = qq[i];
-        qp[i] = cs * u - sn * v;
-        qq[i] = sn * u + cs * v;
-    }
-}
-
 // ---- small path: whole Jacobi in one CTA, X and Q in shared memory ------------
 __global__ void __launch_bounds__(SVD_NT) svd_small_kernel(double* Xg, int64_t len, int64_t ldx, double* Qg,
                                                            int nvec, double tol, int max_sweeps, int* status) {

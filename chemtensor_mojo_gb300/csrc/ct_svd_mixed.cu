@@ -24,17 +24,6 @@
 namespace {
 
 constexpr int NT = 256;
-constexpr int MAX_SWEEPS32 = 40;
-
-__device__ __forceinline__ void pair_of(int P, int r, int k, int& p, int& q) {
-    if (k == 0) {
-        p = P - 1;
-        q = r;
-    } else {
-        p = (r + k) % (P - 1);
-        q = (r - k + (P - 1)) % (P - 1);
-    }
-}
 
 __global__ void to_f32_kernel(const double* M, int64_t m, int64_t n, int cols, float* X, float* Q, int64_t nvec) {
     const int64_t len = cols ? m : n;
@@ -46,58 +35,6 @@ __global__ void to_f32_kernel(const double* M, int64_t m, int64_t n, int cols, f
     const int64_t tq = nvec * nvec;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tq; t += (int64_t)gridDim.x * blockDim.x)
         Q[t] = ((t / nvec) == (t % nvec)) ? 1.f : 0.f;
-}
-
-__global__ void __launch_bounds__(NT) round32_kernel(float* X, int64_t len, float* Q, int64_t nvec, int P, int r,
-                                                     double tol, const double* frob2, int* rot_count) {
-    __shared__ double sm[32];
-    __shared__ float rot[2];
-    __shared__ int do_rot;
-    int p, q;
-    pair_of(P, r, blockIdx.x, p, q);
-    if (p >= nvec || q >= nvec) return;
-    float* xp = X + (int64_t)p * len;
-    float* xq = X + (int64_t)q * len;
-    float fa = 0.f, fb = 0.f, fc = 0.f;
-    for (int64_t i = threadIdx.x; i < len; i += NT) {
-        const float u = xp[i], v = xq[i];
-        fa = fmaf(u, u, fa);
-        fb = fmaf(v, v, fb);
-        fc = fmaf(u, v, fc);
-    }
-    const double a = ct_block_sum<NT>((double)fa, sm);
-    const double b = ct_block_sum<NT>((double)fb, sm);
-    const double c = ct_block_sum<NT>((double)fc, sm);
-    if (threadIdx.x == 0) {
-        const double floor = 1.4210854715202004e-14 * (*frob2);   // (FP32 eps)^2 |M|^2
-        int go = 0;
-        if (a > floor && b > floor && c != 0.0 && fabs(c) > tol * sqrt(a * b)) {
-            const double zeta = (b - a) / (2.0 * c);
-            const double t = (fabs(zeta) > 1e150) ? 0.5 / zeta
-                                                  : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-            const double cs = 1.0 / sqrt(1.0 + t * t);
-            rot[0] = (float)cs;
-            rot[1] = (float)(cs * t);
-            go = 1;
-            atomicAdd(rot_count, 1);
-        }
-        do_rot = go;
-    }
-    __syncthreads();
-    if (!do_rot) return;
-    const float cs = rot[0], sn = rot[1];
-    for (int64_t i = threadIdx.x; i < len; i += NT) {
-        const float u = xp[i], v = xq[i];
-        xp[i] = cs * u - sn * v;
-        xq[i] = sn * u + cs * v;
-    }
-    float* qp = Q + (int64_t)p * nvec;
-    float* qq = Q + (int64_t)q * nvec;
-    for (int64_t i = threadIdx.x; i < nvec; i += NT) {
-        const float u = qp[i], v = qq[i];
-        qp[i] = cs * u - sn * v;
-        qq[i] = sn * u + cs * v;
-    }
 }
 
 __global__ void norms32_kernel(const float* X, int64_t len, int64_t nvec, double* sig) {
@@ -278,7 +215,7 @@ int ct_svd_mixed_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_
     }
     // 1. FP32 one-sided Jacobi
     if (nvec >= 2) {
-        double* d_f2 = h->d_scalars + SC_MISC + 200;
+        double* d_f2 = h->d_scalars + SC_SVD_FROB2;
         CT_TRY(ct_reduce_nrm2sq(h, m * n, M, d_f2, nullptr));
         CT_TRY(ct_jacobi::run<float>(h, X, len, Q, nvec, 1e-6, 1.4210854715202004e-14, d_f2, nullptr));
     }

@@ -18,6 +18,8 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <stdlib.h>
+
 #include <algorithm>
 #include <new>
 
@@ -298,6 +300,183 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
 }
 
+// Persistent variant: one CTA per SM walks tiles t = blockIdx.x, += gridDim.x.
+// The accumulator is double-buffered in TMEM (2 x BN columns), so the epilogue
+// of tile i (TMEM -> global) overlaps the MMAs of tile i+1; the smem ring and
+// its phases run on across tiles.  acc_full[b] is committed by the MMA thread,
+// acc_empty[b] is released by the four epilogue warps.
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <int BN, int STAGES>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    tc_gemm_persist_kernel(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
+                           const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl, int M,
+                           int N, int Kpad, TcEpi epi, const int* skip, int* status) {
+    using L = TcSmem<BN, STAGES>;
+    if (ct_skip(skip)) return;
+    extern __shared__ uint8_t tc_smem_raw[];
+    uint8_t* smem = tc_smem_raw + ((1024u - (smem_u32(tc_smem_raw) & 1023u)) & 1023u);
+    uint64_t* full = (uint64_t*)(smem + L::TILE_BYTES);
+    uint64_t* empty = full + STAGES;
+    uint64_t* acc_full = empty + STAGES;
+    uint64_t* acc_empty = acc_full + 2;
+    uint32_t* tmem_slot = (uint32_t*)(acc_empty + 2);
+    volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tiles_n = (N + BN - 1) / BN;
+    const int tiles = tiles_n * ((M + TC_BM - 1) / TC_BM);
+    const int nkb = Kpad / TC_BK;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 4);
+        }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"((uint32_t)(2 * BN))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int g = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+                const int m0 = (t / tiles_n) * TC_BM, n0 = (t % tiles_n) * BN;
+                for (int kb = 0; kb < nkb; ++kb, ++g) {
+                    const int s = g % STAGES;
+                    const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
+                    if (g >= STAGES && !mbar_wait(&empty[s], ph ^ 1u, abort_flag)) {
+                        *abort_flag = 1;
+                        ct_set_status(status, CT_ERR_CUDA);
+                        ok = false;
+                        break;
+                    }
+                    uint8_t* st = smem + s * L::STAGE_BYTES;
+                    mbar_expect_tx(&full[s], L::STAGE_BYTES);
+                    const int x = kb * TC_BK;
+                    tma_load_2d(st, &tmAh, x, m0, &full[s]);
+                    tma_load_2d(st + L::A_BYTES, &tmAl, x, m0, &full[s]);
+                    tma_load_2d(st + 2 * L::A_BYTES, &tmBh, x, n0, &full[s]);
+                    tma_load_2d(st + 2 * L::A_BYTES + L::B_BYTES, &tmBl, x, n0, &full[s]);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_tf32(TC_BM, BN);
+            int g = 0, i = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++i) {
+                const int b = i & 1, u = i >> 1;
+                if (u > 0 && !mbar_wait(&acc_empty[b], (uint32_t)((u - 1) & 1), abort_flag)) {
+                    *abort_flag = 1;
+                    ct_set_status(status, CT_ERR_CUDA);
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t dt = tmem + (uint32_t)(b * BN);
+                for (int kb = 0; kb < nkb; ++kb, ++g) {
+                    const int s = g % STAGES;
+                    const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
+                    if (!mbar_wait(&full[s], ph, abort_flag)) {
+                        *abort_flag = 1;
+                        ct_set_status(status, CT_ERR_CUDA);
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a_hi = smem_u32(smem + s * L::STAGE_BYTES);
+                    const uint32_t a_lo = a_hi + L::A_BYTES;
+                    const uint32_t b_hi = a_hi + 2 * L::A_BYTES;
+                    const uint32_t b_lo = b_hi + L::B_BYTES;
+#pragma unroll
+                    for (int kk = 0; kk < TC_BK / 8; ++kk) {
+                        const uint32_t off = kk * 32;
+                        const uint32_t acc0 = (kb > 0 || kk > 0) ? 1u : 0u;
+                        mma_tf32(dt, sw128_desc(a_lo + off), sw128_desc(b_hi + off), idesc, acc0);
+                        mma_tf32(dt, sw128_desc(a_hi + off), sw128_desc(b_lo + off), idesc, 1u);
+                        mma_tf32(dt, sw128_desc(a_hi + off), sw128_desc(b_hi + off), idesc, 1u);
+                    }
+                    mma_commit(&empty[s]);
+                }
+                if (ok) mma_commit(&acc_full[b]);
+            }
+        }
+    } else {
+        const int q = warp & 3;
+        const int row = q * 32 + lane;
+        int i = 0;
+        for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++i) {
+            const int b = i & 1, u = i >> 1;
+            const bool ok = mbar_wait(&acc_full[b], (uint32_t)(u & 1), abort_flag);
+            if (!ok) {
+                *abort_flag = 1;
+                ct_set_status(status, CT_ERR_CUDA);
+                break;
+            }
+            __syncwarp();
+            tc_fence_after();
+            const int m0 = (t / tiles_n) * TC_BM, n0 = (t % tiles_n) * BN;
+            const int64_t m = (int64_t)m0 + row;
+            const bool mvalid = m < M;
+            int64_t rbase = 0;
+            if (mvalid) rbase = (m / epi.M0) * epi.sCm1 + (m % epi.M0) * epi.sCm0;
+            const uint32_t tq = tmem + (uint32_t)(b * BN) + ((uint32_t)(q * 32) << 16);
+#pragma unroll 1
+            for (int c = 0; c < BN; c += 16) {
+                uint32_t r[16];
+                tmem_ld16(tq + (uint32_t)c, r);
+                if (!mvalid) continue;
+                if (epi.out_fp64) {
+                    double* Cd = (double*)epi.C + rbase;
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int64_t n = (int64_t)n0 + c + j;
+                        if (n < N) {
+                            double v = epi.alpha * (double)__uint_as_float(r[j]);
+                            if (epi.beta != 0.0) v = fma(epi.beta, Cd[n], v);
+                            Cd[n] = v;
+                        }
+                    }
+                } else {
+                    float* Cf = (float*)epi.C + rbase;
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int64_t n = (int64_t)n0 + c + j;
+                        if (n < N) Cf[n] = (float)epi.alpha * __uint_as_float(r[j]);
+                    }
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[b]);
+        }
+    }
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)(2 * BN))
+                     : "memory");
+    }
+}
+
 // ---------------------------------------------------------------------------
 // operand packer: FP64 source -> split TF32 planes [rows][ldk], K-major.
 // row r = r1 * R0 + r0 ; col k = k1 * K0p + k0 (k0 < K0 valid, K0..K0p zero)
@@ -315,27 +494,35 @@ struct PackDesc {
 };
 
 // 32 x 32 tiles through shared memory; K_FAST: source contiguous along k0.
+// The tile's 32 row offsets and 32 column offsets are computed once per block
+// (the 64-bit divisions of the index split would otherwise dominate).
 template <bool K_FAST>
-__global__ void pack_split_kernel(PackDesc p, const int* skip) {
+__global__ void __launch_bounds__(256) pack_split_kernel(PackDesc p, const int* skip) {
     if (ct_skip(skip)) return;
     __shared__ double tile[32][33];
+    __shared__ int64_t roff[32], koff[32];
     const int64_t rb = (int64_t)blockIdx.y * 32;
     const int64_t kb = (int64_t)blockIdx.x * 32;   // in padded k space
     const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+    if (ty == 0) {
+        const int64_t r = rb + tx;
+        roff[tx] = (r < p.rows) ? (r / p.R0) * p.s_r1 + (r % p.R0) * p.s_r0 : -1;
+    } else if (ty == 1) {
+        const int64_t k = kb + tx;
+        int64_t o = -1;
+        if (k < p.ldk) {
+            const int64_t k1 = k / p.K0p, k0 = k % p.K0p;
+            if (k1 < p.K1 && k0 < p.K0) o = k1 * p.s_k1 + k0 * p.s_k0;
+        }
+        koff[tx] = o;
+    }
     double sc = p.scale;
     if (p.scale_ptr) sc *= *p.scale_ptr;
+    __syncthreads();
     for (int i = ty; i < 32; i += 8) {
-        int64_t r, k;
-        if (K_FAST) { r = rb + i; k = kb + tx; }
-        else        { r = rb + tx; k = kb + i; }
-        double v = 0.0;
-        if (r < p.rows && k < p.ldk) {
-            const int64_t k1 = k / p.K0p, k0 = k % p.K0p;
-            if (k1 < p.K1 && k0 < p.K0) {
-                const int64_t r1 = r / p.R0, r0 = r % p.R0;
-                v = p.src[r1 * p.s_r1 + r0 * p.s_r0 + k1 * p.s_k1 + k0 * p.s_k0];
-            }
-        }
+        const int ri = K_FAST ? i : tx, ki = K_FAST ? tx : i;
+        const int64_t ro = roff[ri], ko = koff[ki];
+        const double v = (ro >= 0 && ko >= 0) ? p.src[ro + ko] : 0.0;
         if (K_FAST) tile[i][tx] = v;
         else tile[tx][i] = v;
     }
@@ -360,23 +547,34 @@ struct MpoTcDesc {
     const int* skip;
 };
 
-constexpr int MPOT_NT = 128, MPOT_JC = 16;
+constexpr int MPOT_NT = 128, MPOT_JC = 32;
 
-__global__ void __launch_bounds__(MPOT_NT) mpo_tc_kernel(MpoTcDesc m) {
+// Block (x, o, z) handles columns i of slab o for the output rows j in chunk z
+// ([z * jch, z * jch + jch) of J).  Dynamic shared memory: that chunk of Wt as
+// FP32 [jch][K], then its jch output offsets (int64).
+__global__ void __launch_bounds__(MPOT_NT) mpo_tc_kernel(MpoTcDesc m, int64_t jch) {
     if (ct_skip(m.skip)) return;
     extern __shared__ float wsf[];
-    const int64_t JK = m.J * m.K;
-    for (int64_t t = threadIdx.x; t < JK; t += MPOT_NT) wsf[t] = (float)m.Wt[t];
+    const int64_t jbeg = (int64_t)blockIdx.z * jch;
+    const int64_t jn = (m.J - jbeg) < jch ? (m.J - jbeg) : jch;
+    const int64_t JK = jn * m.K;
+    int64_t* joff = reinterpret_cast<int64_t*>(wsf + ((jch * m.K + 1) & ~(int64_t)1));
+    for (int64_t t = threadIdx.x; t < JK; t += MPOT_NT) wsf[t] = (float)m.Wt[jbeg * m.K + t];
+    for (int64_t j = threadIdx.x; j < jn; j += MPOT_NT) {
+        const int64_t jj = jbeg + j;
+        joff[j] = (jj / m.J0) * m.sOj1 + (jj % m.J0) * m.sOj0;
+    }
     __syncthreads();
     const int64_t o = blockIdx.y;
     const int64_t i = (int64_t)blockIdx.x * MPOT_NT + threadIdx.x;
     if (i >= m.I) return;
     const float* in = m.in + o * m.sIo + i * m.sIi;
-    for (int64_t j0 = 0; j0 < m.J; j0 += MPOT_JC) {
+    const int64_t obase = o * m.sOo + i * m.sOi;
+    for (int64_t j0 = 0; j0 < jn; j0 += MPOT_JC) {
         float acc[MPOT_JC];
 #pragma unroll
         for (int jj = 0; jj < MPOT_JC; ++jj) acc[jj] = 0.f;
-        const int nj = (int)((m.J - j0) < MPOT_JC ? (m.J - j0) : MPOT_JC);
+        const int nj = (int)((jn - j0) < MPOT_JC ? (jn - j0) : MPOT_JC);
         for (int64_t k = 0; k < m.K; ++k) {
             const float x = in[k * m.sIk];
 #pragma unroll
@@ -386,8 +584,7 @@ __global__ void __launch_bounds__(MPOT_NT) mpo_tc_kernel(MpoTcDesc m) {
 #pragma unroll
         for (int jj = 0; jj < MPOT_JC; ++jj) {
             if (jj >= nj) break;
-            const int64_t j = j0 + jj;
-            const int64_t off = o * m.sOo + i * m.sOi + (j / m.J0) * m.sOj1 + (j % m.J0) * m.sOj0;
+            const int64_t off = obase + joff[j0 + jj];
             float h, l;
             split_tf32((double)acc[jj], h, l);
             m.hi[off] = h;
@@ -437,11 +634,52 @@ int make_map(ct_handle* h, CUtensorMap* m, const float* base, int64_t rows, int6
 constexpr int GEMM_BN = 128;
 constexpr int GEMM_STAGES = 3;
 
+// persistent kernel by default; CTDMRG_TC_TILE_PER_CTA=1 selects the one-tile-per-CTA kernel
+bool tc_use_persistent() {
+    static const bool v = [] {
+        const char* e = getenv("CTDMRG_TC_TILE_PER_CTA");
+        return !(e && e[0] == '1');
+    }();
+    return v;
+}
+
 struct SplitOperand {
     float* hi = nullptr;
     float* lo = nullptr;
     int64_t rows = 0, ldk = 0;
 };
+
+constexpr int KTIME_SLOTS = 4096;
+
+// Sum the elapsed times of the pending event pairs (waits for the last one).
+int ktime_harvest(ct_handle* h) {
+    if (h->ktime_pending == 0) return CT_OK;
+    CT_CUDA(h, cudaEventSynchronize(h->ktime_ev[2 * (h->ktime_pending - 1) + 1]));
+    for (int i = 0; i < h->ktime_pending; ++i) {
+        float ms = 0.f;
+        CT_CUDA(h, cudaEventElapsedTime(&ms, h->ktime_ev[2 * i], h->ktime_ev[2 * i + 1]));
+        h->ktime_ms += ms;
+        h->ktime_flops += h->ktime_slot_flops[i];
+    }
+    h->ktime_launches += h->ktime_pending;
+    h->ktime_pending = 0;
+    return CT_OK;
+}
+
+int ktime_begin(ct_handle* h, double flops, int* slot) {
+    *slot = -1;
+    if (!h->ktime_on) return CT_OK;
+    if (h->ktime_ev.empty()) {
+        h->ktime_ev.resize(2 * KTIME_SLOTS, nullptr);
+        h->ktime_slot_flops.resize(KTIME_SLOTS, 0.0);
+        for (auto& e : h->ktime_ev) CT_CUDA(h, cudaEventCreate(&e));
+    }
+    if (h->ktime_pending == KTIME_SLOTS) CT_TRY(ktime_harvest(h));
+    *slot = h->ktime_pending++;
+    h->ktime_slot_flops[*slot] = flops;
+    CT_CUDA(h, cudaEventRecord(h->ktime_ev[2 * *slot], h->stream));
+    return CT_OK;
+}
 
 int tc_gemm_launch(ct_handle* h, const SplitOperand& A, const SplitOperand& B, int64_t M, int64_t N,
                    const TcEpi& epi, const int* skip) {
@@ -458,13 +696,25 @@ int tc_gemm_launch(ct_handle* h, const SplitOperand& A, const SplitOperand& B, i
     if (attr_dev != h->device) {
         CT_CUDA(h, cudaFuncSetAttribute(tc_gemm_kernel<GEMM_BN, GEMM_STAGES>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, L::TOTAL));
+        CT_CUDA(h, cudaFuncSetAttribute(tc_gemm_persist_kernel<GEMM_BN, GEMM_STAGES>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, L::TOTAL));
         attr_dev = h->device;
     }
-    dim3 grid((unsigned)ct_cdiv(N, GEMM_BN), (unsigned)ct_cdiv(M, TC_BM));
-    if (grid.y > 65535) return CT_ERR_UNSUPPORTED;
-    tc_gemm_kernel<GEMM_BN, GEMM_STAGES><<<grid, TC_THREADS, L::TOTAL, h->stream>>>(
-        ta_h, ta_l, tb_h, tb_l, (int)M, (int)N, (int)A.ldk, epi, skip, h->d_status); ct_note_launch();
+    const int64_t tiles = ct_cdiv(N, GEMM_BN) * ct_cdiv(M, TC_BM);
+    int slot = -1;
+    CT_TRY(ktime_begin(h, 2.0 * (double)M * (double)N * (double)A.ldk, &slot));
+    if (tc_use_persistent()) {
+        const int64_t grid = tiles < h->num_sms ? tiles : h->num_sms;
+        tc_gemm_persist_kernel<GEMM_BN, GEMM_STAGES><<<(unsigned)grid, TC_THREADS, L::TOTAL, h->stream>>>(
+            ta_h, ta_l, tb_h, tb_l, (int)M, (int)N, (int)A.ldk, epi, skip, h->d_status); ct_note_launch();
+    } else {
+        dim3 grid((unsigned)ct_cdiv(N, GEMM_BN), (unsigned)ct_cdiv(M, TC_BM));
+        if (grid.y > 65535) return CT_ERR_UNSUPPORTED;
+        tc_gemm_kernel<GEMM_BN, GEMM_STAGES><<<grid, TC_THREADS, L::TOTAL, h->stream>>>(
+            ta_h, ta_l, tb_h, tb_l, (int)M, (int)N, (int)A.ldk, epi, skip, h->d_status); ct_note_launch();
+    }
     CT_LAUNCH_CHECK(h);
+    if (slot >= 0) CT_CUDA(h, cudaEventRecord(h->ktime_ev[2 * slot + 1], h->stream));
     return CT_OK;
 }
 
@@ -493,15 +743,25 @@ PackDesc pack_desc(const double* src, int64_t rows, int64_t R0, int64_t s_r1, in
 
 int mpo_tc_launch(ct_handle* h, const MpoTcDesc& m) {
     if (m.O <= 0 || m.I <= 0 || m.J <= 0) return CT_OK;
-    const size_t smem = (size_t)(m.J * m.K) * sizeof(float);
-    if (smem > 200 * 1024 || m.O > 65535) return CT_ERR_UNSUPPORTED;
+    // the whole of Wt in shared memory when it fits in 96 KB, else chunks of rows
+    constexpr size_t kBudget = 96 * 1024;
+    const size_t per_row = (size_t)m.K * sizeof(float) + sizeof(int64_t);
+    int64_t jch = m.J;
+    if ((size_t)m.J * per_row + 8 > kBudget) {
+        jch = (int64_t)((kBudget - 8) / per_row);
+        if (jch >= MPOT_JC) jch -= jch % MPOT_JC;
+        if (jch < 1) return CT_ERR_UNSUPPORTED;
+    }
+    const size_t smem = (size_t)((jch * m.K + 1) & ~(int64_t)1) * sizeof(float) + (size_t)jch * sizeof(int64_t);
+    const int64_t nz = ct_cdiv(m.J, jch);
+    if (m.O > 65535 || nz > 65535) return CT_ERR_UNSUPPORTED;
     static int attr_dev = -1;
     if (attr_dev != h->device) {
-        CT_CUDA(h, cudaFuncSetAttribute(mpo_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        CT_CUDA(h, cudaFuncSetAttribute(mpo_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBudget));
         attr_dev = h->device;
     }
-    dim3 grid((unsigned)ct_cdiv(m.I, MPOT_NT), (unsigned)m.O);
-    mpo_tc_kernel<<<grid, MPOT_NT, smem, h->stream>>>(m); ct_note_launch();
+    dim3 grid((unsigned)ct_cdiv(m.I, MPOT_NT), (unsigned)m.O, (unsigned)nz);
+    mpo_tc_kernel<<<grid, MPOT_NT, smem, h->stream>>>(m, jch); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
@@ -759,5 +1019,24 @@ extern "C" CT_API int ct_tc_gemm_time(ct_handle* h, int64_t m, int64_t n, int64_
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *ms_per_launch = (double)ms / reps;
+    return CT_OK;
+}
+
+extern "C" CT_API int ct_kernel_timing(ct_handle* h, int enable) {
+    if (!h) return CT_ERR_INVALID;
+    CT_TRY(ktime_harvest(h));
+    h->ktime_on = enable != 0;
+    h->ktime_launches = 0;
+    h->ktime_ms = 0.0;
+    h->ktime_flops = 0.0;
+    return CT_OK;
+}
+
+extern "C" CT_API int ct_kernel_timing_read(ct_handle* h, int64_t* launches, double* ms, double* flops) {
+    if (!h || !launches || !ms || !flops) return CT_ERR_INVALID;
+    CT_TRY(ktime_harvest(h));
+    *launches = h->ktime_launches;
+    *ms = h->ktime_ms;
+    *flops = h->ktime_flops;
     return CT_OK;
 }

@@ -39,17 +39,19 @@ class DMRGParams:
     krylov_tol: float
     energy_tol: float
     two_site: bool = True
-    verbose: bool = False
+    verbose: int = 0            # 1: per-sweep energies; 2: also every split
     prec: str = "fp64"
     max_rotations: int = REFERENCE_JACOBI_ROTATIONS
     reorth: bool = False
     final_rayleigh: bool = False
+    keep_bases: bool = False
 
     def to_c(self) -> _lib.ct_dmrg_params:
         return _lib.ct_dmrg_params(int(self.num_sweeps), int(self.chi_max), float(self.eps_trunc),
                                    int(self.max_krylov_iter), float(self.krylov_tol), float(self.energy_tol),
-                                   int(bool(self.two_site)), int(bool(self.verbose)), _lib.PRECISIONS[self.prec],
-                                   int(self.max_rotations), int(bool(self.reorth)), int(bool(self.final_rayleigh)))
+                                   int(bool(self.two_site)), int(self.verbose), _lib.PRECISIONS[self.prec],
+                                   int(self.max_rotations), int(bool(self.reorth)), int(bool(self.final_rayleigh)),
+                                   int(bool(self.keep_bases)))
 
 
 @dataclass

@@ -153,6 +153,11 @@ typedef struct ct_dmrg_params {
     int reorth;          /* full FP64 reorthogonalisation                      */
     int final_rayleigh;  /* also return <psi|H|psi>/<psi|psi> of the final MPS,
                             contracted in FP64 (stats.energy_rayleigh)          */
+    int keep_bases;      /* mixed form: the first half-sweep's large splits may
+                            start from the bond bases kept by the previous call
+                            on this handle.  Only valid when the MPS passed in
+                            is the one that call returned and the MPO is the
+                            same; 0 forgets them at the start of the call.     */
 } ct_dmrg_params;
 
 typedef struct ct_dmrg_stats {
@@ -237,6 +242,15 @@ CT_API int ct_heff2_apply_noalloc(void* stream, const double* theta, const doubl
  * Average device time of one launch of the TF32x3 tcgen05 GEMM kernel on an
  * m x n x k problem with operands already split and resident in HBM.       */
 CT_API int ct_tc_gemm_time(ct_handle* h, int64_t m, int64_t n, int64_t k, int reps, double* ms_per_launch);
+
+/* Live timing of the tensor-core GEMM inside real work (no reference
+ * counterpart).  ct_kernel_timing(h, 1) resets the totals and makes every
+ * TF32x3 GEMM launch on h record a CUDA event pair on h's stream;
+ * ct_kernel_timing_read waits for the recorded launches and returns their
+ * count, summed device milliseconds and summed algorithmic FLOPs
+ * (2 M N K, K rounded up to 32).  ct_kernel_timing(h, 0) stops recording. */
+CT_API int ct_kernel_timing(ct_handle* h, int enable);
+CT_API int ct_kernel_timing_read(ct_handle* h, int64_t* launches, double* ms, double* flops);
 
 #ifdef __cplusplus
 }

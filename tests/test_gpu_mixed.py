@@ -159,7 +159,12 @@ def test_svd_split_mixed(ctx, dims, chi_max, eps, l2r):
         recon = np.tensordot(a, b, axes=([2], [0]))
         committed = np.sum((recon - th) ** 2) / np.sum(th * th)
         assert committed <= 1.5 * eps + 1e-10   # FP32 subspace resolves tail weights to ~1e-10
-        assert abs(chi - info.chi) <= max(8, info.chi // 10)
+        if eps >= 1e-10:
+            assert abs(chi - info.chi) <= max(8, info.chi // 10)
+        else:
+            # below the FP32 floor the tail weights read high, so more states
+            # are kept, never fewer
+            assert chi >= info.chi - 8
     kk = min(chi, info.chi)
     assert np.allclose(S[:kk], info.S[:kk], rtol=1e-5, atol=1e-6 * info.S[0])
     am, bm = a.reshape(-1, chi), b.reshape(chi, -1)
@@ -174,18 +179,19 @@ def test_svd_split_mixed(ctx, dims, chi_max, eps, l2r):
 
 
 def test_dmrg_warm_subspace_split(ctx):
-    """Heisenberg L=16, chi_max=64 (bonds of 128 x 128, chi_max binding), 4 sweeps in one call:
-    after the first sweep the mixed form splits large bonds by the warm-started subspace
-    iteration; its FP64 Rayleigh energy matches the FP64 form (exact Jacobi splits) to 1e-9."""
+    """Heisenberg L=20, chi_max=128 (central bonds 256 x 256, chi_max binding), 4 sweeps in one
+    call: after the first half-sweep the mixed form splits the large bonds by the warm-started
+    subspace iteration; its FP64 Rayleigh energy matches the FP64 form (exact Jacobi splits) to
+    1e-9 and the canonical factors are orthonormal to 1e-12."""
     ct = ct_mod()
-    L = 16
+    L = 20
     mpo_a = oh.spin_half_xxz(L, 1.0)
-    sites, _ = orng.create_random_mps_c_compatible(L, 2, 64, 2)
+    sites, _ = orng.create_random_mps_c_compatible(L, 2, 128, 2)
     mps_a = od.right_normalize(sites)
     out = {}
     for prec in ("fp64", "tf32x3"):
         st = ct.DMRGStats()
-        p = ct.DMRGParams(num_sweeps=4, chi_max=64, eps_trunc=0.0, max_krylov_iter=20, krylov_tol=1e-10,
+        p = ct.DMRGParams(num_sweeps=4, chi_max=128, eps_trunc=0.0, max_krylov_iter=20, krylov_tol=1e-10,
                           energy_tol=0.0, max_rotations=0, prec=prec, final_rayleigh=True)
         E, mps = ct.dmrg_two_site(ctx, ct.mpo_from_arrays(ctx, mpo_a), ct.mps_from_arrays(ctx, mps_a), p, st)
         out[prec] = st
@@ -197,3 +203,33 @@ def test_dmrg_warm_subspace_split(ctx):
     assert out["tf32x3"].subspace_splits > 0
     e64 = out["fp64"].energy_rayleigh
     assert abs(out["tf32x3"].energy_rayleigh - e64) <= 1e-9 * abs(e64)
+
+
+def test_dmrg_keep_bases_across_calls(ctx):
+    """keep_bases: a call that continues the previous call's MPS on the same handle starts its
+    first left-to-right half-sweep from the kept bases (more subspace splits than a cold call),
+    and the energy keeps improving."""
+    ct = ct_mod()
+    L = 20
+    mpo = ct.mpo_from_arrays(ctx, oh.spin_half_xxz(L, 1.0))
+    sites, _ = orng.create_random_mps_c_compatible(L, 2, 128, 3)
+    mps = ct.mps_from_arrays(ctx, od.right_normalize(sites))
+
+    def params(keep):
+        return ct.DMRGParams(num_sweeps=1, chi_max=128, eps_trunc=0.0, max_krylov_iter=20, krylov_tol=1e-10,
+                             energy_tol=0.0, max_rotations=0, prec="tf32x3", final_rayleigh=True, keep_bases=keep)
+
+    st1 = ct.DMRGStats()
+    p1 = params(False)
+    p1.num_sweeps = 2
+    E1, mps = ct.dmrg_two_site(ctx, mpo, mps, p1, st1)
+    st_keep = ct.DMRGStats()
+    E2, mps = ct.dmrg_two_site(ctx, mpo, mps, params(True), st_keep)
+    st_cold = ct.DMRGStats()
+    E3, mps = ct.dmrg_two_site(ctx, mpo, mps, params(False), st_cold)
+    assert st_cold.subspace_splits > 0
+    assert st_keep.subspace_splits > st_cold.subspace_splits
+    assert st_keep.subspace_splits + st_keep.exact_splits == st_cold.subspace_splits + st_cold.exact_splits
+    # sweeps at fixed chi_max do not raise the energy beyond truncation noise
+    assert st_keep.energy_rayleigh <= st1.energy_rayleigh + 1e-8 * abs(E1)
+    assert st_cold.energy_rayleigh <= st_keep.energy_rayleigh + 1e-8 * abs(E1)
