@@ -42,7 +42,8 @@ class ct_dmrg_params(C.Structure):
     _fields_ = [("num_sweeps", C.c_int), ("chi_max", C.c_int), ("eps_trunc", C.c_double),
                 ("max_krylov_iter", C.c_int), ("krylov_tol", C.c_double), ("energy_tol", C.c_double),
                 ("two_site", C.c_int), ("verbose", C.c_int), ("prec", C.c_int), ("max_rotations", C.c_int),
-                ("reorth", C.c_int), ("final_rayleigh", C.c_int), ("keep_bases", C.c_int)]
+                ("reorth", C.c_int), ("final_rayleigh", C.c_int), ("keep_bases", C.c_int),
+                ("split_power_steps", C.c_int)]
 
 
 class ct_dmrg_stats(C.Structure):
@@ -92,6 +93,8 @@ SIGNATURES = {
     "ct_random_mps_host": [I32, I32, I32, C.c_uint64, C.POINTER(I64), PP],
     "ct_rng_randnf_host": [C.c_uint64, I64, C.POINTER(C.c_float)],
     "ct_tc_gemm_time": [P, I64, I64, I64, I32, C.POINTER(D)],
+    "ct_svd_split_warm": [P, P, I64, I64, I64, I64, I32, P, I32, P, P, P, C.POINTER(I32), C.POINTER(D),
+                          C.POINTER(D)],
     "ct_kernel_timing": [P, I32],
     "ct_kernel_timing_read": [P, C.POINTER(I64), C.POINTER(D), C.POINTER(D)],
     "ct_heff2_apply_noalloc": [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, I64],

@@ -496,4 +496,41 @@ int ct_svd_split(ct_handle* h, int prec, const double* theta, int64_t Dl, int64_
     return CT_OK;
 }
 
+int ct_svd_split_warm(ct_handle* h, const double* theta, int64_t Dl, int64_t d, int64_t Dr, int64_t chi,
+                      int left_to_right, const double* basis_in, int power_steps,
+                      double* basis_out, double* A_out, double* B_out, int* accepted, double* discarded_host,
+                      double* pivots_host) {
+    CT_NULLCHK(h, h);
+    CT_NULLCHK(h, theta);
+    CT_NULLCHK(h, basis_in);
+    CT_NULLCHK(h, basis_out);
+    CT_NULLCHK(h, A_out);
+    CT_NULLCHK(h, B_out);
+    CT_NULLCHK(h, accepted);
+    CT_POSCHK(h, Dl);
+    CT_POSCHK(h, d);
+    CT_POSCHK(h, Dr);
+    const int64_t m = Dl * d, n = d * Dr;
+    if (chi <= 0 || chi > (m < n ? m : n)) return CT_ERR_SHAPE;
+    if (!ct_tc_available(h)) return CT_ERR_UNSUPPORTED;
+    CT_TRY(ct_reserve(h, ct_split_subspace_ws_bytes(m, n, chi)));
+    Arena ar(h);
+    CT_TRY(ct_reduce_nrm2sq(h, m * n, theta, h->d_scalars + SC_THETA_NSQ, nullptr));
+    SvdOut o;
+    bool ok = false;
+    if (power_steps < 0) return CT_ERR_INVALID;
+    CT_TRY(ct_split_subspace(h, ar, theta, m, n, chi, left_to_right ? 0 : 1, basis_in, basis_out, A_out, B_out,
+                             h->d_scalars + SC_THETA_NSQ, 0.0, -1.0, power_steps, &o, &ok));
+    CT_TRY(check_status(h));
+    *accepted = ok ? 1 : 0;
+    if (discarded_host)
+        *discarded_host = (o.sum_s2_all > 0.0) ? (o.sum_s2_all - o.sum_s2_kept) / o.sum_s2_all : 0.0;
+    if (pivots_host) {
+        pivots_host[0] = o.min_pivot;
+        pivots_host[1] = o.min_pivot2;
+        pivots_host[2] = o.chol_fail;
+    }
+    return CT_OK;
+}
+
 }  // extern "C"

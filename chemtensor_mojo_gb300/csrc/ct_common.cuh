@@ -36,6 +36,7 @@ struct ct_handle {
     struct BasisCache {
         double* p = nullptr;
         int64_t cap = 0, len = -1, c = -1;
+        double disc = -1.0;   // discarded weight of the split that wrote it
     };
     std::vector<BasisCache> basis_cache;
     // diagnostics: Jacobi sweeps of the last SVD split, and the running total

@@ -167,9 +167,20 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         const int64_t m = Dl * d, n = d * Dr;
         size_t need = ct_lanczos_ws_bytes(prec, Dl, d, Dr, wL, wM, wR, P->max_krylov_iter);
         need = std::max(need, ct_split_ws_bytes(prec, m, n, P->chi_max, l2r ? 0 : 1));
-        const bool use_subspace = (prec == CT_PREC_TF32X3) && !ct_svd_is_small(m, n, l2r ? 0 : 1) &&
-                                  (int64_t)P->chi_max < std::min(m, n);
-        if (use_subspace) need = std::max(need, ct_split_subspace_ws_bytes(m, n, P->chi_max));
+        // mixed form, large bonds: where chi_max binds, the warm subspace split
+        // when the other direction kept a basis of this bond; the bases are kept
+        // on every large bond, so a bond that starts binding has one
+        const bool mixed_large = (prec == CT_PREC_TF32X3) && P->split_power_steps >= 0 &&
+                                 !ct_svd_is_small(m, n, l2r ? 0 : 1);
+        const bool binding = (int64_t)P->chi_max < std::min(m, n);
+        const bool use_subspace = mixed_large && binding;
+        const int64_t c_sub = std::min<int64_t>(P->chi_max, std::min(m, n));
+        if (mixed_large) {
+            need = std::max(need, ct_split_subspace_ws_bytes(m, n, c_sub));
+            // short-side Jacobi + gauge move: the basis rows next to the subspace split's workspace
+            need = std::max(need, ct_split_subspace_ws_bytes(m, n, c_sub) + ct_bytes(c_sub * std::max(m, n), 8));
+            need = std::max(need, ct_split_ws_bytes(prec, m, n, P->chi_max, l2r ? 1 : 0));
+        }
         const int64_t chi_ub = std::min<int64_t>(std::min(m, n), P->chi_max);
         need = std::max(need, l2r ? ct_env_ws_bytes(prec, Dl, d, chi_ub, wL, wM)
                                   : ct_env_ws_bytes(prec, chi_ub, d, Dr, wM, wR));
@@ -204,15 +215,16 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         }
         CT_CUDA(h, cudaEventRecord(ev_s.a, h->stream));
         SvdOut so;
+        bool last_split_subspace = false;
         {
             Arena ar(h);
             // kept bond bound by the capacity of the sites it is written into
             bool done_split = false;
             ct_handle::BasisCache* bc = nullptr;
-            if (use_subspace) {
+            if (mixed_large) {
                 // this split keeps its far-side basis in `own`; it starts from the
                 // basis the last split of the bond in the other direction kept
-                const int64_t c = P->chi_max, own_len = l2r ? m : n, src_len = l2r ? n : m;
+                const int64_t c = c_sub, own_len = l2r ? m : n, src_len = l2r ? n : m;
                 ct_handle::BasisCache& own = h->basis_cache[(size_t)(2 * i + (l2r ? 0 : 1))];
                 const ct_handle::BasisCache& src = h->basis_cache[(size_t)(2 * i + (l2r ? 1 : 0))];
                 bc = &own;
@@ -224,12 +236,13 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
                     own.cap = c * own_len;
                 }
                 own.len = own.c = -1;
-                if (src.p && src.len == src_len && src.c == c) {
+                if (use_subspace && src.p && src.len == src_len && src.c == c) {
                     bool ok = false;
-                    CT_TRY(ct_split_subspace(h, ar, th_opt.p, m, n, c, l2r ? 0 : 1, src.p, own.p, mps_sites[i],
-                                             mps_sites[i + 1], h->d_scalars + SC_THETA_NSQ, P->eps_trunc, 0, &so,
-                                             &ok));
+                    CT_TRY(ct_split_subspace(h, ar, th_opt.p, m, n, c, l2r ? 0 : 1, src.p, own.p,
+                                             mps_sites[i], mps_sites[i + 1], h->d_scalars + SC_THETA_NSQ,
+                                             P->eps_trunc, src.disc, P->split_power_steps, &so, &ok));
                     done_split = ok;
+                    last_split_subspace = ok;
                     if (P->verbose >= 2)
                         fprintf(stderr,
                                 "bond %d %s: subspace split %s (pivots %.3g %.3g%s, kept %.12g of %.12g)\n", i,
@@ -239,6 +252,7 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
                         st.subspace_splits++;
                         own.len = own_len;
                         own.c = c;
+                        own.disc = so.sum_s2_all > 0.0 ? 1.0 - so.sum_s2_kept / so.sum_s2_all : 0.0;
                     }
                 }
             }
@@ -259,16 +273,48 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
                 c.m = m;
                 c.n = n;
             }
+            if (!done_split && bc && (l2r ? m > n : m < n)) {
+                // the canonical factor is on the long side: run the Jacobi on the
+                // short side (the other direction), then move the gauge with the
+                // subspace split started from that exact basis
+                Arena ar2(h);
+                SvdOut s0;
+                CT_TRY(ct_split_run(h, ar2, prec, th_opt.p, m, n, P->chi_max, P->eps_trunc, l2r ? 1 : 0,
+                                    mps_sites[i], mps_sites[i + 1], nullptr, h->d_scalars + SC_THETA_NSQ, &s0,
+                                    nullptr, 0));
+                if (s0.chi > 0) {
+                    Arena ar3(h);
+                    const int64_t c0 = s0.chi;
+                    double* basis = ar3.take<double>(c0 * (l2r ? n : m));
+                    if (!basis) return CT_ERR_OOM;
+                    CT_TRY(ct_basis_from_split(h, l2r ? 1 : 0, mps_sites[i], mps_sites[i + 1], m, n, c0, basis));
+                    SvdOut s1;
+                    bool ok = false;
+                    CT_TRY(ct_split_subspace(h, ar3, th_opt.p, m, n, c0, l2r ? 0 : 1, basis, bc->p,
+                                             mps_sites[i], mps_sites[i + 1], h->d_scalars + SC_THETA_NSQ, 0.0,
+                                             -1.0, 0, &s1, &ok));
+                    if (ok) {
+                        so = s0;
+                        done_split = true;
+                        st.exact_splits++;
+                        bc->len = l2r ? m : n;
+                        bc->c = c0;
+                        bc->disc = binding && so.sum_s2_all > 0.0 ? 1.0 - so.sum_s2_kept / so.sum_s2_all : -1.0;
+                    }
+                }
+            }
             if (!done_split) {
                 Arena ar2(h);
                 CT_TRY(ct_split_run(h, ar2, prec, th_opt.p, m, n, P->chi_max, P->eps_trunc, l2r ? 0 : 1,
                                     mps_sites[i], mps_sites[i + 1], nullptr, h->d_scalars + SC_THETA_NSQ, &so, qc,
                                     warm));
                 st.exact_splits++;
-                if (bc && so.chi == P->chi_max) {
+                if (bc && so.chi == c_sub) {
                     CT_TRY(ct_basis_from_split(h, l2r ? 0 : 1, mps_sites[i], mps_sites[i + 1], m, n, so.chi, bc->p));
                     bc->len = l2r ? m : n;
                     bc->c = so.chi;
+                    // a split that truncated nothing is no reference for the loss of one that does
+                    bc->disc = binding && so.sum_s2_all > 0.0 ? 1.0 - so.sum_s2_kept / so.sum_s2_all : -1.0;
                 }
             }
         }
@@ -306,6 +352,11 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         st.seconds_lanczos += ms * 1e-3;
         cudaEventElapsedTime(&ms, ev_s.a, ev_s.b);
         st.seconds_svd += ms * 1e-3;
+        if (P->verbose >= 2)
+            fprintf(stderr, "bond %d %s: %lld x %lld -> chi %lld, %s split %.3f ms\n", i, l2r ? "L->R" : "R->L",
+                    (long long)m, (long long)n, (long long)so.chi,
+                    last_split_subspace ? "subspace" : "exact",
+                    (double)ms);
         cudaEventElapsedTime(&ms, ev_e.a, ev_e.b);
         st.seconds_env += ms * 1e-3;
         st.heff_applies += hb.nk;

@@ -76,10 +76,13 @@ int ct_split_run(ct_handle* h, Arena& ar, int prec, const double* M, int64_t m, 
 size_t ct_split_subspace_ws_bytes(int64_t m, int64_t n, int64_t c);
 // mode 0 (left-to-right): basis_in = V rows (c x n) kept by the last right-to-left
 // split of the bond, basis_out <- Q rows (c x m); mode 1: basis_in = Q rows,
-// basis_out <- V rows.  *accepted = false: outputs are not valid, use the SVD.
+// basis_out <- V rows.  disc_ref: discarded weight at the previous truncating
+// visit of the bond (< 0: unknown).  *accepted = false: outputs are not valid,
+// use the SVD.
 int ct_split_subspace(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t c, int mode,
                       const double* basis_in, double* basis_out, double* Aout, double* Bout,
-                      const double* d_total, double eps_trunc, int power_steps, SvdOut* out, bool* accepted);
+                      const double* d_total, double eps_trunc, double disc_ref, int power_steps, SvdOut* out,
+                      bool* accepted);
 int ct_basis_from_split(ct_handle* h, int mode, const double* Aout, const double* Bout, int64_t m, int64_t n,
                         int64_t c, double* basis);
 

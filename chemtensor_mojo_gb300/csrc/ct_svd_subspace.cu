@@ -20,26 +20,34 @@
 // (optionally after power steps X <- orth(orth(X theta^T) theta)).
 //
 // orth() is CholeskyQR2 on row-normalised rows: G = Z Z^T, G = L L^T,
-// Z <- L^{-1} Z, twice.  It is triangular (Gram-Schmidt order), so rows that
-// start close to singular vectors ordered by weight stay ordered and close to
-// them; a symmetric orthogonalisation would keep any rotation between the
-// basis and the singular vectors and the next product X theta^T would become
-// ill-conditioned.  The first pass takes its Gram matrix and applies L^{-1} on
-// the tensor cores; the second pass is FP64 throughout, so the canonical factor
-// is orthonormal to FP64 rounding.
+// Z <- L^{-1} Z, twice, in FP64.  It is triangular (Gram-Schmidt order), so
+// rows that start close to singular vectors ordered by weight stay ordered and
+// close to them; a symmetric orthogonalisation would keep any rotation between
+// the basis and the singular vectors and the next product X theta^T would
+// become ill-conditioned.  The first pass must be FP64: a basis found by the
+// FP32 Jacobi carries strong directions into its weak rows at the FP32 level,
+// so rows of X theta^T for states near the cut are nearly parallel to the
+// strong ones (first-pass pivots ~1e-6 measured at chi = 128); Gram-Schmidt
+// in FP64 removes that, a TF32x3 Gram matrix cannot resolve it.
 //
-// The split is refused (the caller falls back to the Jacobi SVD) when a
-// Cholesky pivot of the first pass is small (a row of X theta^T nearly in the
-// span of the rows before it: the cached basis no longer tracks the subspace)
-// or when the discarded weight at chi_max is <= eps_trunc (then the rule may
-// keep fewer states and needs the spectrum).
+// The discarded weight is measured from the residual theta - A B (a
+// tensor-core GEMM; the residual is orthogonal to the kept part, so the
+// products' rounding enters only at second order).
+//
+// The split is refused (the caller falls back to the Jacobi SVD) when the
+// Cholesky factorisation breaks down, when the discarded weight exceeds
+// 4x that of the previous visit of the bond plus 1e-8 (the cached basis no
+// longer tracks the dominant subspace), or when it is <= eps_trunc (then the
+// rule may keep fewer states and needs the spectrum).
 #include "ct_ops.cuh"
 
 namespace {
 
 constexpr int CH_NB = 64;            // Cholesky block
 constexpr int FL_CHOL_FAIL = 100;    // d_flags slot: non-positive pivot seen
-constexpr double MIN_PIVOT = 0.25;   // squared share of a row outside the span of the rows before it
+// smallest accepted Cholesky pivot of a first pass (the squared share of a
+// normalised row outside the span of the rows before it)
+constexpr double MIN_PIVOT = 1e-12;
 
 __global__ void row_normalize_kernel(double* Y, int64_t rows, int64_t len) {
     const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
@@ -72,60 +80,65 @@ __global__ void chol_prepare_kernel(double* G, double* Linv, int64_t c, int64_t 
     }
 }
 
-// Cholesky of the diagonal block [k0, k0 + CH_NB) of G (lower triangle, trailing
-// updates already applied) and the inverse of that factor.  L goes back into
-// G's block (zeros above the diagonal), L^{-1} into Linv's block.  A pivot that
-// is not positive and finite is replaced by 1 and flagged; the smallest pivot
-// goes to *minpiv (bit pattern, atomicMin; pivots are >= 0 when recorded).
-__global__ void __launch_bounds__(256) chol_diag_kernel(double* G, double* Linv, int64_t ld, int64_t k0,
+// Cholesky of the CH_NB x CH_NB block at G (lower triangle, trailing updates
+// already applied) and the inverse of that factor, in FP64.  L
+// goes back into G's block (zeros above the diagonal), L^{-1} into Linv's
+// block.  A pivot that is not positive and finite is replaced by 1 and
+// flagged; the smallest pivot goes to *minpiv (bit pattern, atomicMin; pivots
+// are >= 0 when recorded).  256 threads: 8 warps own the rows of the update.
+__global__ void __launch_bounds__(256) chol_diag_kernel(double* G, double* Linv, int64_t ld,
                                                         unsigned long long* minpiv, int* fail) {
-    extern __shared__ double chol_smem[];   // two CH_NB x (CH_NB + 1) tiles
-    double(*A)[CH_NB + 1] = reinterpret_cast<double(*)[CH_NB + 1]>(chol_smem);
-    double(*X)[CH_NB + 1] = reinterpret_cast<double(*)[CH_NB + 1]>(chol_smem + CH_NB * (CH_NB + 1));
-    __shared__ double dj;
-    const int t = threadIdx.x;
+    using T = double;
+    extern __shared__ __align__(16) unsigned char chol_smem_raw[];   // two CH_NB x (CH_NB + 1) tiles
+    T(*A)[CH_NB + 1] = reinterpret_cast<T(*)[CH_NB + 1]>(chol_smem_raw);
+    T(*X)[CH_NB + 1] = reinterpret_cast<T(*)[CH_NB + 1]>(chol_smem_raw + sizeof(T) * CH_NB * (CH_NB + 1));
+    __shared__ T rinv;
+    __shared__ T dinv[CH_NB];
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     for (int e = t; e < CH_NB * CH_NB; e += blockDim.x) {
         const int i = e / CH_NB, j = e % CH_NB;
-        A[i][j] = (j <= i) ? G[(k0 + i) * ld + k0 + j] : 0.0;
+        A[i][j] = (j <= i) ? (T)G[i * ld + j] : (T)0;
+        X[i][j] = (T)0;
     }
     __syncthreads();
     double mp = 1.0e300;
     for (int j = 0; j < CH_NB; ++j) {
         if (t == 0) {
-            double p = A[j][j];
+            double p = (double)A[j][j];
             if (!(p > 0.0) || !isfinite(p)) {
                 *fail = 1;
                 p = 1.0;
             }
             mp = fmin(mp, p);
-            dj = sqrt(p);
+            const T dj = (T)sqrt(p);
             A[j][j] = dj;
+            rinv = (T)1 / dj;
+            dinv[j] = rinv;
         }
         __syncthreads();
-        for (int i = j + 1 + t; i < CH_NB; i += blockDim.x) A[i][j] /= dj;
+        for (int i = j + 1 + t; i < CH_NB; i += blockDim.x) A[i][j] *= rinv;
         __syncthreads();
-        const int r = CH_NB - j - 1;
-        for (int e = t; e < r * r; e += blockDim.x) {
-            const int i = j + 1 + e / r, l = j + 1 + e % r;
-            if (l <= i) A[i][l] = fma(-A[i][j], A[l][j], A[i][l]);
+        // rank-1 update of the trailing lower triangle: warp w takes rows j+1+w, +8, ...
+        for (int i = j + 1 + warp; i < CH_NB; i += 8) {
+            const T aij = A[i][j];
+            for (int l = j + 1 + lane; l <= i; l += 32) A[i][l] -= aij * A[l][j];
         }
         __syncthreads();
     }
     if (t == 0) atomicMin(minpiv, (unsigned long long)__double_as_longlong(mp));
-    // column t of L^{-1} by forward substitution
+    // column t of L^{-1} by forward substitution (the diagonal's reciprocals are kept)
     if (t < CH_NB) {
-        for (int i = 0; i < CH_NB; ++i) X[i][t] = 0.0;
         for (int i = t; i < CH_NB; ++i) {
-            double s = (i == t) ? 1.0 : 0.0;
-            for (int l = t; l < i; ++l) s = fma(-A[i][l], X[l][t], s);
-            X[i][t] = s / A[i][i];
+            T s = (i == t) ? (T)1 : (T)0;
+            for (int l = t; l < i; ++l) s -= A[i][l] * X[l][t];
+            X[i][t] = s * dinv[i];
         }
     }
     __syncthreads();
     for (int e = t; e < CH_NB * CH_NB; e += blockDim.x) {
         const int i = e / CH_NB, j = e % CH_NB;
-        G[(k0 + i) * ld + k0 + j] = A[i][j];
-        Linv[(k0 + i) * ld + k0 + j] = X[i][j];
+        G[i * ld + j] = (double)A[i][j];
+        Linv[i * ld + j] = (double)X[i][j];
     }
 }
 
@@ -154,95 +167,87 @@ GemmDesc gemm2d(int64_t M, int64_t N, int64_t K, const double* A, int64_t sAm, i
     return g;
 }
 
-// Blocked right-looking Cholesky of G (cp x cp, cp a multiple of CH_NB, lower
-// triangle meaningful) followed by the full inverse of the factor into Linv
-// by recursive doubling: inv([A 0; B C]) = [A^-1 0; -C^-1 B A^-1  C^-1].
-// P is scratch of cp * CH_NB doubles, T of cp * cp / 2 doubles.
-int chol_and_inverse(ct_handle* h, double* G, double* Linv, int64_t cp, double* P, double* T,
-                     unsigned long long* d_minpiv, int* d_fail) {
-    constexpr int smem = 2 * CH_NB * (CH_NB + 1) * (int)sizeof(double);
-    static int attr_dev = -1;
-    if (attr_dev != h->device) {
-        CT_CUDA(h, cudaFuncSetAttribute(chol_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        attr_dev = h->device;
-    }
-    for (int64_t k0 = 0; k0 < cp; k0 += CH_NB) {
-        chol_diag_kernel<<<1, 256, smem, h->stream>>>(G, Linv, cp, k0, d_minpiv, d_fail); ct_note_launch();
-        CT_LAUNCH_CHECK(h);
-        const int64_t r0 = k0 + CH_NB, rem = cp - r0;
-        if (rem <= 0) break;
-        // panel: L21 = G21 L11^{-T}
-        CT_TRY(ct_gemm_f64_launch(h, gemm2d(rem, CH_NB, CH_NB, G + r0 * cp + k0, cp, 1, Linv + k0 * cp + k0, 1, cp,
-                                            P, CH_NB, 1.0, 0.0)));
-        CT_CUDA(h, cudaMemcpy2DAsync(G + r0 * cp + k0, (size_t)cp * 8, P, (size_t)CH_NB * 8, (size_t)CH_NB * 8,
-                                     (size_t)rem, cudaMemcpyDeviceToDevice, h->stream));
-        // trailing: G22 -= L21 L21^T (lower tiles only; the upper triangle is never read)
-        GemmDesc gt = gemm2d(rem, rem, CH_NB, P, CH_NB, 1, P, 1, CH_NB, G + r0 * cp + r0, cp, -1.0, 1.0);
-        gt.tri = 1;
-        CT_TRY(ct_gemm_f64_launch(h, gt));
-    }
-    for (int64_t s = CH_NB; s < cp; s *= 2) {
-        // pairs (A at r0, C at r0 + s); full pairs are batched, a short last pair runs alone
-        const int64_t full = cp / (2 * s);
-        const int64_t tail_r0 = full * 2 * s;
-        const int64_t tail_b = (tail_r0 + s < cp) ? cp - tail_r0 - s : 0;
-        for (int part = 0; part < 2; ++part) {
-            const int64_t npairs = part == 0 ? full : (tail_b > 0 ? 1 : 0);
-            if (npairs == 0) continue;
-            const int64_t b = part == 0 ? s : tail_b;
-            const int64_t r0 = part == 0 ? 0 : tail_r0;
-            const int64_t step = 2 * s * (cp + 1);   // down the diagonal by 2s
-            // T = L[r0+s.., r0..] * Linv[r0.., r0..]     (b x s x s)
-            GemmDesc g1 = gemm2d(b, s, s, G + (r0 + s) * cp + r0, cp, 1, Linv + r0 * cp + r0, cp, 1, T, s, 1.0, 0.0);
-            g1.nb0 = npairs; g1.sA0 = step; g1.sB0 = step; g1.sC0 = b * s;
-            CT_TRY(ct_gemm_f64_launch(h, g1));
-            // Linv[r0+s.., r0..] = -Linv[r0+s.., r0+s..] * T   (b x s x b)
-            GemmDesc g2 = gemm2d(b, s, b, Linv + (r0 + s) * cp + r0 + s, cp, 1, T, s, 1, Linv + (r0 + s) * cp + r0,
-                                 cp, -1.0, 0.0);
-            g2.nb0 = npairs; g2.sA0 = step; g2.sB0 = b * s; g2.sC0 = step;
-            g2.tri = 2;
-            CT_TRY(ct_gemm_f64_launch(h, g2));
+// C = alpha A op(B) + beta C in FP64 for the factorisation (tri as in GemmDesc).
+int fac_gemm(ct_handle* h, int64_t M, int64_t N, int64_t K, const double* A, int64_t lda, const double* B,
+             int64_t ldb, int trans_b, double* C, int64_t ldc, double alpha, double beta, int tri) {
+    GemmDesc g = trans_b ? gemm2d(M, N, K, A, lda, 1, B, 1, ldb, C, ldc, alpha, beta)
+                         : gemm2d(M, N, K, A, lda, 1, B, ldb, 1, C, ldc, alpha, beta);
+    g.tri = tri;
+    return ct_gemm_f64_launch(h, g);
+}
+
+// Recursive Cholesky G = L L^T of the n x n block at G (leading dimension ld,
+// n a multiple of CH_NB; the upper triangle is not read) and the inverse of
+// the factor into Linv (its upper triangle must be zero):
+//   L11 = chol(G11);  L21 = G21 L11^{-T};  L22 = chol(G22 - L21 L21^T)
+//   inv(L) = [inv(L11) 0; -inv(L22) L21 inv(L11)  inv(L22)]
+// The large products run as whole FP64 GEMMs, the 64 x 64 leaves in one CTA.
+// S is scratch of (n/2)^2 doubles; it is free again whenever a recursive
+// call runs.
+int chol_inv(ct_handle* h, double* G, double* Linv, int64_t ld, int64_t n, double* S,
+             unsigned long long* d_minpiv, int* d_fail) {
+    if (n <= CH_NB) {
+        constexpr int smem = 2 * CH_NB * (CH_NB + 1) * (int)sizeof(double);
+        static int attr_dev = -1;
+        if (attr_dev != h->device) {
+            CT_CUDA(h, cudaFuncSetAttribute(chol_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            attr_dev = h->device;
         }
+        chol_diag_kernel<<<1, 256, smem, h->stream>>>(G, Linv, ld, d_minpiv, d_fail); ct_note_launch();
+        CT_LAUNCH_CHECK(h);
+        return CT_OK;
     }
+    const int64_t n1 = ct_round_up(n / 2, CH_NB), n2 = n - n1;
+    double* G21 = G + n1 * ld;
+    double* G22 = G21 + n1;
+    double* I21 = Linv + n1 * ld;
+    double* I22 = I21 + n1;
+    CT_TRY(chol_inv(h, G, Linv, ld, n1, S, d_minpiv, d_fail));
+    // L21 = G21 inv(L11)^T -> S -> G21
+    CT_TRY(fac_gemm(h, n2, n1, n1, G21, ld, Linv, ld, 1, S, n1, 1.0, 0.0, 0));
+    CT_CUDA(h, cudaMemcpy2DAsync(G21, (size_t)ld * 8, S, (size_t)n1 * 8, (size_t)n1 * 8, (size_t)n2,
+                                 cudaMemcpyDeviceToDevice, h->stream));
+    // G22 -= L21 L21^T (lower tiles only)
+    CT_TRY(fac_gemm(h, n2, n2, n1, G21, ld, G21, ld, 1, G22, ld, -1.0, 1.0, 1));
+    CT_TRY(chol_inv(h, G22, I22, ld, n2, S, d_minpiv, d_fail));
+    // inv(L)21 = -inv(L22) (L21 inv(L11))
+    CT_TRY(fac_gemm(h, n2, n1, n1, G21, ld, Linv, ld, 0, S, n1, 1.0, 0.0, 0));
+    CT_TRY(fac_gemm(h, n2, n1, n2, I22, ld, S, n1, 0, I21, ld, -1.0, 0.0, 2));
     return CT_OK;
 }
 
 struct OrthBufs {
     double* G;      // cp x cp
     double* Linv;   // cp x cp
-    double* P;      // cp x CH_NB
-    double* T;      // cp x cp / 2
+    double* S;      // (cp / 2)^2 + CH_NB^2
     int64_t cp;
 };
 
-// Orthonormalise the c rows of Z (c x len) by CholeskyQR2; the result is
-// written to W (c x len); Z is left row-normalised.  Pivots of the first pass
-// go to d_minpiv[0], of the second to d_minpiv[1].
+// Orthonormalise the c rows of Z (c x len) by CholeskyQR in FP64; the result
+// goes to W (c x len) and Z is scratch.  The optional second pass makes the rows
+// orthonormal to FP64 rounding.  Pivots of pass 1 go to d_minpiv[0], of pass 2
+// to d_minpiv[1].
 int orth_rows(ct_handle* h, Arena& ar, double* Z, double* W, int64_t c, int64_t len, const OrthBufs& ob,
-              unsigned long long* d_minpiv, int* d_fail) {
-    const size_t mark = ar.off;
+              bool two_pass, unsigned long long* d_minpiv, int* d_fail) {
     const int64_t cp = ob.cp;
     row_normalize_kernel<<<(unsigned)ct_cdiv(c * 32, 256), 256, 0, h->stream>>>(Z, c, len); ct_note_launch();
     CT_LAUNCH_CHECK(h);
-    // pass 1: Gram and L^{-1} Z on the tensor cores, factorisation in FP64
-    chol_prepare_kernel<<<grid_n(h, cp * cp), 256, 0, h->stream>>>(ob.G, ob.Linv, c, cp); ct_note_launch();
-    CT_LAUNCH_CHECK(h);
-    CT_TRY(ct_tc_gemm(h, ar, 0, 1, c, c, len, 1.0, Z, len, Z, len, 0.0, ob.G, cp));
-    ar.off = mark;
-    CT_TRY(chol_and_inverse(h, ob.G, ob.Linv, cp, ob.P, ob.T, d_minpiv, d_fail));
-    CT_TRY(ct_tc_gemm(h, ar, 0, 0, c, len, c, 1.0, ob.Linv, cp, Z, len, 0.0, W, len));
-    ar.off = mark;
-    // pass 2: FP64 throughout
-    chol_prepare_kernel<<<grid_n(h, cp * cp), 256, 0, h->stream>>>(ob.G, ob.Linv, c, cp); ct_note_launch();
-    CT_LAUNCH_CHECK(h);
-    GemmDesc gg = gemm2d(c, c, len, W, len, 1, W, 1, len, ob.G, cp, 1.0, 0.0);
-    gg.tri = 1;   // Cholesky reads the lower triangle only
-    CT_TRY(ct_gemm_f64_launch(h, gg));
-    CT_TRY(chol_and_inverse(h, ob.G, ob.Linv, cp, ob.P, ob.T, d_minpiv + 1, d_fail));
-    GemmDesc ga = gemm2d(c, len, c, ob.Linv, cp, 1, W, len, 1, Z, len, 1.0, 0.0);
-    ga.tri = 2;   // L^{-1} is lower triangular
-    CT_TRY(ct_gemm_f64_launch(h, ga));
-    CT_CUDA(h, cudaMemcpyAsync(W, Z, (size_t)(c * len) * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    double* src = Z;
+    double* dst = W;
+    for (int pass = 0; pass < (two_pass ? 2 : 1); ++pass) {
+        chol_prepare_kernel<<<grid_n(h, cp * cp), 256, 0, h->stream>>>(ob.G, ob.Linv, c, cp); ct_note_launch();
+        CT_LAUNCH_CHECK(h);
+        CT_TRY(fac_gemm(h, c, c, len, src, len, src, len, 1, ob.G, cp, 1.0, 0.0, 1));
+        CT_TRY(chol_inv(h, ob.G, ob.Linv, cp, cp, ob.S, d_minpiv + pass, d_fail));
+        CT_TRY(fac_gemm(h, c, len, c, ob.Linv, cp, src, len, 0, dst, len, 1.0, 0.0, 2));
+        double* t = src;
+        src = dst;
+        dst = t;
+    }
+    // the result is in src: W after one pass, Z after two
+    if (src != W)
+        CT_CUDA(h, cudaMemcpyAsync(W, src, (size_t)(c * len) * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    (void)ar;
     return CT_OK;
 }
 
@@ -251,55 +256,59 @@ int orth_rows(ct_handle* h, Arena& ar, double* Z, double* W, int64_t c, int64_t 
 size_t ct_split_subspace_ws_bytes(int64_t m, int64_t n, int64_t c) {
     const int64_t big = m > n ? m : n;
     const int64_t cp = ct_round_up(c, CH_NB);
-    size_t b = 2 * ct_bytes(c * big, 8) + 2 * ct_bytes(cp * cp, 8) + ct_bytes(cp * CH_NB, 8) +
-               ct_bytes(cp * cp / 2 + CH_NB * CH_NB, 8) + 4096;
+    size_t b = 2 * ct_bytes(c * big, 8) + 2 * ct_bytes(cp * cp, 8) + ct_bytes(cp * cp / 4 + CH_NB * CH_NB, 8) +
+               ct_bytes(m * n, 8) + 4096;
     size_t g = ct_tc_gemm_ws_bytes(c, big, big);
-    const size_t g2 = ct_tc_gemm_ws_bytes(c, c, big);
-    const size_t g3 = ct_tc_gemm_ws_bytes(big, c, big);
-    const size_t g4 = ct_tc_gemm_ws_bytes(c, big, c);
-    if (g2 > g) g = g2;
-    if (g3 > g) g = g3;
-    if (g4 > g) g = g4;
+    const size_t more[] = {ct_tc_gemm_ws_bytes(c, c, big), ct_tc_gemm_ws_bytes(big, c, big),
+                           ct_tc_gemm_ws_bytes(c, big, c), ct_tc_gemm_ws_bytes(m, n, c),
+                           ct_tc_gemm_ws_bytes(cp, cp, cp)};
+    for (size_t x : more)
+        if (x > g) g = x;
     return b + g;
 }
 
-int ct_split_subspace(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t c, int mode,
-                      const double* basis_in, double* basis_out, double* Aout, double* Bout, const double* d_total,
-                      double eps_trunc, int power_steps, SvdOut* out, bool* accepted) {
-    *accepted = false;
-    const int64_t big = m > n ? m : n;
-    OrthBufs ob{};
-    ob.cp = ct_round_up(c, CH_NB);
-    double* Z = ar.take<double>(c * big);
-    double* W = ar.take<double>(c * big);
-    ob.G = ar.take<double>(ob.cp * ob.cp);
-    ob.Linv = ar.take<double>(ob.cp * ob.cp);
-    ob.P = ar.take<double>(ob.cp * CH_NB);
-    ob.T = ar.take<double>(ob.cp * ob.cp / 2 + CH_NB * CH_NB);
-    if (!Z || !W || !ob.G || !ob.Linv || !ob.P || !ob.T) return CT_ERR_OOM;
+namespace {
+
+enum SplitVerdict { SPLIT_OK, SPLIT_BREAKDOWN, SPLIT_STALE, SPLIT_EPS };
+
+struct SplitBufs {
+    double* Z;
+    double* W;
+    double* R;
+    OrthBufs ob;
+};
+
+// The warm split (products with theta on the tensor cores, orthonormalisation in FP64).
+int split_attempt(ct_handle* h, Arena& ar, const SplitBufs& sb, const double* M, int64_t m, int64_t n, int64_t c,
+                  int mode, const double* basis_in, double* basis_out, double* Aout, double* Bout,
+                  const double* d_total, double eps_trunc, double disc_ref, int power_steps, SvdOut* out,
+                  SplitVerdict* verdict) {
     const size_t mark = ar.off;
+    double* Z = sb.Z;
+    double* W = sb.W;
+    const OrthBufs& ob = sb.ob;
     unsigned long long* d_piv = (unsigned long long*)(h->d_scalars + SC_SPLIT_PIV);   // [0] pass 1, [1] pass 2
     int* d_fail = h->d_flags + FL_CHOL_FAIL;
     split_flags_init_kernel<<<1, 32, 0, h->stream>>>(d_piv, d_fail); ct_note_launch();
     CT_LAUNCH_CHECK(h);
-
-    // X: c rows over n (left-to-right) or over m (right-to-left)
+    // X: c rows over n (left-to-right) or over m (right-to-left).  The power
+    // steps' intermediate bases need no second pass.
     const double* X = basis_in;
     for (int it = 0; it < power_steps; ++it) {
         if (mode == 0) {
             CT_TRY(ct_tc_gemm(h, ar, 0, 1, c, m, n, 1.0, X, n, M, n, 0.0, Z, m));   // X theta^T
             ar.off = mark;
-            CT_TRY(orth_rows(h, ar, Z, W, c, m, ob, d_piv, d_fail));
+            CT_TRY(orth_rows(h, ar, Z, W, c, m, ob, false, d_piv, d_fail));
             CT_TRY(ct_tc_gemm(h, ar, 0, 0, c, n, m, 1.0, W, m, M, n, 0.0, Z, n));   // . theta
             ar.off = mark;
-            CT_TRY(orth_rows(h, ar, Z, W, c, n, ob, d_piv, d_fail));
+            CT_TRY(orth_rows(h, ar, Z, W, c, n, ob, false, d_piv, d_fail));
         } else {
             CT_TRY(ct_tc_gemm(h, ar, 0, 0, c, n, m, 1.0, X, m, M, n, 0.0, Z, n));   // X theta
             ar.off = mark;
-            CT_TRY(orth_rows(h, ar, Z, W, c, n, ob, d_piv, d_fail));
+            CT_TRY(orth_rows(h, ar, Z, W, c, n, ob, false, d_piv, d_fail));
             CT_TRY(ct_tc_gemm(h, ar, 0, 1, c, m, n, 1.0, W, n, M, n, 0.0, Z, m));   // . theta^T
             ar.off = mark;
-            CT_TRY(orth_rows(h, ar, Z, W, c, m, ob, d_piv, d_fail));
+            CT_TRY(orth_rows(h, ar, Z, W, c, m, ob, false, d_piv, d_fail));
         }
         X = W;
     }
@@ -307,23 +316,26 @@ int ct_split_subspace(ct_handle* h, Arena& ar, const double* M, int64_t m, int64
         // Q = orth(X theta^T) -> basis_out; A = Q^T; B = Q theta
         CT_TRY(ct_tc_gemm(h, ar, 0, 1, c, m, n, 1.0, X, n, M, n, 0.0, Z, m));
         ar.off = mark;
-        CT_TRY(orth_rows(h, ar, Z, basis_out, c, m, ob, d_piv, d_fail));
+        CT_TRY(orth_rows(h, ar, Z, basis_out, c, m, ob, true, d_piv, d_fail));
         CT_TRY(ct_tc_gemm(h, ar, 0, 0, c, n, m, 1.0, basis_out, m, M, n, 0.0, Bout, n));
         ar.off = mark;
         transpose_copy_kernel<<<grid_n(h, c * m), 256, 0, h->stream>>>(basis_out, c, m, Aout); ct_note_launch();
         CT_LAUNCH_CHECK(h);
-        CT_TRY(ct_reduce_nrm2sq(h, c * n, Bout, h->d_scalars + SC_TMP1, nullptr));
     } else {
         // V = orth(X theta) -> B and basis_out; A = theta V^T
         CT_TRY(ct_tc_gemm(h, ar, 0, 0, c, n, m, 1.0, X, m, M, n, 0.0, Z, n));
         ar.off = mark;
-        CT_TRY(orth_rows(h, ar, Z, Bout, c, n, ob, d_piv, d_fail));
+        CT_TRY(orth_rows(h, ar, Z, Bout, c, n, ob, true, d_piv, d_fail));
         CT_CUDA(h, cudaMemcpyAsync(basis_out, Bout, (size_t)(c * n) * sizeof(double), cudaMemcpyDeviceToDevice,
                                    h->stream));
         CT_TRY(ct_tc_gemm(h, ar, 0, 1, m, c, n, 1.0, M, n, Bout, n, 0.0, Aout, c));
         ar.off = mark;
-        CT_TRY(ct_reduce_nrm2sq(h, m * c, Aout, h->d_scalars + SC_TMP1, nullptr));
     }
+    // discarded weight |theta - A B|^2
+    CT_CUDA(h, cudaMemcpyAsync(sb.R, M, (size_t)(m * n) * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    CT_TRY(ct_tc_gemm(h, ar, 0, 0, m, n, c, -1.0, Aout, c, Bout, n, 1.0, sb.R, n));
+    ar.off = mark;
+    CT_TRY(ct_reduce_nrm2sq(h, m * n, sb.R, h->d_scalars + SC_TMP1, nullptr));
     double host[2];
     unsigned long long piv[2];
     int fail = 0;
@@ -335,18 +347,47 @@ int ct_split_subspace(ct_handle* h, Arena& ar, const double* M, int64_t m, int64
     double piv1, piv2;
     memcpy(&piv1, &piv[0], 8);
     memcpy(&piv2, &piv[1], 8);
-    const double total = host[0], kept = host[1];
-    const double disc = (total > 0.0) ? (total - kept) / total : 0.0;
+    const double total = host[0], resid = host[1];
+    const double disc = (total > 0.0) ? resid / total : 0.0;
     out->chi = c;
     out->sum_s2_all = total;
-    out->sum_s2_kept = kept;
+    out->sum_s2_kept = total - resid;
     out->min_pivot = piv1;
     out->min_pivot2 = piv2;
     out->chol_fail = fail;
-    if (fail || !(piv1 >= MIN_PIVOT) || !(piv2 > 0.5)) return CT_OK;
-    // eps binds: the rule may keep fewer than chi_max states
-    if (eps_trunc > 0.0 && disc <= eps_trunc) return CT_OK;
-    *accepted = true;
+    if (fail || !(piv1 >= MIN_PIVOT) || !(piv2 > 0.5)) {
+        *verdict = SPLIT_BREAKDOWN;
+    } else if (disc_ref >= 0.0 && disc > 4.0 * disc_ref + 1e-8) {
+        *verdict = SPLIT_STALE;   // much more weight lost than at the previous visit of the bond
+    } else if (eps_trunc > 0.0 && disc <= eps_trunc) {
+        *verdict = SPLIT_EPS;     // eps binds: the rule may keep fewer states
+    } else {
+        *verdict = SPLIT_OK;
+    }
+    return CT_OK;
+}
+
+}  // namespace
+
+int ct_split_subspace(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t c, int mode,
+                      const double* basis_in, double* basis_out, double* Aout, double* Bout,
+                      const double* d_total, double eps_trunc, double disc_ref, int power_steps, SvdOut* out,
+                      bool* accepted) {
+    *accepted = false;
+    const int64_t big = m > n ? m : n;
+    SplitBufs sb{};
+    sb.ob.cp = ct_round_up(c, CH_NB);
+    sb.Z = ar.take<double>(c * big);
+    sb.W = ar.take<double>(c * big);
+    sb.ob.G = ar.take<double>(sb.ob.cp * sb.ob.cp);
+    sb.ob.Linv = ar.take<double>(sb.ob.cp * sb.ob.cp);
+    sb.ob.S = ar.take<double>(sb.ob.cp * sb.ob.cp / 4 + CH_NB * CH_NB);
+    sb.R = ar.take<double>(m * n);
+    if (!sb.Z || !sb.W || !sb.ob.G || !sb.ob.Linv || !sb.ob.S || !sb.R) return CT_ERR_OOM;
+    SplitVerdict v = SPLIT_BREAKDOWN;
+    CT_TRY(split_attempt(h, ar, sb, M, m, n, c, mode, basis_in, basis_out, Aout, Bout, d_total, eps_trunc,
+                         disc_ref, power_steps, out, &v));
+    *accepted = (v == SPLIT_OK);
     return CT_OK;
 }
 

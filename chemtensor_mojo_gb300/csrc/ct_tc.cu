@@ -133,9 +133,14 @@ __device__ __forceinline__ float tf32_rne(float x) {
     return __uint_as_float(u);
 }
 
-__device__ __forceinline__ void split_tf32(double x, float& hi, float& lo) {
-    hi = tf32_rne((float)x);
-    lo = tf32_rne((float)(x - (double)hi));
+// x = hi + lo with both halves TF32-representable.  All in FP32: x - hi is
+// exact in FP32, and lo keeps 11 significant bits, so rounding an FP64 value to
+// FP32 first loses nothing that the pair could hold.  (FP64 arithmetic issues
+// at a small fraction of the FP32 rate on this part; the packers stay clear
+// of it apart from the one conversion.)
+__device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
+    hi = tf32_rne(x);
+    lo = tf32_rne(x - hi);
 }
 
 // ---------------------------------------------------------------------------
@@ -516,8 +521,9 @@ __global__ void __launch_bounds__(256) pack_split_kernel(PackDesc p, const int* 
         }
         koff[tx] = o;
     }
-    double sc = p.scale;
-    if (p.scale_ptr) sc *= *p.scale_ptr;
+    double scd = p.scale;
+    if (p.scale_ptr) scd *= *p.scale_ptr;
+    const float sc = (float)scd;
     __syncthreads();
     for (int i = ty; i < 32; i += 8) {
         const int ri = K_FAST ? i : tx, ki = K_FAST ? tx : i;
@@ -531,7 +537,7 @@ __global__ void __launch_bounds__(256) pack_split_kernel(PackDesc p, const int* 
         const int64_t r = rb + i, k = kb + tx;
         if (r < p.rows && k < p.ldk) {
             float h, l;
-            split_tf32(tile[i][tx] * sc, h, l);
+            split_tf32((float)tile[i][tx] * sc, h, l);
             p.hi[r * p.ldk + k] = h;
             p.lo[r * p.ldk + k] = l;
         }
@@ -586,7 +592,7 @@ __global__ void __launch_bounds__(MPOT_NT) mpo_tc_kernel(MpoTcDesc m, int64_t jc
             if (jj >= nj) break;
             const int64_t off = obase + joff[j0 + jj];
             float h, l;
-            split_tf32((double)acc[jj], h, l);
+            split_tf32(acc[jj], h, l);
             m.hi[off] = h;
             m.lo[off] = l;
         }

@@ -45,13 +45,14 @@ class DMRGParams:
     reorth: bool = False
     final_rayleigh: bool = False
     keep_bases: bool = False
+    split_power_steps: int = 0   # -1: always the Jacobi SVD split
 
     def to_c(self) -> _lib.ct_dmrg_params:
         return _lib.ct_dmrg_params(int(self.num_sweeps), int(self.chi_max), float(self.eps_trunc),
                                    int(self.max_krylov_iter), float(self.krylov_tol), float(self.energy_tol),
                                    int(bool(self.two_site)), int(self.verbose), _lib.PRECISIONS[self.prec],
                                    int(self.max_rotations), int(bool(self.reorth)), int(bool(self.final_rayleigh)),
-                                   int(bool(self.keep_bases)))
+                                   int(bool(self.keep_bases)), int(self.split_power_steps))
 
 
 @dataclass

@@ -158,6 +158,10 @@ typedef struct ct_dmrg_params {
                             on this handle.  Only valid when the MPS passed in
                             is the one that call returned and the MPO is the
                             same; 0 forgets them at the start of the call.     */
+    int split_power_steps; /* mixed form, bonds where chi_max binds: power steps
+                            of the warm-started subspace split (0 is enough
+                            for |dE/E| <= 1e-9 on the benchmark chain); -1
+                            always runs the Jacobi SVD instead                */
 } ct_dmrg_params;
 
 typedef struct ct_dmrg_stats {
@@ -220,6 +224,25 @@ CT_API int ct_energy_grad(ct_handle* h, int prec, int nsites, int d, const int64
                    const double* const* mpo_sites, const int64_t* bond_dims,
                    const double* const* mps_sites, double* const* grad_sites,
                    int checkpoint_every, double* energy_host);
+
+/* Warm-started split of theta[Dl,d,d,Dr] into exactly chi states, the mixed
+ * form's replacement of ct_svd_split on bonds where chi_max binds (no
+ * reference counterpart: the reference always runs a full SVD).  basis_in
+ * holds chi orthonormal rows kept by the previous visit of the bond from the
+ * other direction: rows over (s_{i+1}, a_{i+1}) (chi x d*Dr) for a
+ * left-to-right split, over (a_{i-1}, s_i) (chi x Dl*d) for a right-to-left
+ * one.  power_steps >= 0 refines the basis before the split.
+ * Writes A [Dl,d,chi], B [chi,d,Dr] (A left-canonical for
+ * left_to_right, B right-canonical otherwise) and the basis this split keeps
+ * (chi x Dl*d, resp. chi x d*Dr) to basis_out.  *accepted = 0 when the
+ * basis no longer tracks theta's dominant subspace (outputs not valid: use
+ * ct_svd_split).  pivots_host (3 doubles, may be NULL): the smallest Cholesky
+ * pivot of each CholeskyQR pass and a failure flag.  Requires the tensor
+ * cores (CT_ERR_UNSUPPORTED otherwise).                                     */
+CT_API int ct_svd_split_warm(ct_handle* h, const double* theta, int64_t Dl, int64_t d, int64_t Dr, int64_t chi,
+                             int left_to_right, const double* basis_in, int power_steps,
+                             double* basis_out, double* A_out, double* B_out, int* accepted,
+                             double* discarded_host, double* pivots_host);
 
 /* ---- allocation-free H_eff apply (no counterpart in the reference) --------
  * For callers that cannot let a library allocate device memory, e.g. a Mojo/MAX
