@@ -394,11 +394,15 @@ def main():
     launches = _lib.launch_count() - launches0
     clocks.stop()
     kt = None
+    kt_heff = None
     if kt_on:
-        n_kt, ms_kt, fl_kt = C.c_int64(), C.c_double(), C.c_double()
-        ctx.call("ct_kernel_timing_read", C.byref(n_kt), C.byref(ms_kt), C.byref(fl_kt))
+        def read_class(cls):
+            n_kt, ms_kt, fl_kt = C.c_int64(), C.c_double(), C.c_double()
+            ctx.call("ct_kernel_timing_read_class", cls, C.byref(n_kt), C.byref(ms_kt), C.byref(fl_kt))
+            return {"launches": n_kt.value, "ms": ms_kt.value, "flops": fl_kt.value}
+        kt = read_class(0)        # every TF32x3 GEMM launch
+        kt_heff = read_class(1)   # every whole H_eff apply inside Lanczos
         ctx.call("ct_kernel_timing", 0)
-        kt = {"launches": n_kt.value, "ms": ms_kt.value, "flops": fl_kt.value}
     if dist is not None:
         dist.barrier()
     K = max(args.steps, 1)
@@ -442,7 +446,8 @@ def main():
         "energy": energy_rq, "energy_lanczos": Ec.value, "sweep_energies_lanczos": list(sweeps_e)[:done.value],
         "bond_dims_final": final_dims,
         "heff_tflops": heff_tflops, "heff_applies": stats.heff_applies, "local_updates": stats.local_updates,
-        "phase_seconds": {"lanczos": stats.seconds_lanczos, "svd": stats.seconds_svd, "env": stats.seconds_env,
+        "phase_seconds": {"lanczos": stats.seconds_lanczos, "svd": stats.seconds_svd,
+                          "svd_subspace": stats.seconds_subspace, "env": stats.seconds_env,
                           "total_wall": stats.seconds_total},
         "max_discarded": stats.max_discarded, "warmup_log": warm_log,
         "splits": {"subspace": stats.subspace_splits, "exact": stats.exact_splits},
@@ -450,6 +455,7 @@ def main():
                 "d2h_bytes_per_step": d2h // K,
                 "wall_s": t_wall},
         "gpu_launches": launches,
+        "launches_before_timed": launches0,
         "clocks": clocks.summary(),
     }
     line.update(extras)
@@ -466,6 +472,22 @@ def main():
                             "peak_note": f"{peak_src} bf16 {bf16} TFLOP/s / 2 (TF32 rate) / 3 (3 MMAs per product)",
                             "traffic_note": "DRAM read+write bytes of one centre-bond H_eff GEMM "
                                             "(5120x4096x1024) from an ncu capture, per launch"}
+    if kt_heff and kt_heff["launches"] > 0:
+        # CUDA-event breakdown of the timed sweeps (device seconds, summed over both sweeps)
+        heff_s = kt_heff["ms"] * 1e-3
+        gemm_s = kt["ms"] * 1e-3 if kt else 0.0
+        line["breakdown"] = {
+            "timed_region_s": dev_s,
+            "heff_apply_s": heff_s, "heff_apply_count": kt_heff["launches"],
+            "heff_apply_tflops": kt_heff["flops"] / max(heff_s, 1e-12) / 1e12,
+            "tc_gemm_s_all": gemm_s,
+            "lanczos_other_s": stats.seconds_lanczos - heff_s,
+            "split_subspace_s": stats.seconds_subspace,
+            "split_exact_s": stats.seconds_svd - stats.seconds_subspace,
+            "env_s": stats.seconds_env,
+            "note": "lanczos_other = Krylov vector kernels, eigensolve, Ritz vector; tc_gemm_s_all counts the "
+                    "GEMMs of H_eff, environments and splits",
+        }
     if "cpu_sweep_s" in extras:
         line["cpu_baseline"] = {"value": extras["cpu_sweep_s"], "unit": "s/sweep", "cores": os.cpu_count(),
                                 "kind": "port", "sample": extras["cpu_sample"]}

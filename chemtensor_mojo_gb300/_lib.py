@@ -50,7 +50,8 @@ class ct_dmrg_stats(C.Structure):
     _fields_ = [("seconds_total", C.c_double), ("seconds_lanczos", C.c_double), ("seconds_svd", C.c_double),
                 ("seconds_env", C.c_double), ("heff_flops", C.c_double), ("env_flops", C.c_double),
                 ("heff_applies", C.c_int64), ("local_updates", C.c_int64), ("max_discarded", C.c_double),
-                ("energy_rayleigh", C.c_double), ("subspace_splits", C.c_int64), ("exact_splits", C.c_int64)]
+                ("energy_rayleigh", C.c_double), ("subspace_splits", C.c_int64), ("exact_splits", C.c_int64),
+                ("seconds_subspace", C.c_double)]
 
 
 P = C.c_void_p
@@ -97,6 +98,7 @@ SIGNATURES = {
                           C.POINTER(D)],
     "ct_kernel_timing": [P, I32],
     "ct_kernel_timing_read": [P, C.POINTER(I64), C.POINTER(D), C.POINTER(D)],
+    "ct_kernel_timing_read_class": [P, I32, C.POINTER(I64), C.POINTER(D), C.POINTER(D)],
     "ct_heff2_apply_noalloc": [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, I64],
     "ct_energy_grad": [P, I32, I32, I32, C.POINTER(I64), PP, C.POINTER(I64), PP, PP, I32, C.POINTER(D)],
 }

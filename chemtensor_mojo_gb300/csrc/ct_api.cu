@@ -338,6 +338,7 @@ int ct_theta2(ct_handle* h, int prec, const double* A_i, const double* A_ip1, do
     CT_POSCHK(h, d);
     CT_POSCHK(h, Dm);
     CT_POSCHK(h, Dr);
+    CT_TRY(ct_reserve(h, ct_theta_ws_bytes(prec, Dl, d, Dm, Dr)));
     return ct_theta_run(h, prec, A_i, A_ip1, theta, Dl, d, Dm, Dr);
 }
 
@@ -533,4 +534,83 @@ int ct_svd_split_warm(ct_handle* h, const double* theta, int64_t Dl, int64_t d, 
     return CT_OK;
 }
 
+int ct_kernel_timing(ct_handle* h, int enable) {
+    CT_NULLCHK(h, h);
+    CT_TRY(ct_ktime_harvest(h));
+    h->ktime_on = enable != 0;
+    h->ktime_open = 0;
+    h->ktime_dropped = 0;
+    for (int c = 0; c < KT_NCLASSES; ++c) {
+        h->ktime_count[c] = 0;
+        h->ktime_ms[c] = 0.0;
+        h->ktime_flops[c] = 0.0;
+    }
+    return CT_OK;
+}
+
+int ct_kernel_timing_read_class(ct_handle* h, int cls, int64_t* count, double* ms, double* flops) {
+    CT_NULLCHK(h, h);
+    if (!count || !ms || !flops || cls < 0 || cls >= KT_NCLASSES) return CT_ERR_INVALID;
+    CT_TRY(ct_ktime_harvest(h));
+    *count = h->ktime_count[cls];
+    *ms = h->ktime_ms[cls];
+    *flops = h->ktime_flops[cls];
+    return CT_OK;
+}
+
+int ct_kernel_timing_read(ct_handle* h, int64_t* launches, double* ms, double* flops) {
+    return ct_kernel_timing_read_class(h, KT_TC_GEMM, launches, ms, flops);
+}
+
 }  // extern "C"
+
+namespace {
+constexpr int KTIME_SLOTS = 16384;
+}
+
+// Sum the elapsed times of the pending event pairs per class (waits for the last one).
+int ct_ktime_harvest(ct_handle* h) {
+    if (h->ktime_pending == 0 || h->ktime_open > 0) return CT_OK;
+    CT_CUDA(h, cudaEventSynchronize(h->ktime_ev[2 * (h->ktime_pending - 1) + 1]));
+    for (int i = 0; i < h->ktime_pending; ++i) {
+        float ms = 0.f;
+        CT_CUDA(h, cudaEventElapsedTime(&ms, h->ktime_ev[2 * i], h->ktime_ev[2 * i + 1]));
+        const int c = h->ktime_slot_cls[i];
+        h->ktime_ms[c] += ms;
+        h->ktime_flops[c] += h->ktime_slot_flops[i];
+        h->ktime_count[c] += 1;
+    }
+    h->ktime_pending = 0;
+    return CT_OK;
+}
+
+int ct_ktime_begin(ct_handle* h, int cls, double flops, int* slot) {
+    *slot = -1;
+    if (!h->ktime_on) return CT_OK;
+    if (h->ktime_ev.empty()) {
+        h->ktime_ev.resize(2 * KTIME_SLOTS, nullptr);
+        h->ktime_slot_flops.resize(KTIME_SLOTS, 0.0);
+        h->ktime_slot_cls.resize(KTIME_SLOTS, 0);
+        for (auto& e : h->ktime_ev) CT_CUDA(h, cudaEventCreate(&e));
+    }
+    // read the pool back before it fills, at a moment with no open region (a
+    // region nests only a few others, so 64 spare slots are enough)
+    if (h->ktime_pending >= KTIME_SLOTS - 64 && h->ktime_open == 0) CT_TRY(ct_ktime_harvest(h));
+    if (h->ktime_pending == KTIME_SLOTS) {
+        h->ktime_dropped++;
+        return CT_OK;
+    }
+    *slot = h->ktime_pending++;
+    h->ktime_open++;
+    h->ktime_slot_flops[*slot] = flops;
+    h->ktime_slot_cls[*slot] = cls;
+    CT_CUDA(h, cudaEventRecord(h->ktime_ev[2 * *slot], h->stream));
+    return CT_OK;
+}
+
+int ct_ktime_end(ct_handle* h, int slot) {
+    if (slot < 0) return CT_OK;
+    h->ktime_open--;
+    CT_CUDA(h, cudaEventRecord(h->ktime_ev[2 * slot + 1], h->stream));
+    return CT_OK;
+}

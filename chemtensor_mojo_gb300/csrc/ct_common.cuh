@@ -45,15 +45,25 @@ struct ct_handle {
     // tensor-core path state
     bool tc_checked = false;
     bool tc_ok = false;
-    // optional live timing of every tensor-core GEMM launch: an event pair per
-    // launch on the handle's stream, read back when the pool fills or on request
+    // optional live timing (ct_kernel_timing): an event pair per timed region on
+    // the handle's stream, summed per class when the pool fills or on request
     bool ktime_on = false;
     std::vector<cudaEvent_t> ktime_ev;   // 2 per slot
     std::vector<double> ktime_slot_flops;
+    std::vector<int> ktime_slot_cls;
     int ktime_pending = 0;
-    int64_t ktime_launches = 0;
-    double ktime_ms = 0.0, ktime_flops = 0.0;
+    int ktime_open = 0;              // regions begun and not yet ended
+    int64_t ktime_dropped = 0;       // regions not timed: pool full while a region was open
+    int64_t ktime_count[4] = {0, 0, 0, 0};
+    double ktime_ms[4] = {0, 0, 0, 0}, ktime_flops[4] = {0, 0, 0, 0};
 };
+
+// live timing classes
+enum { KT_TC_GEMM = 0, KT_HEFF_APPLY = 1, KT_NCLASSES = 4 };
+// start a timed region of class cls (slot = -1 when timing is off); end it after the launches
+int ct_ktime_begin(ct_handle* h, int cls, double flops, int* slot);
+int ct_ktime_end(ct_handle* h, int slot);
+int ct_ktime_harvest(ct_handle* h);
 
 enum { CT_NSCALARS = 1024, CT_NPARTIALS = 8192, CT_NFLAGS = 256, CT_MAX_KRYLOV_SLOTS = 128 };
 

@@ -166,14 +166,17 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         const int64_t wL = mpo_dims[i], wM = mpo_dims[i + 1], wR = mpo_dims[i + 2];
         const int64_t m = Dl * d, n = d * Dr;
         size_t need = ct_lanczos_ws_bytes(prec, Dl, d, Dr, wL, wM, wR, P->max_krylov_iter);
+        need = std::max(need, ct_theta_ws_bytes(prec, Dl, d, Dm, Dr));
         need = std::max(need, ct_split_ws_bytes(prec, m, n, P->chi_max, l2r ? 0 : 1));
-        // mixed form, large bonds: where chi_max binds, the warm subspace split
-        // when the other direction kept a basis of this bond; the bases are kept
-        // on every large bond, so a bond that starts binding has one
+        // mixed form, large bonds: the warm subspace split when the other
+        // direction kept a basis of this bond -- where chi_max binds, and with
+        // eps_trunc = 0 also where every state is kept (then any orthonormal
+        // basis of the whole space will do); the bases are kept on every large
+        // bond, so a bond that starts binding has one
         const bool mixed_large = (prec == CT_PREC_TF32X3) && P->split_power_steps >= 0 &&
                                  !ct_svd_is_small(m, n, l2r ? 0 : 1);
         const bool binding = (int64_t)P->chi_max < std::min(m, n);
-        const bool use_subspace = mixed_large && binding;
+        const bool use_subspace = mixed_large && (binding || P->eps_trunc <= 0.0);
         const int64_t c_sub = std::min<int64_t>(P->chi_max, std::min(m, n));
         if (mixed_large) {
             need = std::max(need, ct_split_subspace_ws_bytes(m, n, c_sub));
@@ -252,7 +255,7 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
                         st.subspace_splits++;
                         own.len = own_len;
                         own.c = c;
-                        own.disc = so.sum_s2_all > 0.0 ? 1.0 - so.sum_s2_kept / so.sum_s2_all : 0.0;
+                        own.disc = binding && so.sum_s2_all > 0.0 ? 1.0 - so.sum_s2_kept / so.sum_s2_all : -1.0;
                     }
                 }
             }
@@ -352,6 +355,7 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         st.seconds_lanczos += ms * 1e-3;
         cudaEventElapsedTime(&ms, ev_s.a, ev_s.b);
         st.seconds_svd += ms * 1e-3;
+        if (last_split_subspace) st.seconds_subspace += ms * 1e-3;
         if (P->verbose >= 2)
             fprintf(stderr, "bond %d %s: %lld x %lld -> chi %lld, %s split %.3f ms\n", i, l2r ? "L->R" : "R->L",
                     (long long)m, (long long)n, (long long)so.chi,

@@ -12,13 +12,19 @@
 
 namespace {
 
-constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
+constexpr int BK = 16;
 
-template <bool A_K_CONTIG, bool B_N_CONTIG>
-__global__ void __launch_bounds__(NT) gemm_f64_kernel(GemmDesc g) {
+// One CTA computes a TBM x TBN tile of C with (TBM/4) x (TBN/4) threads, each
+// holding a 4 x 4 register block.  The 64 x 64 tile is the default; the
+// 32 x 32 tile gives small problems (the factorisation's panels) enough CTAs
+// to occupy every SM's FP64 pipe.
+template <int TBM, int TBN, bool A_K_CONTIG, bool B_N_CONTIG>
+__global__ void __launch_bounds__((TBM / 4) * (TBN / 4)) gemm_f64_kernel(GemmDesc g) {
+    constexpr int NT = (TBM / 4) * (TBN / 4);
+    constexpr int TX = TBN / 4;
     if (ct_skip(g.skip)) return;
-    __shared__ double As[BK][BM + 1];
-    __shared__ double Bs[BK][BN + 1];
+    __shared__ double As[BK][TBM + 1];
+    __shared__ double Bs[BK][TBN + 1];
 
     const int64_t bz = blockIdx.z;
     const int64_t b1 = bz / g.nb0, b0 = bz % g.nb0;
@@ -26,10 +32,10 @@ __global__ void __launch_bounds__(NT) gemm_f64_kernel(GemmDesc g) {
     const double* B = g.B + b1 * g.sB1 + b0 * g.sB0;
     double* C = g.C + b1 * g.sC1 + b0 * g.sC0;
 
-    const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    if (g.tri == 1 && n0 >= m0 + BM) return;   // tile strictly above the diagonal
-    const int64_t kend = (g.tri == 2 && m0 + BM < g.K) ? m0 + BM : g.K;
+    const int64_t m0 = (int64_t)blockIdx.y * TBM, n0 = (int64_t)blockIdx.x * TBN;
+    const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
+    if (g.tri == 1 && n0 >= m0 + TBM) return;   // tile strictly above the diagonal
+    const int64_t kend = (g.tri == 2 && m0 + TBM < g.K) ? m0 + TBM : g.K;
 
     double acc[4][4];
 #pragma unroll
@@ -39,19 +45,19 @@ __global__ void __launch_bounds__(NT) gemm_f64_kernel(GemmDesc g) {
 
     for (int64_t k0 = 0; k0 < kend; k0 += BK) {
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
+        for (int r = 0; r < (BK * TBM) / NT; ++r) {
             const int e = tid + NT * r;
             int mm, kk;
             if (A_K_CONTIG) { kk = e % BK; mm = e / BK; }
-            else            { mm = e % BM; kk = e / BM; }
+            else            { mm = e % TBM; kk = e / TBM; }
             const int64_t gm = m0 + mm, gk = k0 + kk;
             As[kk][mm] = (gm < g.M && gk < g.K) ? A[gm * g.sAm + gk * g.sAk] : 0.0;
         }
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
+        for (int r = 0; r < (BK * TBN) / NT; ++r) {
             const int e = tid + NT * r;
             int nn, kk;
-            if (B_N_CONTIG) { nn = e % BN; kk = e / BN; }
+            if (B_N_CONTIG) { nn = e % TBN; kk = e / TBN; }
             else            { kk = e % BK; nn = e / BK; }
             const int64_t gn = n0 + nn, gk = k0 + kk;
             Bs[kk][nn] = (gn < g.N && gk < g.K) ? B[gk * g.sBk + gn * g.sBn] : 0.0;
@@ -61,9 +67,9 @@ __global__ void __launch_bounds__(NT) gemm_f64_kernel(GemmDesc g) {
         for (int kk = 0; kk < BK; ++kk) {
             double a[4], b[4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + (TBM / 4) * i];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + (TBN / 4) * j];
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -73,11 +79,11 @@ __global__ void __launch_bounds__(NT) gemm_f64_kernel(GemmDesc g) {
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        const int64_t gm = m0 + ty + 16 * i;
+        const int64_t gm = m0 + ty + (TBM / 4) * i;
         if (gm >= g.M) continue;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const int64_t gn = n0 + tx + 16 * j;
+            const int64_t gn = n0 + tx + (TBN / 4) * j;
             if (gn >= g.N) continue;
             double* c = C + gm * g.sCm + gn * g.sCn;
             double v = g.alpha * acc[i][j];
@@ -87,6 +93,24 @@ __global__ void __launch_bounds__(NT) gemm_f64_kernel(GemmDesc g) {
     }
 }
 
+template <int TBM, int TBN>
+int launch_tiles(ct_handle* h, const GemmDesc& g, int64_t nb) {
+    dim3 grid((unsigned)ct_cdiv(g.N, TBN), (unsigned)ct_cdiv(g.M, TBM), (unsigned)nb);
+    if (grid.y > 65535 || grid.z > 65535) {
+        ct_seterr(h, "gemm grid too large (M=%lld nb=%lld)", (long long)g.M, (long long)nb);
+        return CT_ERR_UNSUPPORTED;
+    }
+    constexpr int nt = (TBM / 4) * (TBN / 4);
+    const bool ak = (g.sAk == 1);
+    const bool bn = (g.sBn == 1);
+    if (ak && bn) { gemm_f64_kernel<TBM, TBN, true, true><<<grid, nt, 0, h->stream>>>(g); ct_note_launch(); }
+    else if (ak) { gemm_f64_kernel<TBM, TBN, true, false><<<grid, nt, 0, h->stream>>>(g); ct_note_launch(); }
+    else if (bn) { gemm_f64_kernel<TBM, TBN, false, true><<<grid, nt, 0, h->stream>>>(g); ct_note_launch(); }
+    else { gemm_f64_kernel<TBM, TBN, false, false><<<grid, nt, 0, h->stream>>>(g); ct_note_launch(); }
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
 }  // namespace
 
 int ct_gemm_f64_launch(ct_handle* h, const GemmDesc& g) {
@@ -94,17 +118,8 @@ int ct_gemm_f64_launch(ct_handle* h, const GemmDesc& g) {
     const int64_t nb = g.nb1 * g.nb0;
     if (nb <= 0) return CT_OK;
     if (g.K <= 0 && g.beta == 1.0) return CT_OK;  // C unchanged; K = 0 otherwise gives C = beta*C
-    dim3 grid((unsigned)ct_cdiv(g.N, BN), (unsigned)ct_cdiv(g.M, BM), (unsigned)nb);
-    if (grid.y > 65535 || grid.z > 65535) {
-        ct_seterr(h, "gemm grid too large (M=%lld nb=%lld)", (long long)g.M, (long long)nb);
-        return CT_ERR_UNSUPPORTED;
-    }
-    const bool ak = (g.sAk == 1);
-    const bool bn = (g.sBn == 1);
-    if (ak && bn) { gemm_f64_kernel<true, true><<<grid, NT, 0, h->stream>>>(g); ct_note_launch(); }
-    else if (ak) { gemm_f64_kernel<true, false><<<grid, NT, 0, h->stream>>>(g); ct_note_launch(); }
-    else if (bn) { gemm_f64_kernel<false, true><<<grid, NT, 0, h->stream>>>(g); ct_note_launch(); }
-    else { gemm_f64_kernel<false, false><<<grid, NT, 0, h->stream>>>(g); ct_note_launch(); }
-    CT_LAUNCH_CHECK(h);
-    return CT_OK;
+    // fewer 64 x 64 tiles than two per SM: 32 x 32 tiles
+    const int64_t tiles64 = ct_cdiv(g.N, 64) * ct_cdiv(g.M, 64) * nb;
+    if (tiles64 < 2 * (int64_t)h->num_sms) return launch_tiles<32, 32>(h, g, nb);
+    return launch_tiles<64, 64>(h, g, nb);
 }

@@ -166,9 +166,20 @@ int ct_env_right_run(ct_handle* h, Arena& ar, int prec, const double* Rn, const 
     return CT_OK;
 }
 
+size_t ct_theta_ws_bytes(int prec, int64_t Dl, int64_t d, int64_t Dm, int64_t Dr) {
+    return prec == CT_PREC_TF32X3 ? ct_tc_gemm_ws_bytes(Dl * d, d * Dr, Dm) : 0;
+}
+
+// theta = A_i . A_{i+1}.  In the mixed form the product runs on the tensor
+// cores: theta is only the Lanczos start vector, and an FP64 GEMM of this size
+// (8.6 GFLOP at chi = 1024) costs ~7 ms at this part's FP64 rate.  The
+// workspace must hold ct_theta_ws_bytes (the caller reserves it).
 int ct_theta_run(ct_handle* h, int prec, const double* Ai, const double* Aj, double* theta, int64_t Dl,
                  int64_t d, int64_t Dm, int64_t Dr) {
-    (void)prec;  // once per bond: always FP64
+    if (prec == CT_PREC_TF32X3 && ct_tc_available(h)) {
+        Arena ar(h);
+        return ct_tc_gemm(h, ar, 0, 0, Dl * d, d * Dr, Dm, 1.0, Ai, Dm, Aj, d * Dr, 0.0, theta, d * Dr);
+    }
     GemmDesc g{};
     g.M = Dl * d; g.N = d * Dr; g.K = Dm;
     g.A = Ai; g.sAm = Dm; g.sAk = 1;
@@ -207,10 +218,16 @@ int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, do
     CT_TRY(ct_reduce_nrm2sq(h, N, theta_in, h->d_scalars + SC_NORM, nullptr));
     CT_TRY(ct_scale_by_inv_sqrt(h, N, theta_in, V, h->d_scalars + SC_NORM, nullptr, CT_ERR_ZERO_NORM));
     const double thr = 100.0 * (double)N * 2.2204460492503131e-16;
+    // algorithmic FLOPs of one apply (the reference's four contractions)
+    const double heff_flops = 2.0 * (double)Dl * wL * d * d * Dr * Dl + 2.0 * (double)Dl * d * Dr * wL * d * d * wM +
+                              2.0 * (double)Dl * Dr * d * wM * d * d * wR + 2.0 * (double)Dl * d * d * Dr * wR * Dr;
     for (int j = 0; j < max_iter - 1; ++j) {
         double* vj = V + (int64_t)j * N;
         const double* vjm1 = (j > 0) ? V + (int64_t)(j - 1) * N : nullptr;
+        int ks = -1;
+        CT_TRY(ct_ktime_begin(h, KT_HEFF_APPLY, heff_flops, &ks));
         CT_TRY(ct_heff_run(h, plan, vj, w, stop));
+        CT_TRY(ct_ktime_end(h, ks));
         CT_TRY(ct_lanczos_alpha(h, N, vj, w, j, stop));
         CT_TRY(ct_lanczos_update(h, N, w, vj, vjm1, j, thr, stop));
         if (reorth) CT_TRY(ct_lanczos_reorth_beta(h, N, w, V, N, j + 1, j, thr, stop));
@@ -219,7 +236,10 @@ int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, do
     {   // final alpha-only iteration, only when no breakdown (dmrg.mojo:691-703)
         const int j = max_iter - 1;
         double* vj = V + (int64_t)j * N;
+        int ks = -1;
+        CT_TRY(ct_ktime_begin(h, KT_HEFF_APPLY, heff_flops, &ks));
         CT_TRY(ct_heff_run(h, plan, vj, w, stop));
+        CT_TRY(ct_ktime_end(h, ks));
         CT_TRY(ct_lanczos_alpha(h, N, vj, w, j, stop));
     }
     CT_TRY(ct_tridiag_eig(h, max_iter, tol, max_rotations));

@@ -655,38 +655,6 @@ struct SplitOperand {
     int64_t rows = 0, ldk = 0;
 };
 
-constexpr int KTIME_SLOTS = 4096;
-
-// Sum the elapsed times of the pending event pairs (waits for the last one).
-int ktime_harvest(ct_handle* h) {
-    if (h->ktime_pending == 0) return CT_OK;
-    CT_CUDA(h, cudaEventSynchronize(h->ktime_ev[2 * (h->ktime_pending - 1) + 1]));
-    for (int i = 0; i < h->ktime_pending; ++i) {
-        float ms = 0.f;
-        CT_CUDA(h, cudaEventElapsedTime(&ms, h->ktime_ev[2 * i], h->ktime_ev[2 * i + 1]));
-        h->ktime_ms += ms;
-        h->ktime_flops += h->ktime_slot_flops[i];
-    }
-    h->ktime_launches += h->ktime_pending;
-    h->ktime_pending = 0;
-    return CT_OK;
-}
-
-int ktime_begin(ct_handle* h, double flops, int* slot) {
-    *slot = -1;
-    if (!h->ktime_on) return CT_OK;
-    if (h->ktime_ev.empty()) {
-        h->ktime_ev.resize(2 * KTIME_SLOTS, nullptr);
-        h->ktime_slot_flops.resize(KTIME_SLOTS, 0.0);
-        for (auto& e : h->ktime_ev) CT_CUDA(h, cudaEventCreate(&e));
-    }
-    if (h->ktime_pending == KTIME_SLOTS) CT_TRY(ktime_harvest(h));
-    *slot = h->ktime_pending++;
-    h->ktime_slot_flops[*slot] = flops;
-    CT_CUDA(h, cudaEventRecord(h->ktime_ev[2 * *slot], h->stream));
-    return CT_OK;
-}
-
 int tc_gemm_launch(ct_handle* h, const SplitOperand& A, const SplitOperand& B, int64_t M, int64_t N,
                    const TcEpi& epi, const int* skip) {
     if (A.ldk != B.ldk) return CT_ERR_SHAPE;
@@ -708,7 +676,7 @@ int tc_gemm_launch(ct_handle* h, const SplitOperand& A, const SplitOperand& B, i
     }
     const int64_t tiles = ct_cdiv(N, GEMM_BN) * ct_cdiv(M, TC_BM);
     int slot = -1;
-    CT_TRY(ktime_begin(h, 2.0 * (double)M * (double)N * (double)A.ldk, &slot));
+    CT_TRY(ct_ktime_begin(h, KT_TC_GEMM, 2.0 * (double)M * (double)N * (double)A.ldk, &slot));
     if (tc_use_persistent()) {
         const int64_t grid = tiles < h->num_sms ? tiles : h->num_sms;
         tc_gemm_persist_kernel<GEMM_BN, GEMM_STAGES><<<(unsigned)grid, TC_THREADS, L::TOTAL, h->stream>>>(
@@ -720,7 +688,7 @@ int tc_gemm_launch(ct_handle* h, const SplitOperand& A, const SplitOperand& B, i
             ta_h, ta_l, tb_h, tb_l, (int)M, (int)N, (int)A.ldk, epi, skip, h->d_status); ct_note_launch();
     }
     CT_LAUNCH_CHECK(h);
-    if (slot >= 0) CT_CUDA(h, cudaEventRecord(h->ktime_ev[2 * slot + 1], h->stream));
+    CT_TRY(ct_ktime_end(h, slot));
     return CT_OK;
 }
 
@@ -1028,21 +996,3 @@ extern "C" CT_API int ct_tc_gemm_time(ct_handle* h, int64_t m, int64_t n, int64_
     return CT_OK;
 }
 
-extern "C" CT_API int ct_kernel_timing(ct_handle* h, int enable) {
-    if (!h) return CT_ERR_INVALID;
-    CT_TRY(ktime_harvest(h));
-    h->ktime_on = enable != 0;
-    h->ktime_launches = 0;
-    h->ktime_ms = 0.0;
-    h->ktime_flops = 0.0;
-    return CT_OK;
-}
-
-extern "C" CT_API int ct_kernel_timing_read(ct_handle* h, int64_t* launches, double* ms, double* flops) {
-    if (!h || !launches || !ms || !flops) return CT_ERR_INVALID;
-    CT_TRY(ktime_harvest(h));
-    *launches = h->ktime_launches;
-    *ms = h->ktime_ms;
-    *flops = h->ktime_flops;
-    return CT_OK;
-}

@@ -177,6 +177,7 @@ typedef struct ct_dmrg_stats {
     double energy_rayleigh;    /* FP64 Rayleigh quotient (NaN unless requested)  */
     int64_t subspace_splits;   /* mixed form: warm-started subspace splits      */
     int64_t exact_splits;      /* Jacobi-SVD splits                              */
+    double seconds_subspace;   /* part of seconds_svd spent in subspace splits   */
 } ct_dmrg_stats;
 
 /* Runs the sweeps in place.  mps_sites[i] are caller-owned device buffers of
@@ -274,6 +275,10 @@ CT_API int ct_tc_gemm_time(ct_handle* h, int64_t m, int64_t n, int64_t k, int re
  * (2 M N K, K rounded up to 32).  ct_kernel_timing(h, 0) stops recording. */
 CT_API int ct_kernel_timing(ct_handle* h, int enable);
 CT_API int ct_kernel_timing_read(ct_handle* h, int64_t* launches, double* ms, double* flops);
+/* Same per class: 0 = TF32x3 GEMM launches (as above), 1 = whole H_eff applies
+ * inside Lanczos (FLOPs = 4 D d^2 chi^3 + 4 D^2 d^3 chi^2 per apply, as in
+ * ct_dmrg_stats.heff_flops).                                                 */
+CT_API int ct_kernel_timing_read_class(ct_handle* h, int cls, int64_t* count, double* ms, double* flops);
 
 #ifdef __cplusplus
 }
