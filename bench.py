@@ -69,8 +69,9 @@ def parse():
     ap.add_argument("--L", type=int, default=L_SITES)
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64/roofline/CPU side measurements")
     ap.add_argument("--verbose", action="store_true", help="log every split of the timed sweeps to stderr")
-    ap.add_argument("--mode", default="sweep", choices=["sweep", "heff", "heff-grid"],
-                    help="heff: only centre-bond H_eff applies (a small, fixed workload for profilers)")
+    ap.add_argument("--mode", default="sweep", choices=["sweep", "heff", "heff-grid", "split"],
+                    help="heff / split: only centre-bond H_eff applies / warm splits (small, fixed workloads "
+                         "for profilers); heff-grid: H_eff over chi x D x d")
     return ap.parse_args()
 
 
@@ -104,6 +105,56 @@ def heff_mode(args):
                       "dtype": args.prec, "config": {"workload": f"centre-bond H_eff chi={chi} D=5 d=2"},
                       "steps": args.steps, "warmup": args.warmup,
                       "gpu_launches": _lib.launch_count() - n0}), flush=True)
+
+
+def split_mode(args):
+    """W + K warm subspace splits (ct_svd_split_warm) of a chi=1024 centre bond (profiling workload).
+
+    theta [1024, 2, 2, 1024] with singular values exp(-0.012 k) and random
+    singular vectors; the start basis is the exact right basis perturbed by
+    1e-5 noise and re-orthonormalised, i.e. a basis kept by the previous
+    visit of the bond.  One JSON line.
+    """
+    import ctypes as C
+    import torch
+    import chemtensor_mojo_gb300 as ct
+    ctx = ct.get_context(0)
+    dev = ctx.torch_device
+    Dl = Dr = args.chi
+    d = D_PHYS
+    m = n = Dl * d
+    c = args.chi
+    g = np.random.default_rng(4)
+    U, _ = np.linalg.qr(g.standard_normal((m, m)))
+    V, _ = np.linalg.qr(g.standard_normal((n, n)))
+    s = np.exp(-0.012 * np.arange(m))
+    M = (U * s) @ V.T
+    X, _ = np.linalg.qr((V[:, :c] + 1e-5 * g.standard_normal((n, c))))
+    th = torch.from_numpy(M.reshape(Dl, d, d, Dr).copy()).to(dev)
+    Xd = torch.from_numpy(np.ascontiguousarray(X.T)).to(dev)
+    bout = torch.empty(c * m, dtype=torch.float64, device=dev)
+    A = torch.empty(m * c, dtype=torch.float64, device=dev)
+    B = torch.empty(c * n, dtype=torch.float64, device=dev)
+    acc, disc = C.c_int(), C.c_double()
+
+    def one():
+        ctx.call("ct_svd_split_warm", C.c_void_p(th.data_ptr()), Dl, d, Dr, c, 1, C.c_void_p(Xd.data_ptr()), 0,
+                 C.c_void_p(bout.data_ptr()), C.c_void_p(A.data_ptr()), C.c_void_p(B.data_ptr()), C.byref(acc),
+                 C.byref(disc), None)
+
+    for _ in range(args.warmup):
+        one()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one()
+    torch.cuda.synchronize()
+    sec = (time.perf_counter() - t0) / max(args.steps, 1)
+    opt = float(np.sum(s[c:] ** 2) / np.sum(s ** 2))
+    print(json.dumps({"metric": "warm subspace split seconds", "value": sec, "unit": "s/split",
+                      "config": {"workload": f"theta {m}x{n}, chi={c}, left-to-right, no power steps"},
+                      "accepted": acc.value, "discarded": disc.value, "optimal_discarded": opt,
+                      "steps": args.steps, "warmup": args.warmup}), flush=True)
 
 
 def heff_grid_mode(args):
@@ -296,6 +347,9 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         reference_arm(args, rank)
+        return
+    if args.mode == "split":
+        split_mode(args)
         return
     if args.mode == "heff-grid":
         heff_grid_mode(args)

@@ -160,6 +160,7 @@ int ct_destroy(ct_handle* h) {
     cudaFree(h->ws);
     for (auto& b : h->basis_cache) cudaFree(b.p);
     for (auto e : h->ktime_ev) cudaEventDestroy(e);
+    cudaFree(h->splitk);
     cudaFree(h->d_status);
     cudaFree(h->d_scalars);
     cudaFree(h->d_partials);

@@ -42,6 +42,9 @@ struct ct_handle {
     // diagnostics: Jacobi sweeps of the last SVD split, and the running total
     int last_svd_sweeps = 0;
     int64_t total_svd_sweeps = 0;
+    // FP64 GEMM split-K partial sums (grown on demand, freed by ct_destroy)
+    double* splitk = nullptr;
+    size_t splitk_cap = 0;   // doubles
     // tensor-core path state
     bool tc_checked = false;
     bool tc_ok = false;
@@ -189,6 +192,9 @@ struct GemmDesc {
     const int* skip;
     int tri;   // 0: full; 1: write only C tiles on or below the diagonal (symmetric C);
                // 2: A is lower triangular (A(m, k) = 0 for k > m), skip those k
+    // set by the launcher: split-K partial sums (ksplit > 1) go to part[ks][M][N]
+    int64_t ksplit;
+    double* part;
 };
 int ct_gemm_f64_launch(ct_handle* h, const GemmDesc& g);
 

@@ -8,6 +8,8 @@
 // transposes.  FP64 on GB300 issues at a small fraction of the FP32 rate, so
 // a 64x64x16 smem tile with a 4x4 register block already saturates the FP64
 // pipe; the tensor-core path lives in ct_tc.cu.
+#include <algorithm>
+
 #include "ct_common.cuh"
 
 namespace {
@@ -26,7 +28,9 @@ __global__ void __launch_bounds__((TBM / 4) * (TBN / 4)) gemm_f64_kernel(GemmDes
     __shared__ double As[BK][TBM + 1];
     __shared__ double Bs[BK][TBN + 1];
 
-    const int64_t bz = blockIdx.z;
+    // blockIdx.z = batch * ksplit + k-chunk
+    const int64_t ks = (int64_t)blockIdx.z % g.ksplit;
+    const int64_t bz = (int64_t)blockIdx.z / g.ksplit;
     const int64_t b1 = bz / g.nb0, b0 = bz % g.nb0;
     const double* A = g.A + b1 * g.sA1 + b0 * g.sA0;
     const double* B = g.B + b1 * g.sB1 + b0 * g.sB0;
@@ -35,7 +39,13 @@ __global__ void __launch_bounds__((TBM / 4) * (TBN / 4)) gemm_f64_kernel(GemmDes
     const int64_t m0 = (int64_t)blockIdx.y * TBM, n0 = (int64_t)blockIdx.x * TBN;
     const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
     if (g.tri == 1 && n0 >= m0 + TBM) return;   // tile strictly above the diagonal
-    const int64_t kend = (g.tri == 2 && m0 + TBM < g.K) ? m0 + TBM : g.K;
+    int64_t kend = (g.tri == 2 && m0 + TBM < g.K) ? m0 + TBM : g.K;
+    int64_t kbeg = 0;
+    if (g.ksplit > 1) {
+        const int64_t chunk = ((g.K + g.ksplit - 1) / g.ksplit + BK - 1) / BK * BK;
+        kbeg = ks * chunk;
+        if (kbeg + chunk < kend) kend = kbeg + chunk;
+    }
 
     double acc[4][4];
 #pragma unroll
@@ -43,7 +53,7 @@ __global__ void __launch_bounds__((TBM / 4) * (TBN / 4)) gemm_f64_kernel(GemmDes
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
 
-    for (int64_t k0 = 0; k0 < kend; k0 += BK) {
+    for (int64_t k0 = kbeg; k0 < kend; k0 += BK) {
 #pragma unroll
         for (int r = 0; r < (BK * TBM) / NT; ++r) {
             const int e = tid + NT * r;
@@ -51,7 +61,7 @@ __global__ void __launch_bounds__((TBM / 4) * (TBN / 4)) gemm_f64_kernel(GemmDes
             if (A_K_CONTIG) { kk = e % BK; mm = e / BK; }
             else            { mm = e % TBM; kk = e / TBM; }
             const int64_t gm = m0 + mm, gk = k0 + kk;
-            As[kk][mm] = (gm < g.M && gk < g.K) ? A[gm * g.sAm + gk * g.sAk] : 0.0;
+            As[kk][mm] = (gm < g.M && gk < kend) ? A[gm * g.sAm + gk * g.sAk] : 0.0;
         }
 #pragma unroll
         for (int r = 0; r < (BK * TBN) / NT; ++r) {
@@ -60,7 +70,7 @@ __global__ void __launch_bounds__((TBM / 4) * (TBN / 4)) gemm_f64_kernel(GemmDes
             if (B_N_CONTIG) { nn = e % TBN; kk = e / TBN; }
             else            { kk = e % BK; nn = e / BK; }
             const int64_t gn = n0 + nn, gk = k0 + kk;
-            Bs[kk][nn] = (gn < g.N && gk < g.K) ? B[gk * g.sBk + gn * g.sBn] : 0.0;
+            Bs[kk][nn] = (gn < g.N && gk < kend) ? B[gk * g.sBk + gn * g.sBn] : 0.0;
         }
         __syncthreads();
 #pragma unroll
@@ -85,6 +95,10 @@ __global__ void __launch_bounds__((TBM / 4) * (TBN / 4)) gemm_f64_kernel(GemmDes
         for (int j = 0; j < 4; ++j) {
             const int64_t gn = n0 + tx + (TBN / 4) * j;
             if (gn >= g.N) continue;
+            if (g.ksplit > 1) {
+                g.part[(ks * g.M + gm) * g.N + gn] = acc[i][j];
+                continue;
+            }
             double* c = C + gm * g.sCm + gn * g.sCn;
             double v = g.alpha * acc[i][j];
             if (g.beta != 0.0) v = fma(g.beta, *c, v);
@@ -93,9 +107,25 @@ __global__ void __launch_bounds__((TBM / 4) * (TBN / 4)) gemm_f64_kernel(GemmDes
     }
 }
 
+// C = alpha * sum_ks part[ks] + beta * C, the partial sums added in a fixed
+// order (deterministic); tiles the GEMM kernel skips (tri == 1) stay untouched.
+__global__ void splitk_reduce_kernel(GemmDesc g, int tile) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < g.M * g.N;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t gm = t / g.N, gn = t % g.N;
+        if (g.tri == 1 && (gn / tile) * tile >= (gm / tile) * tile + tile) continue;
+        double a = 0.0;
+        for (int64_t ks = 0; ks < g.ksplit; ++ks) a += g.part[(ks * g.M + gm) * g.N + gn];
+        double* c = g.C + gm * g.sCm + gn * g.sCn;
+        double v = g.alpha * a;
+        if (g.beta != 0.0) v = fma(g.beta, *c, v);
+        *c = v;
+    }
+}
+
 template <int TBM, int TBN>
 int launch_tiles(ct_handle* h, const GemmDesc& g, int64_t nb) {
-    dim3 grid((unsigned)ct_cdiv(g.N, TBN), (unsigned)ct_cdiv(g.M, TBM), (unsigned)nb);
+    dim3 grid((unsigned)ct_cdiv(g.N, TBN), (unsigned)ct_cdiv(g.M, TBM), (unsigned)(nb * g.ksplit));
     if (grid.y > 65535 || grid.z > 65535) {
         ct_seterr(h, "gemm grid too large (M=%lld nb=%lld)", (long long)g.M, (long long)nb);
         return CT_ERR_UNSUPPORTED;
@@ -108,6 +138,13 @@ int launch_tiles(ct_handle* h, const GemmDesc& g, int64_t nb) {
     else if (bn) { gemm_f64_kernel<TBM, TBN, false, true><<<grid, nt, 0, h->stream>>>(g); ct_note_launch(); }
     else { gemm_f64_kernel<TBM, TBN, false, false><<<grid, nt, 0, h->stream>>>(g); ct_note_launch(); }
     CT_LAUNCH_CHECK(h);
+    if (g.ksplit > 1) {
+        const int64_t tot = g.M * g.N;
+        int64_t blocks = ct_cdiv(tot, 256);
+        if (blocks > 4 * (int64_t)h->num_sms) blocks = 4 * (int64_t)h->num_sms;
+        splitk_reduce_kernel<<<(unsigned)blocks, 256, 0, h->stream>>>(g, TBM); ct_note_launch();
+        CT_LAUNCH_CHECK(h);
+    }
     return CT_OK;
 }
 
@@ -118,8 +155,41 @@ int ct_gemm_f64_launch(ct_handle* h, const GemmDesc& g) {
     const int64_t nb = g.nb1 * g.nb0;
     if (nb <= 0) return CT_OK;
     if (g.K <= 0 && g.beta == 1.0) return CT_OK;  // C unchanged; K = 0 otherwise gives C = beta*C
-    // fewer 64 x 64 tiles than two per SM: 32 x 32 tiles
-    const int64_t tiles64 = ct_cdiv(g.N, 64) * ct_cdiv(g.M, 64) * nb;
-    if (tiles64 < 2 * (int64_t)h->num_sms) return launch_tiles<32, 32>(h, g, nb);
-    return launch_tiles<64, 64>(h, g, nb);
+    GemmDesc gg = g;
+    gg.ksplit = 1;
+    gg.part = nullptr;
+    const int64_t sms = h->num_sms;
+    // the FP64 pipe of one SM bounds a CTA here, so the launch needs about one
+    // CTA per SM: 64 x 64 tiles when there are enough of them, else split K over
+    // the idle SMs (64 x 64 tiles for deep K, 32 x 32 tiles for shallow K)
+    // tiles that do work (tri == 1 skips those strictly above the diagonal)
+    auto active = [&](int64_t t) {
+        const int64_t tm = ct_cdiv(g.M, t), tn = ct_cdiv(g.N, t);
+        if (g.tri != 1) return tm * tn * nb;
+        int64_t a = 0;
+        for (int64_t i = 0; i < tm; ++i) a += std::min<int64_t>(tn, i + 1);
+        return a * nb;
+    };
+    const int64_t tiles64 = active(64);
+    if (tiles64 >= sms) return launch_tiles<64, 64>(h, gg, nb);
+    const bool deep = g.K >= 512;
+    const int tile = deep ? 64 : 32;
+    const int64_t tiles = deep ? tiles64 : active(32);
+    if (nb == 1 && tiles < sms && g.K >= 2 * tile) {
+        int64_t ks = ct_cdiv(sms, tiles);
+        if (ks > g.K / tile) ks = g.K / tile;
+        if (ks > 1) {
+            const size_t need = (size_t)(ks * g.M * g.N);
+            if (h->splitk_cap < need) {
+                if (h->splitk) cudaFree(h->splitk);
+                h->splitk = nullptr;
+                h->splitk_cap = 0;
+                CT_CUDA(h, cudaMalloc((void**)&h->splitk, need * sizeof(double)));
+                h->splitk_cap = need;
+            }
+            gg.ksplit = ks;
+            gg.part = h->splitk;
+        }
+    }
+    return deep ? launch_tiles<64, 64>(h, gg, nb) : launch_tiles<32, 32>(h, gg, nb);
 }

@@ -126,12 +126,21 @@ __global__ void __launch_bounds__(256) chol_diag_kernel(double* G, double* Linv,
         __syncthreads();
     }
     if (t == 0) atomicMin(minpiv, (unsigned long long)__double_as_longlong(mp));
-    // column t of L^{-1} by forward substitution (the diagonal's reciprocals are kept)
-    if (t < CH_NB) {
-        for (int i = t; i < CH_NB; ++i) {
-            T s = (i == t) ? (T)1 : (T)0;
-            for (int l = t; l < i; ++l) s -= A[i][l] * X[l][t];
-            X[i][t] = s * dinv[i];
+    // column col of L^{-1} by forward substitution, four lanes per column: each
+    // lane sums every fourth term, two shuffles combine them (the diagonal's
+    // reciprocals are kept)
+    {
+        // the row loop is uniform across the warp (its 8 columns start at 8w);
+        // a column takes part once i reaches it
+        const int col = t >> 2, q = t & 3, first = (t >> 5) * 8;
+        for (int i = first; i < CH_NB; ++i) {
+            T s = (T)0;
+            if (i >= col)
+                for (int l = col + q; l < i; l += 4) s += A[i][l] * X[l][col];
+            s += __shfl_xor_sync(0xffffffffu, s, 1);
+            s += __shfl_xor_sync(0xffffffffu, s, 2);
+            if (q == 0 && i >= col) X[i][col] = (((i == col) ? (T)1 : (T)0) - s) * dinv[i];
+            __syncwarp();
         }
     }
     __syncthreads();

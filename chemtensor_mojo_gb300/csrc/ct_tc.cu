@@ -599,6 +599,62 @@ __global__ void __launch_bounds__(MPOT_NT) mpo_tc_kernel(MpoTcDesc m, int64_t jc
     }
 }
 
+// Two adjacent columns per thread (float2 loads and stores) and the weights
+// stored k-major in shared memory, read four at a time: per k one global load
+// and JT/4 shared loads feed 2 JT FMAs.  Block (x, o, z): columns
+// [2 (x * MPOT_NT + tid), +2) of slab o, output rows [z JT, z JT + JT) of J.
+// Needs unit column strides and even I, sIo, sIk, sOo and output offsets.
+template <int JT>
+__global__ void __launch_bounds__(MPOT_NT) mpo_tc2_kernel(MpoTcDesc m) {
+    if (ct_skip(m.skip)) return;
+    extern __shared__ __align__(16) float wk[];   // [K][JT], then JT int64 offsets
+    const int64_t jbeg = (int64_t)blockIdx.z * JT;
+    const int jn = (int)((m.J - jbeg) < JT ? (m.J - jbeg) : JT);
+    int64_t* joff = reinterpret_cast<int64_t*>(wk + ((m.K * JT + 3) & ~(int64_t)3));
+    for (int64_t t = threadIdx.x; t < m.K * JT; t += MPOT_NT) {
+        const int64_t k = t / JT, jj = t % JT;
+        wk[t] = (jj < jn) ? (float)m.Wt[(jbeg + jj) * m.K + k] : 0.f;
+    }
+    for (int j = threadIdx.x; j < jn; j += MPOT_NT) {
+        const int64_t jj = jbeg + j;
+        joff[j] = (jj / m.J0) * m.sOj1 + (jj % m.J0) * m.sOj0;
+    }
+    __syncthreads();
+    const int64_t o = blockIdx.y;
+    const int64_t i = 2 * ((int64_t)blockIdx.x * MPOT_NT + threadIdx.x);
+    if (i >= m.I) return;
+    const float* in = m.in + o * m.sIo + i;
+    float acc[JT][2];
+#pragma unroll
+    for (int j = 0; j < JT; ++j) acc[j][0] = acc[j][1] = 0.f;
+    for (int64_t k = 0; k < m.K; ++k) {
+        const float2 x = *reinterpret_cast<const float2*>(in + k * m.sIk);
+        const float4* w = reinterpret_cast<const float4*>(wk + k * JT);
+#pragma unroll
+        for (int j4 = 0; j4 < JT / 4; ++j4) {
+            const float4 v = w[j4];
+            acc[4 * j4 + 0][0] = fmaf(v.x, x.x, acc[4 * j4 + 0][0]);
+            acc[4 * j4 + 0][1] = fmaf(v.x, x.y, acc[4 * j4 + 0][1]);
+            acc[4 * j4 + 1][0] = fmaf(v.y, x.x, acc[4 * j4 + 1][0]);
+            acc[4 * j4 + 1][1] = fmaf(v.y, x.y, acc[4 * j4 + 1][1]);
+            acc[4 * j4 + 2][0] = fmaf(v.z, x.x, acc[4 * j4 + 2][0]);
+            acc[4 * j4 + 2][1] = fmaf(v.z, x.y, acc[4 * j4 + 2][1]);
+            acc[4 * j4 + 3][0] = fmaf(v.w, x.x, acc[4 * j4 + 3][0]);
+            acc[4 * j4 + 3][1] = fmaf(v.w, x.y, acc[4 * j4 + 3][1]);
+        }
+    }
+    const int64_t obase = o * m.sOo + i;
+#pragma unroll
+    for (int j = 0; j < JT; ++j) {
+        if (j >= jn) break;
+        float2 hv, lv;
+        split_tf32(acc[j][0], hv.x, lv.x);
+        split_tf32(acc[j][1], hv.y, lv.y);
+        *reinterpret_cast<float2*>(m.hi + obase + joff[j]) = hv;
+        *reinterpret_cast<float2*>(m.lo + obase + joff[j]) = lv;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -715,8 +771,36 @@ PackDesc pack_desc(const double* src, int64_t rows, int64_t R0, int64_t s_r1, in
     return p;
 }
 
+template <int JT>
+int mpo_tc2_launch(ct_handle* h, const MpoTcDesc& m) {
+    const size_t smem = (size_t)((m.K * JT + 3) & ~(int64_t)3) * sizeof(float) + JT * sizeof(int64_t);
+    static int attr_dev = -1;
+    if (attr_dev != h->device) {
+        CT_CUDA(h, cudaFuncSetAttribute(mpo_tc2_kernel<JT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        96 * 1024));
+        attr_dev = h->device;
+    }
+    dim3 grid((unsigned)ct_cdiv(m.I / 2, MPOT_NT), (unsigned)m.O, (unsigned)ct_cdiv(m.J, JT));
+    mpo_tc2_kernel<JT><<<grid, MPOT_NT, smem, h->stream>>>(m); ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
 int mpo_tc_launch(ct_handle* h, const MpoTcDesc& m) {
     if (m.O <= 0 || m.I <= 0 || m.J <= 0) return CT_OK;
+    // paired-column kernel when the layout allows float2 access and the weight
+    // chunk fits (K x 32 floats within 96 KB)
+    const bool even = m.sIi == 1 && m.sOi == 1 && (m.I % 2) == 0 && (m.sIo % 2) == 0 && (m.sIk % 2) == 0 &&
+                      (m.sOo % 2) == 0 && (m.sOj1 % 2) == 0 && (m.sOj0 % 2) == 0 &&
+                      (((uintptr_t)m.in | (uintptr_t)m.hi | (uintptr_t)m.lo) & 7) == 0;
+    if (even && m.O <= 65535 && (size_t)m.K * 32 * sizeof(float) + 256 <= 96 * 1024) {
+        if (m.J <= 8) return mpo_tc2_launch<8>(h, m);
+        if (m.J <= 12) return mpo_tc2_launch<12>(h, m);
+        if (m.J <= 16) return mpo_tc2_launch<16>(h, m);
+        if (m.J <= 20) return mpo_tc2_launch<20>(h, m);
+        if (m.J <= 24) return mpo_tc2_launch<24>(h, m);
+        return mpo_tc2_launch<32>(h, m);
+    }
     // the whole of Wt in shared memory when it fits in 96 KB, else chunks of rows
     constexpr size_t kBudget = 96 * 1024;
     const size_t per_row = (size_t)m.K * sizeof(float) + sizeof(int64_t);
