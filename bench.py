@@ -18,10 +18,12 @@ Reported (one JSON line on rank 0):
   e2e            the same through the C ABI from pinned host buffers
                  (MPS/MPO copied in and the final MPS + energy copied out
                  inside the timed region)
-  heff_tflops    algorithmic H_eff FLOP/s inside the sweep (Lanczos phase)
-  roofline       tcgen05 TF32x3 GEMM (the dominant kernel) at the centre-bond
-                 shapes, algorithmic FLOP/s vs the measured-BF16-derived
-                 3xTF32 ceiling
+  heff_tflops    algorithmic H_eff FLOP/s over the whole Lanczos phase
+  roofline       the tcgen05 TF32x3 GEMM: every launch of the timed sweeps,
+                 timed with CUDA events on the launching stream; algorithmic
+                 FLOP/s vs the measured-BF16-derived 3xTF32 ceiling
+  breakdown      CUDA-event seconds of the timed sweeps per phase (H_eff
+                 applies, other Lanczos work, subspace / Jacobi splits, envs)
   fp64           the plain FP64 form: centre-bond H_eff apply time and an
                  accuracy check |dE/E| (mixed vs FP64) on the same ramp to chi=256
   cpu_baseline   the CPU FP64 oracle (NumPy/LAPACK, all host cores) on one

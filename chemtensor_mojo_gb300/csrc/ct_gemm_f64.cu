@@ -159,9 +159,9 @@ int ct_gemm_f64_launch(ct_handle* h, const GemmDesc& g) {
     gg.ksplit = 1;
     gg.part = nullptr;
     const int64_t sms = h->num_sms;
-    // the FP64 pipe of one SM bounds a CTA here, so the launch needs about one
-    // CTA per SM: 64 x 64 tiles when there are enough of them, else split K over
-    // the idle SMs (64 x 64 tiles for deep K, 32 x 32 tiles for shallow K)
+    // the FP64 pipe of one SM bounds a CTA here, so the launch needs at least
+    // one CTA per SM: 64 x 64 tiles when there are two per SM, else 32 x 32
+    // tiles, with K split over the idle SMs when even those are too few
     // tiles that do work (tri == 1 skips those strictly above the diagonal)
     auto active = [&](int64_t t) {
         const int64_t tm = ct_cdiv(g.M, t), tn = ct_cdiv(g.N, t);
@@ -170,14 +170,13 @@ int ct_gemm_f64_launch(ct_handle* h, const GemmDesc& g) {
         for (int64_t i = 0; i < tm; ++i) a += std::min<int64_t>(tn, i + 1);
         return a * nb;
     };
-    const int64_t tiles64 = active(64);
-    if (tiles64 >= sms) return launch_tiles<64, 64>(h, gg, nb);
-    const bool deep = g.K >= 512;
-    const int tile = deep ? 64 : 32;
-    const int64_t tiles = deep ? tiles64 : active(32);
-    if (nb == 1 && tiles < sms && g.K >= 2 * tile) {
+    // (measured: 32 x 32 tiles, several CTAs per SM, beat 64 x 64 tiles with
+    // split K on a 1024 x 1024 x 2048 lower-only product, 2.7 vs 3.1 ms)
+    if (active(64) >= 2 * sms) return launch_tiles<64, 64>(h, gg, nb);
+    const int64_t tiles = active(32);
+    if (nb == 1 && tiles < sms && g.K >= 64) {
         int64_t ks = ct_cdiv(sms, tiles);
-        if (ks > g.K / tile) ks = g.K / tile;
+        if (ks > g.K / 32) ks = g.K / 32;
         if (ks > 1) {
             const size_t need = (size_t)(ks * g.M * g.N);
             if (h->splitk_cap < need) {
@@ -191,5 +190,5 @@ int ct_gemm_f64_launch(ct_handle* h, const GemmDesc& g) {
             gg.part = h->splitk;
         }
     }
-    return deep ? launch_tiles<64, 64>(h, gg, nb) : launch_tiles<32, 32>(h, gg, nb);
+    return launch_tiles<32, 32>(h, gg, nb);
 }
