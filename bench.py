@@ -54,6 +54,9 @@ MPO_D = 5
 LANCZOS = 24
 EPS = 0.0
 RAMP = [64, 256, 1024]
+# accuracy check (mixed vs FP64): sweeps at chi=256 until both forms converge, so
+# the difference measures precision rather than early-trajectory noise
+ACC_RAMP = (64, 256, 256, 256, 256)
 # dram__bytes_read.sum + dram__bytes_write.sum of one centre-bond H_eff GEMM launch
 # (5120 x 4096 x 1024, chi=1024) from ncu; profiles/tc_gemm_kernel_heff_chi1024.md
 TC_GEMM_TRAFFIC_BYTES = (78.5 + 55.7) * 1e6
@@ -71,7 +74,7 @@ def parse():
     ap.add_argument("--L", type=int, default=L_SITES)
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64/roofline/CPU side measurements")
     ap.add_argument("--verbose", action="store_true", help="log every split of the timed sweeps to stderr")
-    ap.add_argument("--mode", default="sweep", choices=["sweep", "heff", "heff-grid", "split"],
+    ap.add_argument("--mode", default="sweep", choices=["sweep", "heff", "heff-grid", "split", "hubbard"],
                     help="heff / split: only centre-bond H_eff applies / warm splits (small, fixed workloads "
                          "for profilers); heff-grid: H_eff over chi x D x d")
     return ap.parse_args()
@@ -157,6 +160,64 @@ def split_mode(args):
                       "config": {"workload": f"theta {m}x{n}, chi={c}, left-to-right, no power steps"},
                       "accepted": acc.value, "discarded": disc.value, "optimal_discarded": opt,
                       "steps": args.steps, "warmup": args.warmup}), flush=True)
+
+
+def hubbard_mode(args):
+    """Large mixed-precision run with gradient, at the chi this box's time allows.
+
+    1D Fermi-Hubbard chain (Jordan-Wigner), L=48, d=4, t=1, U=8, MPO bond
+    dimension 6; seeded Gaussian initial MPS; chi_max ramped 256 -> 512 ->
+    1024 (two sweeps each, 24 Lanczos steps, eps_trunc = 0) in the mixed form
+    with kept bases across the ramp and randomized first-visit splits (two
+    power steps); then one FP64 adjoint-gradient pass at the final state
+    (environment checkpoints every 7 sites).  Reports sweep seconds per chi,
+    the FP64 Rayleigh energy, the gradient residual |grad E| (zero at a
+    stationary state) and peak device memory.  One JSON line.
+    """
+    import ctypes as C
+    import torch
+    import chemtensor_mojo_gb300 as ct
+    from chemtensor_mojo_gb300 import _lib
+    from chemtensor_mojo_gb300.autograd import energy_and_gradient
+    ctx = ct.get_context(0)
+    L = 48
+    ramp = [256, 512, 1024] if args.chi >= 1024 else [c for c in (256, 512, 1024) if c <= args.chi]
+    mpo = ct.create_fermi_hubbard_mpo(ctx, L, 1.0, 8.0)
+    arrays, _ = ct.random_mps_c_compatible_arrays(L, 4, ramp[0], 11)
+    mps = ct.mps_right_normalize(ctx, ct.mps_from_arrays(ctx, arrays))
+    free0, total = torch.cuda.mem_get_info()
+    peak_used = 0
+    log = []
+    first = True
+    for chi in ramp:
+        st = ct.DMRGStats()
+        p = ct.DMRGParams(num_sweeps=2, chi_max=chi, eps_trunc=0.0, max_krylov_iter=LANCZOS, krylov_tol=1e-10,
+                          energy_tol=0.0, max_rotations=0, prec="tf32x3", final_rayleigh=True,
+                          keep_bases=not first, cold_power_steps=2)
+        E, mps = ct.dmrg_two_site(ctx, mpo, mps, p, st)
+        first = False
+        free, _ = torch.cuda.mem_get_info()
+        peak_used = max(peak_used, total - free)
+        log.append({"chi_max": chi, "seconds_per_sweep": st.seconds_total / 2, "energy_rayleigh": st.energy_rayleigh,
+                    "subspace_splits": st.subspace_splits, "cold_splits": st.cold_splits,
+                    "exact_splits": st.exact_splits, "heff_tflops": st.heff_flops / max(st.seconds_lanczos, 1e-12) / 1e12,
+                    "max_discarded": st.max_discarded})
+    sites = [s.tensor.storage[: int(np.prod(s.tensor.shape))].view(*s.tensor.shape) for s in mps.sites]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Eg, grads = energy_and_gradient(mpo, sites, checkpoint_every=7, ctx=ctx)
+    torch.cuda.synchronize()
+    tg = time.perf_counter() - t0
+    free, _ = torch.cuda.mem_get_info()
+    peak_used = max(peak_used, total - free)
+    gnorm = float(torch.sqrt(sum((g * g).sum() for g in grads)))
+    print(json.dumps({"metric": "Fermi-Hubbard L=48 mixed sweep seconds", "unit": "s/sweep", "data": "synthetic",
+                      "config": {"workload": "1D Fermi-Hubbard JW L=48 d=4 t=1 U=8 D=6, chi ramp " +
+                                 "->".join(str(c) for c in ramp) + ", 2 sweeps each, lanczos=24, eps=0"},
+                      "ramp": log, "gradient": {"energy": Eg, "seconds": tg, "norm": gnorm,
+                                                "checkpoint_every": 7, "dtype": "f64"},
+                      "peak_device_bytes": int(peak_used), "device_bytes_before": int(total - free0)}),
+          flush=True)
 
 
 def heff_grid_mode(args):
@@ -353,6 +414,9 @@ def main():
     if args.mode == "split":
         split_mode(args)
         return
+    if args.mode == "hubbard":
+        hubbard_mode(args)
+        return
     if args.mode == "heff-grid":
         heff_grid_mode(args)
         return
@@ -451,6 +515,7 @@ def main():
     clocks.stop()
     kt = None
     kt_heff = None
+    kt_centre = None
     if kt_on:
         def read_class(cls):
             n_kt, ms_kt, fl_kt = C.c_int64(), C.c_double(), C.c_double()
@@ -458,6 +523,7 @@ def main():
             return {"launches": n_kt.value, "ms": ms_kt.value, "flops": fl_kt.value}
         kt = read_class(0)        # every TF32x3 GEMM launch
         kt_heff = read_class(1)   # every whole H_eff apply inside Lanczos
+        kt_centre = read_class(2)  # the applies at the largest size (centre bonds at chi_max)
         ctx.call("ct_kernel_timing", 0)
     if dist is not None:
         dist.barrier()
@@ -515,6 +581,8 @@ def main():
         "clocks": clocks.summary(),
     }
     line.update(extras)
+    if "fp64_sweep_s_estimate" in extras:
+        line["speedup_vs_fp64_form_estimate"] = extras["fp64_sweep_s_estimate"] / per_sweep
     if kt and kt["launches"] > 0 and kt["ms"] > 0:
         # live: every TF32x3 GEMM launch of the timed sweeps, CUDA events on the launching stream
         ach = kt["flops"] / (kt["ms"] * 1e-3) / 1e12
@@ -536,6 +604,11 @@ def main():
             "timed_region_s": dev_s,
             "heff_apply_s": heff_s, "heff_apply_count": kt_heff["launches"],
             "heff_apply_tflops": kt_heff["flops"] / max(heff_s, 1e-12) / 1e12,
+            "heff_apply_centre_count": kt_centre["launches"],
+            "heff_apply_centre_ms": kt_centre["ms"] / max(kt_centre["launches"], 1),
+            "heff_apply_centre_tflops": kt_centre["flops"] / max(kt_centre["ms"] * 1e-3, 1e-12) / 1e12,
+            "heff_apply_centre_frac_of_3xtf32_peak": (kt_centre["flops"] / max(kt_centre["ms"] * 1e-3, 1e-12)
+                                                      / 1e12) / (bf16 / 6.0),
             "tc_gemm_s_all": gemm_s,
             "lanczos_other_s": stats.seconds_lanczos - heff_s,
             "split_subspace_s": stats.seconds_subspace,
@@ -591,6 +664,26 @@ def side_measurements(ctx, ct, _lib, C, chi, prec, L, mpo):
             o64 = o.to_numpy()
     out["heff_apply_rel_err_tf32x3_vs_fp64"] = float(np.linalg.norm(o_mixed - o64) / np.linalg.norm(o64))
     out["heff_apply_speedup_vs_fp64"] = out["heff_apply_fp64_s"] / out["heff_apply_tf32x3_s"]
+    # plain FP64 form of the sweep, estimated from its measured centre-bond pieces:
+    # one FP64 Jacobi split of theta (2chi x 2chi) and the FP64 H_eff apply, weighted
+    # like the sweep (H_eff by FLOPs; one full-size split per binding bond visit)
+    thm = torch.randn(chi * 4 * chi, generator=g, dtype=torch.float64).to(dev)
+    Ab = torch.empty(2 * chi * chi, dtype=torch.float64, device=dev)
+    Bb = torch.empty(2 * chi * chi, dtype=torch.float64, device=dev)
+    chi_c, disc_c = C.c_int64(), C.c_double()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx.call("ct_svd_split", _lib.CT_PREC_FP64, C.c_void_p(thm.data_ptr()), chi, D_PHYS, chi, chi, 0.0, 1,
+             C.c_void_p(Ab.data_ptr()), C.c_void_p(Bb.data_ptr()), None, C.byref(chi_c), C.byref(disc_c))
+    torch.cuda.synchronize()
+    split64 = time.perf_counter() - t0
+    caps = bond_caps(L, chi)
+    full_visits = 2 * sum(1 for i in range(L - 1) if min(2 * caps[i], 2 * caps[i + 2]) > chi)
+    weight = sweep_flop_weight(L, chi)
+    out["fp64_split_s"] = split64
+    out["fp64_sweep_s_estimate"] = LANCZOS * out["heff_apply_fp64_s"] * weight + split64 * full_visits
+    out["fp64_sweep_note"] = (f"{LANCZOS} FP64 H_eff applies x {weight:.1f} centre-bond FLOP weights + "
+                              f"{full_visits} FP64 Jacobi splits of {2 * chi}x{2 * chi} (measured once)")
     # accuracy: mixed vs FP64 on the same ramp capped at chi=256 (FP64 affordable)
     arrays, _ = ct.random_mps_c_compatible_arrays(L, D_PHYS, RAMP[0], 7)
     res = {}
@@ -599,13 +692,14 @@ def side_measurements(ctx, ct, _lib, C, chi, prec, L, mpo):
         mps = ct.mps_right_normalize(ctx, ct.mps_from_arrays(ctx, arrays))
         t0 = time.perf_counter()
         st = ct.DMRGStats()
-        for c in (64, 256, 256):
+        for c in ACC_RAMP:
             E, mps = ct.dmrg_two_site(ctx, mpo, mps, ct.DMRGParams(
                 num_sweeps=1, chi_max=c, eps_trunc=EPS, max_krylov_iter=LANCZOS, krylov_tol=1e-10,
                 energy_tol=0.0, max_rotations=0, prec=pr, final_rayleigh=(c == 256)), st)
         tsec[pr] = time.perf_counter() - t0
         res[pr] = st.energy_rayleigh if pr == "tf32x3" else E
-    out["accuracy_check"] = {"workload": f"same chain, ramp 64,256,256 ({L} sites)", "E_fp64": res["fp64"],
+    out["accuracy_check"] = {"workload": f"same chain, chi ramp {','.join(map(str, ACC_RAMP))} ({L} sites)",
+                             "E_fp64": res["fp64"],
                              "E_tf32x3_rayleigh_fp64": res["tf32x3"],
                              "dE_over_E": abs(res["tf32x3"] - res["fp64"]) / abs(res["fp64"]),
                              "seconds_fp64": tsec["fp64"], "seconds_tf32x3": tsec["tf32x3"]}

@@ -43,7 +43,7 @@ class ct_dmrg_params(C.Structure):
                 ("max_krylov_iter", C.c_int), ("krylov_tol", C.c_double), ("energy_tol", C.c_double),
                 ("two_site", C.c_int), ("verbose", C.c_int), ("prec", C.c_int), ("max_rotations", C.c_int),
                 ("reorth", C.c_int), ("final_rayleigh", C.c_int), ("keep_bases", C.c_int),
-                ("split_power_steps", C.c_int)]
+                ("split_power_steps", C.c_int), ("cold_power_steps", C.c_int)]
 
 
 class ct_dmrg_stats(C.Structure):
@@ -51,7 +51,7 @@ class ct_dmrg_stats(C.Structure):
                 ("seconds_env", C.c_double), ("heff_flops", C.c_double), ("env_flops", C.c_double),
                 ("heff_applies", C.c_int64), ("local_updates", C.c_int64), ("max_discarded", C.c_double),
                 ("energy_rayleigh", C.c_double), ("subspace_splits", C.c_int64), ("exact_splits", C.c_int64),
-                ("seconds_subspace", C.c_double)]
+                ("seconds_subspace", C.c_double), ("cold_splits", C.c_int64)]
 
 
 P = C.c_void_p

@@ -577,9 +577,26 @@ int ct_ktime_harvest(ct_handle* h) {
         float ms = 0.f;
         CT_CUDA(h, cudaEventElapsedTime(&ms, h->ktime_ev[2 * i], h->ktime_ev[2 * i + 1]));
         const int c = h->ktime_slot_cls[i];
+        const double fl = h->ktime_slot_flops[i];
         h->ktime_ms[c] += ms;
-        h->ktime_flops[c] += h->ktime_slot_flops[i];
+        h->ktime_flops[c] += fl;
         h->ktime_count[c] += 1;
+        if (c == KT_HEFF_APPLY) {
+            // running bucket of the largest applies (relative tolerance 1e-9 on the FLOP count)
+            const double top = h->ktime_count[KT_HEFF_LARGEST] > 0
+                                   ? h->ktime_flops[KT_HEFF_LARGEST] / (double)h->ktime_count[KT_HEFF_LARGEST]
+                                   : 0.0;
+            if (fl > top * (1.0 + 1e-9)) {
+                h->ktime_count[KT_HEFF_LARGEST] = 0;
+                h->ktime_ms[KT_HEFF_LARGEST] = 0.0;
+                h->ktime_flops[KT_HEFF_LARGEST] = 0.0;
+            }
+            if (fl >= top * (1.0 - 1e-9)) {
+                h->ktime_count[KT_HEFF_LARGEST] += 1;
+                h->ktime_ms[KT_HEFF_LARGEST] += ms;
+                h->ktime_flops[KT_HEFF_LARGEST] += fl;
+            }
+        }
     }
     h->ktime_pending = 0;
     return CT_OK;

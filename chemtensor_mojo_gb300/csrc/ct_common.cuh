@@ -61,8 +61,9 @@ struct ct_handle {
     double ktime_ms[4] = {0, 0, 0, 0}, ktime_flops[4] = {0, 0, 0, 0};
 };
 
-// live timing classes
-enum { KT_TC_GEMM = 0, KT_HEFF_APPLY = 1, KT_NCLASSES = 4 };
+// live timing classes; KT_HEFF_LARGEST is derived: the H_eff applies with the
+// largest FLOP count seen (the centre bond at chi_max)
+enum { KT_TC_GEMM = 0, KT_HEFF_APPLY = 1, KT_HEFF_LARGEST = 2, KT_NCLASSES = 4 };
 // start a timed region of class cls (slot = -1 when timing is off); end it after the launches
 int ct_ktime_begin(ct_handle* h, int cls, double flops, int* slot);
 int ct_ktime_end(ct_handle* h, int slot);

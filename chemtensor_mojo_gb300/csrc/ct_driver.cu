@@ -139,6 +139,7 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         for (auto& b : h->basis_cache) b.len = b.c = -1;
 
     EventTimer ev_l, ev_s, ev_e;
+    uint64_t cold_seq = 0;   // seeds of the random start rows of first-visit splits
     ct_dmrg_stats st{};
     std::vector<double> disc_all;
 
@@ -256,6 +257,32 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
                         own.len = own_len;
                         own.c = c;
                         own.disc = binding && so.sum_s2_all > 0.0 ? 1.0 - so.sum_s2_kept / so.sum_s2_all : -1.0;
+                    }
+                }
+                if (!done_split && use_subspace && P->cold_power_steps >= 0) {
+                    // first visit: rows the bond kept at a smaller chi (same length), then random rows
+                    const size_t mark = ar.off;
+                    double* X = ar.take<double>(c * src_len);
+                    if (!X) return CT_ERR_OOM;
+                    const bool reuse = src.p && src.len == src_len && src.c > 0 && src.c < c;
+                    const uint64_t seed = 0x5DEECE66Dull * (uint64_t)(2 * i + (l2r ? 0 : 1)) + (uint64_t)(++cold_seq);
+                    CT_TRY(ct_cold_basis(h, reuse ? src.p : nullptr, reuse ? src.c : 0, c, src_len, seed, X));
+                    bool ok = false;
+                    CT_TRY(ct_split_subspace(h, ar, th_opt.p, m, n, c, l2r ? 0 : 1, X, own.p, mps_sites[i],
+                                             mps_sites[i + 1], h->d_scalars + SC_THETA_NSQ, P->eps_trunc, -1.0,
+                                             P->cold_power_steps, &so, &ok));
+                    ar.off = mark;
+                    done_split = ok;
+                    last_split_subspace = ok;
+                    if (P->verbose >= 2)
+                        fprintf(stderr, "bond %d %s: cold subspace split %s (%lld kept rows reused)\n", i,
+                                l2r ? "L->R" : "R->L", ok ? "accepted" : "refused", reuse ? (long long)src.c : 0ll);
+                    if (ok) {
+                        st.subspace_splits++;
+                        st.cold_splits++;
+                        own.len = own_len;
+                        own.c = c;
+                        own.disc = -1.0;   // no reference: the next visit must not be judged against it
                     }
                 }
             }

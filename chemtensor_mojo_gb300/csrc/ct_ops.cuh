@@ -84,6 +84,9 @@ int ct_split_subspace(ct_handle* h, Arena& ar, const double* M, int64_t m, int64
                       const double* basis_in, double* basis_out, double* Aout, double* Bout,
                       const double* d_total, double eps_trunc, double disc_ref, int power_steps, SvdOut* out,
                       bool* accepted);
+// first-visit start basis: kept rows (may be null) then random Gaussian rows
+int ct_cold_basis(ct_handle* h, const double* prev, int64_t c_prev, int64_t c, int64_t len, uint64_t seed,
+                  double* X);
 int ct_basis_from_split(ct_handle* h, int mode, const double* Aout, const double* Bout, int64_t m, int64_t n,
                         int64_t c, double* basis);
 

@@ -400,6 +400,42 @@ int ct_split_subspace(ct_handle* h, Arena& ar, const double* M, int64_t m, int64
     return CT_OK;
 }
 
+namespace {
+// counter-based N(0,1) fill: splitmix64 of (seed, index), Box-Muller
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__global__ void randn_fill_kernel(double* X, int64_t n, uint64_t seed) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t a = mix64(seed ^ mix64((uint64_t)t * 2)), b = mix64(seed ^ mix64((uint64_t)t * 2 + 1));
+        const double u1 = ((double)(a >> 11) + 1.0) * (1.0 / 9007199254740993.0);   // (0, 1]
+        const double u2 = (double)(b >> 11) * (1.0 / 9007199254740992.0);
+        X[t] = sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+    }
+}
+}  // namespace
+
+// Start basis for a first visit: the rows kept at a smaller chi (prev, c_prev
+// rows of length len, may be null) followed by random Gaussian rows.
+int ct_cold_basis(ct_handle* h, const double* prev, int64_t c_prev, int64_t c, int64_t len, uint64_t seed,
+                  double* X) {
+    if (c_prev > c) c_prev = c;
+    if (prev && c_prev > 0)
+        CT_CUDA(h, cudaMemcpyAsync(X, prev, (size_t)(c_prev * len) * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   h->stream));
+    else
+        c_prev = 0;
+    const int64_t nr = (c - c_prev) * len;
+    if (nr > 0) {
+        randn_fill_kernel<<<grid_n(h, nr), 256, 0, h->stream>>>(X + c_prev * len, nr, seed); ct_note_launch();
+        CT_LAUNCH_CHECK(h);
+    }
+    return CT_OK;
+}
+
 // Refresh a basis cache (c rows) from an exact split's outputs: the rows of
 // A^T after a left-to-right split, the rows of B after a right-to-left one.
 int ct_basis_from_split(ct_handle* h, int mode, const double* Aout, const double* Bout, int64_t m, int64_t n,

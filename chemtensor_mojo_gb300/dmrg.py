@@ -46,13 +46,15 @@ class DMRGParams:
     final_rayleigh: bool = False
     keep_bases: bool = False
     split_power_steps: int = 0   # -1: always the Jacobi SVD split
+    cold_power_steps: int = -1   # >= 0: randomized subspace split on first visits
 
     def to_c(self) -> _lib.ct_dmrg_params:
         return _lib.ct_dmrg_params(int(self.num_sweeps), int(self.chi_max), float(self.eps_trunc),
                                    int(self.max_krylov_iter), float(self.krylov_tol), float(self.energy_tol),
                                    int(bool(self.two_site)), int(self.verbose), _lib.PRECISIONS[self.prec],
                                    int(self.max_rotations), int(bool(self.reorth)), int(bool(self.final_rayleigh)),
-                                   int(bool(self.keep_bases)), int(self.split_power_steps))
+                                   int(bool(self.keep_bases)), int(self.split_power_steps),
+                                   int(self.cold_power_steps))
 
 
 @dataclass
@@ -70,6 +72,7 @@ class DMRGStats:
     subspace_splits: int = 0
     exact_splits: int = 0
     seconds_subspace: float = 0.0
+    cold_splits: int = 0
     sweep_energies: List[float] = field(default_factory=list)
     discarded: List[float] = field(default_factory=list)
 
@@ -260,7 +263,7 @@ def dmrg_two_site(ctx: DeviceContext | None, mpo: MatrixProductOperator, mps: Ma
     if stats is not None:
         for f in ("seconds_total", "seconds_lanczos", "seconds_svd", "seconds_env", "heff_flops", "env_flops",
                   "heff_applies", "local_updates", "max_discarded", "energy_rayleigh", "subspace_splits",
-                  "exact_splits", "seconds_subspace"):
+                  "exact_splits", "seconds_subspace", "cold_splits"):
             setattr(stats, f, getattr(st, f))
         stats.sweep_energies = list(sweeps)[:done.value]
         stats.discarded = list(disc)[:done.value * 2 * (N - 1)]

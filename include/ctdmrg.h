@@ -162,6 +162,13 @@ typedef struct ct_dmrg_params {
                             of the warm-started subspace split (0 is enough
                             for |dE/E| <= 1e-9 on the benchmark chain); -1
                             always runs the Jacobi SVD instead                */
+    int cold_power_steps;  /* mixed form, a large bond with no kept basis (first
+                            visit, or chi_max just raised): -1 runs the Jacobi
+                            SVD; >= 0 runs the subspace split from the rows the
+                            bond kept at a smaller chi (if any) plus random
+                            Gaussian rows, with this many power steps first
+                            (2 or more: the truncation of that first visit is
+                            then close to, not equal to, the SVD's)          */
 } ct_dmrg_params;
 
 typedef struct ct_dmrg_stats {
@@ -178,6 +185,7 @@ typedef struct ct_dmrg_stats {
     int64_t subspace_splits;   /* mixed form: warm-started subspace splits      */
     int64_t exact_splits;      /* Jacobi-SVD splits                              */
     double seconds_subspace;   /* part of seconds_svd spent in subspace splits   */
+    int64_t cold_splits;       /* subspace splits started from random rows       */
 } ct_dmrg_stats;
 
 /* Runs the sweeps in place.  mps_sites[i] are caller-owned device buffers of
@@ -277,7 +285,8 @@ CT_API int ct_kernel_timing(ct_handle* h, int enable);
 CT_API int ct_kernel_timing_read(ct_handle* h, int64_t* launches, double* ms, double* flops);
 /* Same per class: 0 = TF32x3 GEMM launches (as above), 1 = whole H_eff applies
  * inside Lanczos (FLOPs = 4 D d^2 chi^3 + 4 D^2 d^3 chi^2 per apply, as in
- * ct_dmrg_stats.heff_flops).                                                 */
+ * ct_dmrg_stats.heff_flops), 2 = the applies of class 1 with the largest FLOP
+ * count seen (the centre bond at chi_max).                                   */
 CT_API int ct_kernel_timing_read_class(ct_handle* h, int cls, int64_t* count, double* ms, double* flops);
 
 #ifdef __cplusplus

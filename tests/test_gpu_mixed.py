@@ -233,3 +233,28 @@ def test_dmrg_keep_bases_across_calls(ctx):
     # sweeps at fixed chi_max do not raise the energy beyond truncation noise
     assert st_keep.energy_rayleigh <= st1.energy_rayleigh + 1e-8 * abs(E1)
     assert st_cold.energy_rayleigh <= st_keep.energy_rayleigh + 1e-8 * abs(E1)
+
+
+def test_dmrg_cold_subspace_split(ctx):
+    """cold_power_steps: first visits of large bonds use the subspace split from random rows (two
+    power steps) instead of the Jacobi SVD; after four sweeps the FP64 Rayleigh energy matches the
+    FP64 form to 1e-9 and the sites stay right-canonical."""
+    ct = ct_mod()
+    L = 20
+    mpo_a = oh.spin_half_xxz(L, 1.0)
+    sites, _ = orng.create_random_mps_c_compatible(L, 2, 128, 2)
+    mps_a = od.right_normalize(sites)
+    out = {}
+    for prec, cold in (("fp64", -1), ("tf32x3", 2)):
+        st = ct.DMRGStats()
+        p = ct.DMRGParams(num_sweeps=4, chi_max=128, eps_trunc=0.0, max_krylov_iter=20, krylov_tol=1e-10,
+                          energy_tol=0.0, max_rotations=0, prec=prec, final_rayleigh=True, cold_power_steps=cold)
+        E, mps = ct.dmrg_two_site(ctx, ct.mpo_from_arrays(ctx, mpo_a), ct.mps_from_arrays(ctx, mps_a), p, st)
+        out[prec] = st
+        if prec == "tf32x3":
+            for a in mps.to_numpy()[1:]:
+                mat = a.reshape(a.shape[0], -1)
+                assert np.abs(mat @ mat.T - np.eye(a.shape[0])).max() < 1e-12
+    assert out["tf32x3"].cold_splits > 0
+    e64 = out["fp64"].energy_rayleigh
+    assert abs(out["tf32x3"].energy_rayleigh - e64) <= 1e-9 * abs(e64)
