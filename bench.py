@@ -172,7 +172,9 @@ def hubbard_mode(args):
     power steps); then one FP64 adjoint-gradient pass at the final state
     (environment checkpoints every 7 sites).  Reports sweep seconds per chi,
     the FP64 Rayleigh energy, the gradient residual |grad E| (zero at a
-    stationary state) and peak device memory.  One JSON line.
+    stationary state), |dE/E| of the mixed form against the FP64 form at
+    chi=256 (two sweeps each from the same start, Jacobi first visits in both)
+    and peak device memory.  One JSON line.
     """
     import ctypes as C
     import torch
@@ -202,6 +204,21 @@ def hubbard_mode(args):
                     "subspace_splits": st.subspace_splits, "cold_splits": st.cold_splits,
                     "exact_splits": st.exact_splits, "heff_tflops": st.heff_flops / max(st.seconds_lanczos, 1e-12) / 1e12,
                     "max_discarded": st.max_discarded})
+    # mixed vs FP64 form at chi=256, two sweeps each from the same start with
+    # Jacobi first visits in both (so the difference is precision, not the start)
+    acc_e = {}
+    acc_t = {}
+    for pr in ("fp64", "tf32x3"):
+        mps_c = ct.mps_right_normalize(ctx, ct.mps_from_arrays(ctx, arrays))
+        st_c = ct.DMRGStats()
+        E_c, _ = ct.dmrg_two_site(ctx, mpo, mps_c, ct.DMRGParams(
+            num_sweeps=2, chi_max=ramp[0], eps_trunc=0.0, max_krylov_iter=LANCZOS, krylov_tol=1e-10,
+            energy_tol=0.0, max_rotations=0, prec=pr, final_rayleigh=(pr == "tf32x3")), st_c)
+        acc_e[pr] = st_c.energy_rayleigh if pr == "tf32x3" else E_c
+        acc_t[pr] = st_c.seconds_total / 2
+    accuracy = {"chi_max": ramp[0], "sweeps": 2, "E_fp64": acc_e["fp64"], "E_mixed_rayleigh_fp64": acc_e["tf32x3"],
+                "dE_over_E": abs(acc_e["tf32x3"] - acc_e["fp64"]) / abs(acc_e["fp64"]),
+                "seconds_per_sweep": acc_t}
     sites = [s.tensor.storage[: int(np.prod(s.tensor.shape))].view(*s.tensor.shape) for s in mps.sites]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -214,7 +231,8 @@ def hubbard_mode(args):
     print(json.dumps({"metric": "Fermi-Hubbard L=48 mixed sweep seconds", "unit": "s/sweep", "data": "synthetic",
                       "config": {"workload": "1D Fermi-Hubbard JW L=48 d=4 t=1 U=8 D=6, chi ramp " +
                                  "->".join(str(c) for c in ramp) + ", 2 sweeps each, lanczos=24, eps=0"},
-                      "ramp": log, "gradient": {"energy": Eg, "seconds": tg, "norm": gnorm,
+                      "ramp": log, "accuracy_vs_fp64": accuracy,
+                      "gradient": {"energy": Eg, "seconds": tg, "norm": gnorm,
                                                 "checkpoint_every": 7, "dtype": "f64"},
                       "peak_device_bytes": int(peak_used), "device_bytes_before": int(total - free0)}),
           flush=True)

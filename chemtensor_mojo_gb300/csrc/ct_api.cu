@@ -161,6 +161,8 @@ int ct_destroy(ct_handle* h) {
     for (auto& b : h->basis_cache) cudaFree(b.p);
     for (auto e : h->ktime_ev) cudaEventDestroy(e);
     cudaFree(h->splitk);
+    cudaFree(h->tc_sk_part);
+    cudaFree(h->tc_sk_flag);
     cudaFree(h->d_status);
     cudaFree(h->d_scalars);
     cudaFree(h->d_partials);

@@ -45,6 +45,10 @@ struct ct_handle {
     // FP64 GEMM split-K partial sums (grown on demand, freed by ct_destroy)
     double* splitk = nullptr;
     size_t splitk_cap = 0;   // doubles
+    // stream-K scratch of the persistent tensor-core GEMM (lazily sized, freed by ct_destroy)
+    float* tc_sk_part = nullptr;
+    int* tc_sk_flag = nullptr;
+    int tc_sk_ctas = 0;
     // tensor-core path state
     bool tc_checked = false;
     bool tc_ok = false;

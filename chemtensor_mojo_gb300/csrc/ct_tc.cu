@@ -305,20 +305,75 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
 }
 
-// Persistent variant: one CTA per SM walks tiles t = blockIdx.x, += gridDim.x.
-// The accumulator is double-buffered in TMEM (2 x BN columns), so the epilogue
-// of tile i (TMEM -> global) overlaps the MMAs of tile i+1; the smem ring and
-// its phases run on across tiles.  acc_full[b] is committed by the MMA thread,
-// acc_empty[b] is released by the four epilogue warps.
+// Persistent variant: one CTA per SM walks its work items.  The accumulator is
+// double-buffered in TMEM (2 x BN columns), so the epilogue of item i (TMEM ->
+// global) overlaps the MMAs of item i+1; the smem ring and its phases run on
+// across items.  acc_full[b] is committed by the MMA thread, acc_empty[b] is
+// released by the four epilogue warps.
+//
+// Schedules.  Tile-per-item: CTA c takes tiles c, c + G, ...  Stream-K (sk
+// != null): the tiles x nkb k-blocks are cut into G equal contiguous ranges,
+// one per CTA, so a last partial wave of tiles no longer leaves SMs idle.  A
+// range of at least nkb + 1 k-blocks splits a tile between at most two CTAs:
+// the head (k-blocks from 0) ends CTA c's range, the tail starts CTA c+1's.
+// Each CTA walks its range backwards, tile by tile: its head fragment first,
+// which it stores raw (FP32) to sk->part[c] and flags per TMEM lane quadrant;
+// its tail fragment last, which adds the head that CTA c-1 stored long before
+// (a bounded wait on the flag) -- always in the same order, so the result is
+// deterministic.  All CTAs are resident (one per SM), so no wait depends on a
+// CTA that cannot run.
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+struct TcStreamK {
+    float* part;     // [G][TC_BM][BN] head partials
+    int* flag;       // [G][4]: 1 when quadrant q of CTA c's head partial is stored
+    int64_t total;   // tiles * nkb
+};
+
+struct TcItem {
+    int t, kb0, kb1;
+};
+
+// Number of work items of CTA c, and item j (0-based, in processing order).
+__device__ __forceinline__ int tc_items(const TcStreamK* sk, int tiles, int nkb, int c, int G) {
+    if (!sk) return c < tiles ? (tiles - 1 - c) / G + 1 : 0;
+    const int64_t w0 = (int64_t)c * sk->total / G, w1 = (int64_t)(c + 1) * sk->total / G;
+    if (w1 <= w0) return 0;
+    return (int)((w1 - 1) / nkb - w0 / nkb + 1);
+}
+__device__ __forceinline__ TcItem tc_item(const TcStreamK* sk, int nkb, int c, int G, int j) {
+    TcItem it;
+    if (!sk) {
+        it.t = c + j * G;
+        it.kb0 = 0;
+        it.kb1 = nkb;
+        return it;
+    }
+    const int64_t w0 = (int64_t)c * sk->total / G, w1 = (int64_t)(c + 1) * sk->total / G;
+    const int64_t t = (w1 - 1) / nkb - j;   // backwards: head fragment first, tail last
+    const int64_t b = t * nkb;
+    it.t = (int)t;
+    it.kb0 = (int)(w0 > b ? w0 - b : 0);
+    it.kb1 = (int)(w1 - b < nkb ? w1 - b : nkb);
+    return it;
+}
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 template <int BN, int STAGES>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_gemm_persist_kernel(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                            const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl, int M,
-                           int N, int Kpad, TcEpi epi, const int* skip, int* status) {
+                           int N, int Kpad, TcEpi epi, TcStreamK skd, int use_sk, const int* skip, int* status) {
     using L = TcSmem<BN, STAGES>;
     if (ct_skip(skip)) return;
     extern __shared__ uint8_t tc_smem_raw[];
@@ -334,6 +389,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int tiles_n = (N + BN - 1) / BN;
     const int tiles = tiles_n * ((M + TC_BM - 1) / TC_BM);
     const int nkb = Kpad / TC_BK;
+    const TcStreamK* sk = use_sk ? &skd : nullptr;
+    const int c = blockIdx.x, G = gridDim.x;
+    const int nitems = tc_items(sk, tiles, nkb, c, G);
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -362,9 +420,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (lane == 0) {
             int g = 0;
             bool ok = true;
-            for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
-                const int m0 = (t / tiles_n) * TC_BM, n0 = (t % tiles_n) * BN;
-                for (int kb = 0; kb < nkb; ++kb, ++g) {
+            for (int j = 0; j < nitems && ok; ++j) {
+                const TcItem it = tc_item(sk, nkb, c, G, j);
+                const int m0 = (it.t / tiles_n) * TC_BM, n0 = (it.t % tiles_n) * BN;
+                for (int kb = it.kb0; kb < it.kb1; ++kb, ++g) {
                     const int s = g % STAGES;
                     const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
                     if (g >= STAGES && !mbar_wait(&empty[s], ph ^ 1u, abort_flag)) {
@@ -386,9 +445,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     } else if (warp == 1) {
         if (lane == 0) {
             constexpr uint32_t idesc = idesc_tf32(TC_BM, BN);
-            int g = 0, i = 0;
+            int g = 0;
             bool ok = true;
-            for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++i) {
+            for (int i = 0; i < nitems && ok; ++i) {
+                const TcItem it = tc_item(sk, nkb, c, G, i);
                 const int b = i & 1, u = i >> 1;
                 if (u > 0 && !mbar_wait(&acc_empty[b], (uint32_t)((u - 1) & 1), abort_flag)) {
                     *abort_flag = 1;
@@ -397,7 +457,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
                 tc_fence_after();
                 const uint32_t dt = tmem + (uint32_t)(b * BN);
-                for (int kb = 0; kb < nkb; ++kb, ++g) {
+                for (int kb = it.kb0; kb < it.kb1; ++kb, ++g) {
                     const int s = g % STAGES;
                     const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
                     if (!mbar_wait(&full[s], ph, abort_flag)) {
@@ -414,7 +474,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
                     for (int kk = 0; kk < TC_BK / 8; ++kk) {
                         const uint32_t off = kk * 32;
-                        const uint32_t acc0 = (kb > 0 || kk > 0) ? 1u : 0u;
+                        const uint32_t acc0 = (kb > it.kb0 || kk > 0) ? 1u : 0u;
                         mma_tf32(dt, sw128_desc(a_lo + off), sw128_desc(b_hi + off), idesc, acc0);
                         mma_tf32(dt, sw128_desc(a_hi + off), sw128_desc(b_lo + off), idesc, 1u);
                         mma_tf32(dt, sw128_desc(a_hi + off), sw128_desc(b_hi + off), idesc, 1u);
@@ -427,8 +487,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     } else {
         const int q = warp & 3;
         const int row = q * 32 + lane;
-        int i = 0;
-        for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++i) {
+        for (int i = 0; i < nitems; ++i) {
+            const TcItem it = tc_item(sk, nkb, c, G, i);
             const int b = i & 1, u = i >> 1;
             const bool ok = mbar_wait(&acc_full[b], (uint32_t)(u & 1), abort_flag);
             if (!ok) {
@@ -438,24 +498,54 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             __syncwarp();
             tc_fence_after();
-            const int m0 = (t / tiles_n) * TC_BM, n0 = (t % tiles_n) * BN;
+            const bool head = sk && it.kb0 == 0 && it.kb1 < nkb;   // the rest of this tile is CTA c+1's
+            const bool tail = sk && it.kb0 > 0;                    // CTA c-1 holds this tile's head
+            const float* prev = nullptr;
+            if (tail) {
+                // CTA c-1 stored its head of this tile as its first item; wait for quadrant q
+                const int* f = skd.flag + (int64_t)(c - 1) * 4 + q;
+                bool seen = ld_acquire(f) != 0;
+                if (!seen) {
+                    const unsigned long long t0 = gtimer();
+                    while (!(seen = ld_acquire(f) != 0)) {
+                        if (*abort_flag || gtimer() - t0 > TC_WAIT_NS) break;
+                    }
+                }
+                if (!seen) {
+                    *abort_flag = 1;
+                    ct_set_status(status, CT_ERR_CUDA);
+                    break;
+                }
+                prev = skd.part + ((int64_t)(c - 1) * TC_BM + row) * BN;
+            }
+            const int m0 = (it.t / tiles_n) * TC_BM, n0 = (it.t % tiles_n) * BN;
             const int64_t m = (int64_t)m0 + row;
             const bool mvalid = m < M;
             int64_t rbase = 0;
             if (mvalid) rbase = (m / epi.M0) * epi.sCm1 + (m % epi.M0) * epi.sCm0;
             const uint32_t tq = tmem + (uint32_t)(b * BN) + ((uint32_t)(q * 32) << 16);
+            float* mine = head ? skd.part + ((int64_t)c * TC_BM + row) * BN : nullptr;
 #pragma unroll 1
-            for (int c = 0; c < BN; c += 16) {
+            for (int cc = 0; cc < BN; cc += 16) {
                 uint32_t r[16];
-                tmem_ld16(tq + (uint32_t)c, r);
+                tmem_ld16(tq + (uint32_t)cc, r);
+                if (head) {
+                    // raw partial of k-blocks [0, kb1), every row (the tail CTA masks)
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) mine[cc + j] = __uint_as_float(r[j]);
+                    continue;
+                }
                 if (!mvalid) continue;
+                float v32[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v32[j] = prev ? prev[cc + j] + __uint_as_float(r[j]) : __uint_as_float(r[j]);
                 if (epi.out_fp64) {
                     double* Cd = (double*)epi.C + rbase;
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
-                        const int64_t n = (int64_t)n0 + c + j;
+                        const int64_t n = (int64_t)n0 + cc + j;
                         if (n < N) {
-                            double v = epi.alpha * (double)__uint_as_float(r[j]);
+                            double v = epi.alpha * (double)v32[j];
                             if (epi.beta != 0.0) v = fma(epi.beta, Cd[n], v);
                             Cd[n] = v;
                         }
@@ -464,10 +554,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     float* Cf = (float*)epi.C + rbase;
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
-                        const int64_t n = (int64_t)n0 + c + j;
-                        if (n < N) Cf[n] = (float)epi.alpha * __uint_as_float(r[j]);
+                        const int64_t n = (int64_t)n0 + cc + j;
+                        if (n < N) Cf[n] = (float)epi.alpha * v32[j];
                     }
                 }
+            }
+            if (head) {
+                __syncwarp();
+                __threadfence();
+                if (lane == 0) st_release(skd.flag + (int64_t)c * 4 + q, 1);
             }
             tc_fence_before();
             __syncwarp();
@@ -705,6 +800,17 @@ bool tc_use_persistent() {
     return v;
 }
 
+// stream-K schedule of the persistent kernel only on request (CTDMRG_TC_STREAM_K=1): measured
+// on the H_eff shapes it did not pay (4096x1024x5120: 0.192 vs 0.191 ms; 5120x4096x1024:
+// 0.242 vs 0.217 ms), the contiguous per-CTA ranges lose the L2 reuse of neighbouring tiles
+bool tc_use_stream_k() {
+    static const bool v = [] {
+        const char* e = getenv("CTDMRG_TC_STREAM_K");
+        return e && e[0] == '1';
+    }();
+    return v;
+}
+
 struct SplitOperand {
     float* hi = nullptr;
     float* lo = nullptr;
@@ -735,8 +841,30 @@ int tc_gemm_launch(ct_handle* h, const SplitOperand& A, const SplitOperand& B, i
     CT_TRY(ct_ktime_begin(h, KT_TC_GEMM, 2.0 * (double)M * (double)N * (double)A.ldk, &slot));
     if (tc_use_persistent()) {
         const int64_t grid = tiles < h->num_sms ? tiles : h->num_sms;
+        // stream-K when the tiles leave a partial last wave and every CTA's share
+        // of k-blocks covers at least one whole tile (so a tile has at most two owners)
+        const int64_t nkb = A.ldk / TC_BK;
+        TcStreamK sk{};
+        sk.total = tiles * nkb;
+        const bool use_sk = tc_use_stream_k() && tiles > grid && (tiles % grid) != 0 && sk.total / grid >= nkb + 1;
+        if (use_sk) {
+            if (h->tc_sk_ctas < grid) {
+                if (h->tc_sk_part) cudaFree(h->tc_sk_part);
+                if (h->tc_sk_flag) cudaFree(h->tc_sk_flag);
+                h->tc_sk_part = nullptr;
+                h->tc_sk_flag = nullptr;
+                h->tc_sk_ctas = 0;
+                CT_CUDA(h, cudaMalloc((void**)&h->tc_sk_part, (size_t)grid * TC_BM * GEMM_BN * sizeof(float)));
+                CT_CUDA(h, cudaMalloc((void**)&h->tc_sk_flag, (size_t)grid * 4 * sizeof(int)));
+                h->tc_sk_ctas = (int)grid;
+            }
+            CT_CUDA(h, cudaMemsetAsync(h->tc_sk_flag, 0, (size_t)grid * 4 * sizeof(int), h->stream));
+            sk.part = h->tc_sk_part;
+            sk.flag = h->tc_sk_flag;
+        }
         tc_gemm_persist_kernel<GEMM_BN, GEMM_STAGES><<<(unsigned)grid, TC_THREADS, L::TOTAL, h->stream>>>(
-            ta_h, ta_l, tb_h, tb_l, (int)M, (int)N, (int)A.ldk, epi, skip, h->d_status); ct_note_launch();
+            ta_h, ta_l, tb_h, tb_l, (int)M, (int)N, (int)A.ldk, epi, sk, use_sk ? 1 : 0, skip, h->d_status);
+        ct_note_launch();
     } else {
         dim3 grid((unsigned)ct_cdiv(N, GEMM_BN), (unsigned)ct_cdiv(M, TC_BM));
         if (grid.y > 65535) return CT_ERR_UNSUPPORTED;

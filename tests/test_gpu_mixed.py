@@ -258,3 +258,48 @@ def test_dmrg_cold_subspace_split(ctx):
     assert out["tf32x3"].cold_splits > 0
     e64 = out["fp64"].energy_rayleigh
     assert abs(out["tf32x3"].energy_rayleigh - e64) <= 1e-9 * abs(e64)
+
+
+@pytest.mark.parametrize("l2r", [True, False])
+def test_svd_split_warm_entry(ctx, l2r):
+    """ct_svd_split_warm (C ABI): from a slightly perturbed exact basis, the split is accepted,
+    the canonical factor is orthonormal to 1e-12, A B reproduces the rank-chi truncation of theta
+    to the optimal discarded weight (within the TF32x3 resolution of the residual), and the kept
+    basis it writes spans the same subspace as the canonical factor."""
+    import ctypes as C
+    import torch
+    ct = ct_mod()
+    Dl, d, Dr, c = 256, 2, 256, 200
+    m, n = Dl * d, d * Dr
+    rng = np.random.default_rng(7)
+    U, _ = np.linalg.qr(rng.standard_normal((m, m)))
+    V, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = np.exp(-0.02 * np.arange(m))
+    M = (U * s) @ V.T
+    X0 = (V[:, :c] if l2r else U[:, :c]) + 1e-6 * rng.standard_normal(((n if l2r else m), c))
+    X, _ = np.linalg.qr(X0)
+    dev = ctx.torch_device
+    th = torch.from_numpy(M.reshape(Dl, d, d, Dr).copy()).to(dev)
+    Xd = torch.from_numpy(np.ascontiguousarray(X.T)).to(dev)
+    bout = torch.zeros(c * (m if l2r else n), dtype=torch.float64, device=dev)
+    A = torch.zeros(m * c, dtype=torch.float64, device=dev)
+    B = torch.zeros(c * n, dtype=torch.float64, device=dev)
+    acc, disc = C.c_int(), C.c_double()
+    piv = (C.c_double * 3)()
+    ctx.call("ct_svd_split_warm", C.c_void_p(th.data_ptr()), Dl, d, Dr, c, int(l2r), C.c_void_p(Xd.data_ptr()), 0,
+             C.c_void_p(bout.data_ptr()), C.c_void_p(A.data_ptr()), C.c_void_p(B.data_ptr()), C.byref(acc),
+             C.byref(disc), piv)
+    torch.cuda.synchronize()
+    assert acc.value == 1 and piv[2] == 0
+    a = A.cpu().numpy().reshape(m, c)
+    b = B.cpu().numpy().reshape(c, n)
+    can = a.T @ a if l2r else b @ b.T
+    assert np.abs(can - np.eye(c)).max() < 1e-12
+    opt = np.sum(s[c:] ** 2) / np.sum(s ** 2)
+    err = np.sum((a @ b - M) ** 2) / np.sum(s ** 2)
+    assert err <= opt * (1 + 1e-3) + 1e-9
+    assert abs(disc.value - err) <= 1e-9
+    kept = bout.cpu().numpy().reshape(c, -1)
+    canon = a.T if l2r else b
+    # same row space: projecting the kept rows on the canonical rows loses nothing
+    assert np.abs(kept @ canon.T @ canon - kept).max() < 1e-10
