@@ -607,7 +607,7 @@ def main():
         peak = bf16 / 6.0
         line["roofline"] = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                             "traffic": TC_GEMM_TRAFFIC_BYTES,
-                            "kernel": "tc_gemm_persist_kernel<128,3> (TF32x3, tcgen05)",
+                            "kernel": "tc_gemm_persist_kernel<128,3> and <256,2> (TF32x3, tcgen05; tile width chosen per shape)",
                             "launches": kt["launches"], "avg_launch_ms": kt["ms"] / kt["launches"],
                             "flops_per_launch": kt["flops"] / kt["launches"],
                             "share_of_timed_region": kt["ms"] * 1e-3 / max(dev_s, 1e-12),

@@ -48,7 +48,7 @@ struct ct_handle {
     // stream-K scratch of the persistent tensor-core GEMM (lazily sized, freed by ct_destroy)
     float* tc_sk_part = nullptr;
     int* tc_sk_flag = nullptr;
-    int tc_sk_ctas = 0;
+    int64_t tc_sk_floats = 0;       // floats held by tc_sk_part
     // tensor-core path state
     bool tc_checked = false;
     bool tc_ok = false;
@@ -89,9 +89,11 @@ enum {
     SC_BETA = 512,         // Lanczos beta (<= 128)
     SC_MISC = 768,         // scratch (<= 128): Thomas coefficients, reorthogonalisation
     SC_SVD_FROB2 = 968,    // mixed SVD: |M|_F^2
-    SC_SPLIT_PIV = 970     // subspace split: smallest Cholesky pivot of each pass (2)
+    SC_SPLIT_PIV = 970,    // subspace split: smallest Cholesky pivot of each pass (2)
+    SC_ORTH_EMAX = 972     // subspace split: largest |Q Q^T - I| seen by the second pass
 };
-static_assert(SC_MISC + CT_MAX_KRYLOV_SLOTS <= SC_SVD_FROB2 && SC_SPLIT_PIV + 2 <= CT_NSCALARS,
+static_assert(SC_MISC + CT_MAX_KRYLOV_SLOTS <= SC_SVD_FROB2 && SC_SPLIT_PIV + 2 <= SC_ORTH_EMAX &&
+                  SC_ORTH_EMAX + 1 <= CT_NSCALARS,
               "scalar slots overlap or overflow d_scalars");
 // int slots inside d_flags
 enum { FL_STOP = 0, FL_NUMITER = 1, FL_ROT = 2, FL_CHI = 3, FL_TMP = 4, FL_CNT = 8 };

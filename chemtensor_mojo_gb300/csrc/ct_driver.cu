@@ -249,8 +249,10 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
                     last_split_subspace = ok;
                     if (P->verbose >= 2)
                         fprintf(stderr,
-                                "bond %d %s: subspace split %s (pivots %.3g %.3g%s, kept %.12g of %.12g)\n", i,
-                                l2r ? "L->R" : "R->L", ok ? "accepted" : "refused", so.min_pivot, so.min_pivot2,
+                                "bond %d %s: subspace split %s (pivot %.3g, pass-2 deviation %.2g%s, kept %.12g of "
+                                "%.12g)\n",
+                                i, l2r ? "L->R" : "R->L", ok ? "accepted" : "refused", so.min_pivot,
+                                1.0 - so.min_pivot2,
                                 so.chol_fail ? ", Cholesky failed" : "", so.sum_s2_kept, so.sum_s2_all);
                     if (ok) {
                         st.subspace_splits++;

@@ -20,7 +20,14 @@
 // (optionally after power steps X <- orth(orth(X theta^T) theta)).
 //
 // orth() is CholeskyQR2 on row-normalised rows: G = Z Z^T, G = L L^T,
-// Z <- L^{-1} Z, twice, in FP64.  It is triangular (Gram-Schmidt order), so
+// Z <- L^{-1} Z in FP64, then a second pass on the nearly orthonormal rows Q.
+// The second pass computes E = Q Q^T - I in FP64 and, when |E| <= 1e-4, applies
+// the first-order inverse Cholesky factor of I + E instead of factorising it:
+//   L = I + Phi(E) + O(E^2),  Phi(E) = strict_lower(E) + diag(E) / 2,
+//   Q <- (I - Phi(E)) Q   (a TF32x3 GEMM: the correction is ~|E| small, so its
+//                          rounding is ~1e-7 |E|; repeated once if |E| > 1e-7)
+// which leaves |Q Q^T - I| = O(E^2) and keeps the triangular order.  Larger E
+// takes the full Cholesky pass.  It is triangular (Gram-Schmidt order), so
 // rows that start close to singular vectors ordered by weight stay ordered and
 // close to them; a symmetric orthogonalisation would keep any rotation between
 // the basis and the singular vectors and the next product X theta^T would
@@ -151,6 +158,10 @@ __global__ void __launch_bounds__(256) chol_diag_kernel(double* G, double* Linv,
     }
 }
 
+__global__ void split_piv_set_kernel(unsigned long long* piv, double p) {
+    if (threadIdx.x == 0) atomicMin(piv, (unsigned long long)__double_as_longlong(p < 0.0 ? 0.0 : p));
+}
+
 // running minima of the two passes' pivots start at 1e300; the failure flag at 0
 __global__ void split_flags_init_kernel(unsigned long long* piv, int* fail) {
     if (threadIdx.x < 2) piv[threadIdx.x] = (unsigned long long)__double_as_longlong(1.0e300);
@@ -225,12 +236,80 @@ int chol_inv(ct_handle* h, double* G, double* Linv, int64_t ld, int64_t n, doubl
     return CT_OK;
 }
 
+// F = -Phi(G - I) (see the header) from G's lower triangle, F c x c with leading
+// dimension c; the largest |G - I| of the lower triangle -> *emax (bit pattern of
+// a non-negative double, atomicMax; a NaN counts as 1e300).
+__global__ void orth_correction_kernel(const double* G, int64_t ldg, int64_t c, double* F,
+                                       unsigned long long* emax) {
+    double m = 0.0;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < c * c;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / c, j = t % c;
+        double f = 0.0;
+        if (j <= i) {
+            const double e = G[i * ldg + j] - (i == j ? 1.0 : 0.0);
+            const double a = fabs(e);
+            if (!(a <= m)) m = (a == a) ? a : 1.0e300;
+            f = (i == j) ? -0.5 * e : -e;
+        }
+        F[t] = f;
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(emax, (unsigned long long)__double_as_longlong(m));
+}
+
 struct OrthBufs {
     double* G;      // cp x cp
     double* Linv;   // cp x cp
     double* S;      // (cp / 2)^2 + CH_NB^2
     int64_t cp;
 };
+
+constexpr double ORTH_CORR_MAX = 1e-4;    // largest |Q Q^T - I| the first-order step takes
+constexpr double ORTH_CORR_DONE = 1e-7;   // one step suffices below this (leaves ~E^2)
+
+// Second pass by first-order correction: rows Q (c x len, nearly orthonormal)
+// -> out.  *done is false (out untouched beyond scratch use) when |E| exceeds
+// ORTH_CORR_MAX and the caller runs the Cholesky pass.  1 - |E| of the first
+// step goes to *piv (the smallest pivot of a Cholesky pass is ~ 1 - |E|).
+int orth_correct(ct_handle* h, Arena& ar, const double* Q, double* out, int64_t c, int64_t len, const OrthBufs& ob,
+                 unsigned long long* piv, bool* done) {
+    *done = false;
+    const size_t mark = ar.off;
+    unsigned long long* d_emax = (unsigned long long*)(h->d_scalars + SC_ORTH_EMAX);
+    const double* cur = Q;
+    for (int step = 0; step < 2; ++step) {
+        CT_CUDA(h, cudaMemsetAsync(d_emax, 0, sizeof(unsigned long long), h->stream));
+        CT_TRY(fac_gemm(h, c, c, len, cur, len, cur, len, 1, ob.G, ob.cp, 1.0, 0.0, 1));   // lower tiles of Q Q^T
+        orth_correction_kernel<<<grid_n(h, c * c), 256, 0, h->stream>>>(ob.G, ob.cp, c, ob.Linv, d_emax);
+        ct_note_launch();
+        CT_LAUNCH_CHECK(h);
+        unsigned long long bits = 0;
+        CT_CUDA(h, cudaMemcpyAsync(&bits, d_emax, sizeof(bits), cudaMemcpyDeviceToHost, h->stream));
+        CT_CUDA(h, cudaStreamSynchronize(h->stream));
+        double emax;
+        memcpy(&emax, &bits, sizeof(emax));
+        if (step == 0) {
+            if (!(emax <= ORTH_CORR_MAX)) return CT_OK;
+            const double p = 1.0 - emax;
+            split_piv_set_kernel<<<1, 32, 0, h->stream>>>(piv, p);
+            ct_note_launch();
+            CT_LAUNCH_CHECK(h);
+        } else if (!(emax <= ORTH_CORR_MAX)) {
+            return CT_OK;   // the step did not converge: Cholesky pass from Q
+        }
+        // out = cur + F cur   (out may alias cur only through the copy below)
+        if (out != cur)
+            CT_CUDA(h, cudaMemcpyAsync(out, cur, (size_t)(c * len) * sizeof(double), cudaMemcpyDeviceToDevice,
+                                       h->stream));
+        CT_TRY(ct_tc_gemm(h, ar, 0, 0, c, len, c, 1.0, ob.Linv, c, cur, len, 1.0, out, len));
+        ar.off = mark;
+        cur = out;
+        if (emax <= ORTH_CORR_DONE) break;
+    }
+    *done = true;
+    return CT_OK;
+}
 
 // Orthonormalise the c rows of Z (c x len) by CholeskyQR in FP64; the result
 // goes to W (c x len) and Z is scratch.  The optional second pass makes the rows
@@ -244,6 +323,14 @@ int orth_rows(ct_handle* h, Arena& ar, double* Z, double* W, int64_t c, int64_t 
     double* src = Z;
     double* dst = W;
     for (int pass = 0; pass < (two_pass ? 2 : 1); ++pass) {
+        if (pass == 1) {
+            bool done = false;
+            CT_TRY(orth_correct(h, ar, src, dst, c, len, ob, d_minpiv + 1, &done));
+            if (done) {
+                src = dst;   // the corrected rows
+                break;
+            }
+        }
         chol_prepare_kernel<<<grid_n(h, cp * cp), 256, 0, h->stream>>>(ob.G, ob.Linv, c, cp); ct_note_launch();
         CT_LAUNCH_CHECK(h);
         CT_TRY(fac_gemm(h, c, c, len, src, len, src, len, 1, ob.G, cp, 1.0, 0.0, 1));

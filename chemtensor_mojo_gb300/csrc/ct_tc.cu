@@ -152,6 +152,7 @@ struct TcEpi {
     int64_t M0;          // row m -> (m / M0) * sCm1 + (m % M0) * sCm0
     int64_t sCm1, sCm0;
     double alpha, beta;  // C = alpha * acc + beta * C
+    int vec;             // set by the launcher: C and both row strides 16-byte aligned
 };
 
 template <int BN, int STAGES>
@@ -539,6 +540,33 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 float v32[16];
 #pragma unroll
                 for (int j = 0; j < 16; ++j) v32[j] = prev ? prev[cc + j] + __uint_as_float(r[j]) : __uint_as_float(r[j]);
+                const int64_t nb = (int64_t)n0 + cc;
+                if (epi.vec && nb + 16 <= N) {
+                    // 16-byte stores: a warp writes 32 rows x 64 B (FP32) or 128 B (FP64)
+                    // per group of 4 / 8 instructions instead of one 4-byte word per row
+                    if (epi.out_fp64) {
+                        double2* Cd = (double2*)((double*)epi.C + rbase + nb);
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            double2 o;
+                            o.x = epi.alpha * (double)v32[2 * j];
+                            o.y = epi.alpha * (double)v32[2 * j + 1];
+                            if (epi.beta != 0.0) {
+                                const double2 c0 = Cd[j];
+                                o.x = fma(epi.beta, c0.x, o.x);
+                                o.y = fma(epi.beta, c0.y, o.y);
+                            }
+                            Cd[j] = o;
+                        }
+                    } else {
+                        float4* Cf = (float4*)((float*)epi.C + rbase + nb);
+                        const float a = (float)epi.alpha;
+#pragma unroll
+                        for (int j = 0; j < 4; ++j)
+                            Cf[j] = make_float4(a * v32[4 * j], a * v32[4 * j + 1], a * v32[4 * j + 2], a * v32[4 * j + 3]);
+                    }
+                    continue;
+                }
                 if (epi.out_fp64) {
                     double* Cd = (double*)epi.C + rbase;
 #pragma unroll
@@ -788,8 +816,21 @@ int make_map(ct_handle* h, CUtensorMap* m, const float* base, int64_t rows, int6
     return CT_OK;
 }
 
-constexpr int GEMM_BN = 128;
-constexpr int GEMM_STAGES = 3;
+// Tile shapes of the GEMM: 128 x 128 with a 3-stage ring (64 KB stages), or 128 x 256 with a
+// 2-stage ring (96 KB stages).  The wide tile reads 25% fewer operand bytes from shared memory
+// and L2 per MMA flop; the narrow one leaves smaller partial waves.  CTDMRG_TC_BN=128 or 256
+// forces one; otherwise tc_pick_bn chooses per shape.
+constexpr int GEMM_STAGES_N = 3;
+constexpr int GEMM_STAGES_W = 2;
+
+// read on every launch (one environment scan, next to a launch of tens of microseconds), so a
+// test can switch tile shapes inside one process
+int tc_bn_mode() {
+    const char* e = getenv("CTDMRG_TC_BN");
+    if (!e) return 0;
+    const int b = atoi(e);
+    return (b == 128 || b == 256) ? b : 0;
+}
 
 // persistent kernel by default; CTDMRG_TC_TILE_PER_CTA=1 selects the one-tile-per-CTA kernel
 bool tc_use_persistent() {
@@ -811,34 +852,45 @@ bool tc_use_stream_k() {
     return v;
 }
 
+// Wide tiles when their whole waves cost less.  Time per tile ~ BN at equal K; at K <= 2048 the
+// wide tile's fixed per-tile cost (pipeline fill, epilogue) is spread over twice the MMAs, measured
+// as 1.12x the narrow tile's rate per flop (5120x4096x1024: 0.164 vs 0.166 ms; 2048x2048x1024:
+// 0.037 vs 0.041 ms); at K = 5120 both run at the same rate per flop.
+int tc_pick_bn(int64_t M, int64_t N, int64_t K, int num_sms) {
+    const int mode = tc_bn_mode();
+    if (mode) return mode;
+    if (N <= 128) return 128;
+    const int64_t tm = ct_cdiv(M, TC_BM);
+    const int64_t w128 = ct_cdiv(tm * ct_cdiv(N, 128), num_sms);
+    const int64_t w256 = ct_cdiv(tm * ct_cdiv(N, 256), num_sms);
+    const double wide_speed = K <= 2048 ? 1.12 : 1.0;
+    return (double)w256 * 256.0 / wide_speed < (double)w128 * 128.0 ? 256 : 128;
+}
+
 struct SplitOperand {
     float* hi = nullptr;
     float* lo = nullptr;
     int64_t rows = 0, ldk = 0;
 };
 
-int tc_gemm_launch(ct_handle* h, const SplitOperand& A, const SplitOperand& B, int64_t M, int64_t N,
-                   const TcEpi& epi, const int* skip) {
-    if (A.ldk != B.ldk) return CT_ERR_SHAPE;
-    if (M <= 0 || N <= 0) return CT_OK;
-    if (M > (1ll << 31) || N > (1ll << 31)) return CT_ERR_UNSUPPORTED;
+template <int BN, int STAGES>
+int tc_gemm_run(ct_handle* h, const SplitOperand& A, const SplitOperand& B, int64_t M, int64_t N,
+                const TcEpi& epi, const int* skip) {
     CUtensorMap ta_h, ta_l, tb_h, tb_l;
     CT_TRY(make_map(h, &ta_h, A.hi, A.rows, A.ldk, TC_BM));
     CT_TRY(make_map(h, &ta_l, A.lo, A.rows, A.ldk, TC_BM));
-    CT_TRY(make_map(h, &tb_h, B.hi, B.rows, B.ldk, GEMM_BN));
-    CT_TRY(make_map(h, &tb_l, B.lo, B.rows, B.ldk, GEMM_BN));
-    using L = TcSmem<GEMM_BN, GEMM_STAGES>;
+    CT_TRY(make_map(h, &tb_h, B.hi, B.rows, B.ldk, BN));
+    CT_TRY(make_map(h, &tb_l, B.lo, B.rows, B.ldk, BN));
+    using L = TcSmem<BN, STAGES>;
     static int attr_dev = -1;
     if (attr_dev != h->device) {
-        CT_CUDA(h, cudaFuncSetAttribute(tc_gemm_kernel<GEMM_BN, GEMM_STAGES>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, L::TOTAL));
-        CT_CUDA(h, cudaFuncSetAttribute(tc_gemm_persist_kernel<GEMM_BN, GEMM_STAGES>,
+        CT_CUDA(h, cudaFuncSetAttribute(tc_gemm_kernel<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        L::TOTAL));
+        CT_CUDA(h, cudaFuncSetAttribute(tc_gemm_persist_kernel<BN, STAGES>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, L::TOTAL));
         attr_dev = h->device;
     }
-    const int64_t tiles = ct_cdiv(N, GEMM_BN) * ct_cdiv(M, TC_BM);
-    int slot = -1;
-    CT_TRY(ct_ktime_begin(h, KT_TC_GEMM, 2.0 * (double)M * (double)N * (double)A.ldk, &slot));
+    const int64_t tiles = ct_cdiv(N, BN) * ct_cdiv(M, TC_BM);
     if (tc_use_persistent()) {
         const int64_t grid = tiles < h->num_sms ? tiles : h->num_sms;
         // stream-K when the tiles leave a partial last wave and every CTA's share
@@ -848,30 +900,50 @@ int tc_gemm_launch(ct_handle* h, const SplitOperand& A, const SplitOperand& B, i
         sk.total = tiles * nkb;
         const bool use_sk = tc_use_stream_k() && tiles > grid && (tiles % grid) != 0 && sk.total / grid >= nkb + 1;
         if (use_sk) {
-            if (h->tc_sk_ctas < grid) {
+            const size_t need = (size_t)grid * TC_BM * BN;
+            if (h->tc_sk_floats < (int64_t)need) {
                 if (h->tc_sk_part) cudaFree(h->tc_sk_part);
                 if (h->tc_sk_flag) cudaFree(h->tc_sk_flag);
                 h->tc_sk_part = nullptr;
                 h->tc_sk_flag = nullptr;
-                h->tc_sk_ctas = 0;
-                CT_CUDA(h, cudaMalloc((void**)&h->tc_sk_part, (size_t)grid * TC_BM * GEMM_BN * sizeof(float)));
-                CT_CUDA(h, cudaMalloc((void**)&h->tc_sk_flag, (size_t)grid * 4 * sizeof(int)));
-                h->tc_sk_ctas = (int)grid;
+                h->tc_sk_floats = 0;
+                CT_CUDA(h, cudaMalloc((void**)&h->tc_sk_part, need * sizeof(float)));
+                CT_CUDA(h, cudaMalloc((void**)&h->tc_sk_flag, (size_t)h->num_sms * 4 * sizeof(int)));
+                h->tc_sk_floats = (int64_t)need;
             }
             CT_CUDA(h, cudaMemsetAsync(h->tc_sk_flag, 0, (size_t)grid * 4 * sizeof(int), h->stream));
             sk.part = h->tc_sk_part;
             sk.flag = h->tc_sk_flag;
         }
-        tc_gemm_persist_kernel<GEMM_BN, GEMM_STAGES><<<(unsigned)grid, TC_THREADS, L::TOTAL, h->stream>>>(
+        tc_gemm_persist_kernel<BN, STAGES><<<(unsigned)grid, TC_THREADS, L::TOTAL, h->stream>>>(
             ta_h, ta_l, tb_h, tb_l, (int)M, (int)N, (int)A.ldk, epi, sk, use_sk ? 1 : 0, skip, h->d_status);
         ct_note_launch();
     } else {
-        dim3 grid((unsigned)ct_cdiv(N, GEMM_BN), (unsigned)ct_cdiv(M, TC_BM));
+        dim3 grid((unsigned)ct_cdiv(N, BN), (unsigned)ct_cdiv(M, TC_BM));
         if (grid.y > 65535) return CT_ERR_UNSUPPORTED;
-        tc_gemm_kernel<GEMM_BN, GEMM_STAGES><<<grid, TC_THREADS, L::TOTAL, h->stream>>>(
+        tc_gemm_kernel<BN, STAGES><<<grid, TC_THREADS, L::TOTAL, h->stream>>>(
             ta_h, ta_l, tb_h, tb_l, (int)M, (int)N, (int)A.ldk, epi, skip, h->d_status); ct_note_launch();
     }
     CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int tc_gemm_launch(ct_handle* h, const SplitOperand& A, const SplitOperand& B, int64_t M, int64_t N,
+                   const TcEpi& epi, const int* skip) {
+    if (A.ldk != B.ldk) return CT_ERR_SHAPE;
+    if (M <= 0 || N <= 0) return CT_OK;
+    if (M > (1ll << 31) || N > (1ll << 31)) return CT_ERR_UNSUPPORTED;
+    TcEpi e = epi;
+    {
+        const int64_t per16 = e.out_fp64 ? 2 : 4;   // elements per 16 bytes
+        e.vec = ((uintptr_t)e.C % 16 == 0) && e.sCm0 % per16 == 0 && (e.M0 >= M || e.sCm1 % per16 == 0);
+    }
+    int slot = -1;
+    CT_TRY(ct_ktime_begin(h, KT_TC_GEMM, 2.0 * (double)M * (double)N * (double)A.ldk, &slot));
+    const int bn = tc_pick_bn(M, N, A.ldk, h->num_sms);
+    const int rc = bn == 256 ? tc_gemm_run<256, GEMM_STAGES_W>(h, A, B, M, N, e, skip)
+                             : tc_gemm_run<128, GEMM_STAGES_N>(h, A, B, M, N, e, skip);
+    CT_TRY(rc);
     CT_TRY(ct_ktime_end(h, slot));
     return CT_OK;
 }

@@ -52,6 +52,27 @@ def test_tc_gemm_matches_fp64(ctx, m, n, k, ta, tb):
     assert rel(tC.to_numpy(), ref) < TOL
 
 
+@pytest.mark.parametrize("bn", ["128", "256"])
+@pytest.mark.parametrize("m,n,k", [(128, 256, 32), (300, 520, 96), (130, 1000, 333), (1024, 768, 256)])
+def test_tc_gemm_tile_widths(ctx, monkeypatch, bn, m, n, k):
+    """Both tile shapes of the TF32x3 GEMM (128x128 / 3 stages, 128x256 / 2 stages), forced
+    through CTDMRG_TC_BN, on ragged M, N and K."""
+    import ctypes as C
+    import torch
+    monkeypatch.setenv("CTDMRG_TC_BN", bn)
+    rng = np.random.default_rng(m * 7 + n + k)
+    A = rng.standard_normal((m, k))
+    B = rng.standard_normal((k, n))
+    Cin = rng.standard_normal((m, n))
+    ref = 1.5 * (A @ B) + 0.25 * Cin
+    tA, tB, tC = dt(ctx, A), dt(ctx, B), dt(ctx, Cin)
+    ctx.call("ct_gemm", 1, 0, 0, C.c_int64(m), C.c_int64(n), C.c_int64(k), C.c_double(1.5),
+             C.c_void_p(tA.storage.data_ptr()), C.c_int64(k), C.c_void_p(tB.storage.data_ptr()), C.c_int64(n),
+             C.c_double(0.25), C.c_void_p(tC.storage.data_ptr()), C.c_int64(n))
+    torch.cuda.synchronize()
+    assert rel(tC.to_numpy(), ref) < TOL
+
+
 def test_dense_tensor_dot_tf32x3(ctx):
     ct = ct_mod()
     rng = np.random.default_rng(11)
