@@ -91,6 +91,11 @@ SIGNATURES = {
                          C.POINTER(ct_dmrg_stats)],
     "ct_mps_right_normalize": [P, I32, I32, C.POINTER(I64), PP],
     "ct_mps_expectation": [P, I32, I32, I32, C.POINTER(I64), PP, C.POINTER(I64), PP, C.POINTER(D), C.POINTER(D)],
+    "ct_env_left2": [P, I32, P, P, P, P, P, I64, I64, I64, I64, I64, I64, I64],
+    "ct_mps_expectation2": [P, I32, I32, I32, C.POINTER(I64), PP, C.POINTER(I64), PP, C.POINTER(I64), PP,
+                            C.POINTER(D)],
+    "ct_mpo_compose_site": [P, P, P, P, I64, I64, I64, I64, I64, I64, I64],
+    "ct_apply_mpo_site": [P, P, P, P, I64, I64, I64, I64, I64, I64],
     "ct_random_mps_host": [I32, I32, I32, C.c_uint64, C.POINTER(I64), PP],
     "ct_rng_randnf_host": [C.c_uint64, I64, C.POINTER(C.c_float)],
     "ct_tc_gemm_time": [P, I64, I64, I64, I32, C.POINTER(D)],

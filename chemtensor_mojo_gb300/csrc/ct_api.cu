@@ -388,6 +388,65 @@ int ct_env_left(ct_handle* h, int prec, const double* Lprev, const double* A, co
     return ct_env_left_run(h, ar, prec, Lprev, A, W, Lnext, Dl, d, Dr, wL, wR);
 }
 
+int ct_env_left2(ct_handle* h, int prec, const double* Lprev, const double* A_ket, const double* A_bra,
+                 const double* W, double* Lnext, int64_t Dl_ket, int64_t Dl_bra, int64_t d, int64_t Dr_ket,
+                 int64_t Dr_bra, int64_t wL, int64_t wR) {
+    CT_NULLCHK(h, h);
+    if (prec != CT_PREC_FP64) {
+        ct_seterr(h, "ct_env_left2: only the FP64 form takes a bra different from the ket");
+        return CT_ERR_UNSUPPORTED;
+    }
+    CT_NULLCHK(h, Lprev);
+    CT_NULLCHK(h, A_ket);
+    CT_NULLCHK(h, A_bra);
+    CT_NULLCHK(h, Lnext);
+    CT_POSCHK(h, Dl_ket);
+    CT_POSCHK(h, Dl_bra);
+    CT_POSCHK(h, d);
+    CT_POSCHK(h, Dr_ket);
+    CT_POSCHK(h, Dr_bra);
+    CT_POSCHK(h, wL);
+    CT_POSCHK(h, wR);
+    if (!W && (wL != 1 || wR != 1)) {
+        ct_seterr(h, "ct_env_left2: without an MPO site wL and wR must be 1");
+        return CT_ERR_SHAPE;
+    }
+    CT_TRY(ct_reserve(h, ct_env2_ws_bytes(Dl_ket, Dl_bra, d, Dr_ket, Dr_bra, wL, wR)));
+    Arena ar(h);
+    return ct_env_left2_run(h, ar, Lprev, A_ket, A_bra, W, Lnext, Dl_ket, Dl_bra, d, Dr_ket, Dr_bra, wL, wR);
+}
+
+int ct_mpo_compose_site(ct_handle* h, const double* Wa, const double* Wb, double* Wout, int64_t wLa,
+                        int64_t d_in, int64_t d_mid, int64_t wRa, int64_t wLb, int64_t d_out, int64_t wRb) {
+    CT_NULLCHK(h, h);
+    CT_NULLCHK(h, Wa);
+    CT_NULLCHK(h, Wb);
+    CT_NULLCHK(h, Wout);
+    CT_POSCHK(h, wLa);
+    CT_POSCHK(h, d_in);
+    CT_POSCHK(h, d_mid);
+    CT_POSCHK(h, wRa);
+    CT_POSCHK(h, wLb);
+    CT_POSCHK(h, d_out);
+    CT_POSCHK(h, wRb);
+    return ct_mpo_compose_launch(h, Wa, Wb, Wout, wLa, d_in, d_mid, wRa, wLb, d_out, wRb);
+}
+
+int ct_apply_mpo_site(ct_handle* h, const double* A, const double* W, double* out, int64_t Dl, int64_t d,
+                      int64_t Dr, int64_t wL, int64_t d_out, int64_t wR) {
+    CT_NULLCHK(h, h);
+    CT_NULLCHK(h, A);
+    CT_NULLCHK(h, W);
+    CT_NULLCHK(h, out);
+    CT_POSCHK(h, Dl);
+    CT_POSCHK(h, d);
+    CT_POSCHK(h, Dr);
+    CT_POSCHK(h, wL);
+    CT_POSCHK(h, d_out);
+    CT_POSCHK(h, wR);
+    return ct_apply_mpo_launch(h, A, W, out, Dl, d, Dr, wL, d_out, wR);
+}
+
 int ct_env_right(ct_handle* h, int prec, const double* Rnext, const double* A, const double* W, double* Rprev,
                  int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR) {
     CT_NULLCHK(h, h);

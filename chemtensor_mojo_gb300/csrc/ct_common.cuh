@@ -220,6 +220,11 @@ int ct_build_w12(ct_handle* h, const double* W1, const double* W2, double* W12t,
                  int64_t d, int64_t wM, int64_t wR);
 int ct_build_wt_left(ct_handle* h, const double* W, double* Wt, int64_t wL, int64_t d, int64_t wR);
 int ct_build_wt_right(ct_handle* h, const double* W, double* Wt, int64_t wL, int64_t d, int64_t wR);
+// MPO x MPO and MPO x MPS site products (ct_mpo.cu)
+int ct_mpo_compose_launch(ct_handle* h, const double* Wa, const double* Wb, double* Wout, int64_t wLa,
+                          int64_t d_in, int64_t d_mid, int64_t wRa, int64_t wLb, int64_t d_out, int64_t wRb);
+int ct_apply_mpo_launch(ct_handle* h, const double* A, const double* W, double* out, int64_t Dl, int64_t d,
+                        int64_t Dr, int64_t wL, int64_t d_out, int64_t wR);
 
 // vector kernels (ct_vec.cu)
 int ct_reduce_dot(ct_handle* h, int64_t n, const double* x, const double* y, double* d_out,
@@ -232,6 +237,8 @@ int ct_copy(ct_handle* h, double* dst, const double* src, int64_t n);
 int ct_permute_launch(ct_handle* h, const double* in, double* out, int rank, const int64_t* shape,
                       const int32_t* perm);
 int ct_identity_env(ct_handle* h, double* E, int64_t w, int64_t D);
+// E[w, Dk, Db] = delta(k, b) for k, b < min(Dk, Db) in every channel
+int ct_identity_env_rect(ct_handle* h, double* E, int64_t w, int64_t Dk, int64_t Db);
 
 // Lanczos pieces
 int ct_lanczos_update(ct_handle* h, int64_t n, double* w, const double* vj, const double* vjm1,

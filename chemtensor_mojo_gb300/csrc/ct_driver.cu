@@ -521,6 +521,52 @@ int ct_mps_expectation(ct_handle* h, int prec, int N, int d, const int64_t* mpo_
     return CT_OK;
 }
 
+// <bra|mpo|ket> (expectation_value_two_mps, environments.mojo:698-730) or, with
+// mpo_sites == NULL, <bra|ket> (mps_vdot_direct, environments.mojo:971-1016),
+// through left environments L[w, D_ket, D_bra] in FP64.
+int ct_mps_expectation2(ct_handle* h, int prec, int N, int d, const int64_t* mpo_dims,
+                        const double* const* mpo_sites, const int64_t* bra_dims, const double* const* bra_sites,
+                        const int64_t* ket_dims, const double* const* ket_sites, double* value_host) {
+    if (!h || !bra_dims || !bra_sites || !ket_dims || !ket_sites || !value_host || N < 1 || d < 1)
+        return CT_ERR_INVALID;
+    if (mpo_sites && !mpo_dims) return CT_ERR_INVALID;
+    if (prec != CT_PREC_FP64) {
+        ct_seterr(h, "ct_mps_expectation2: only the FP64 form takes a bra different from the ket");
+        return CT_ERR_UNSUPPORTED;
+    }
+    for (int k = 0; k <= N; ++k)
+        if (bra_dims[k] < 1 || ket_dims[k] < 1 || (mpo_sites && mpo_dims[k] < 1)) return CT_ERR_SHAPE;
+    if (mpo_sites && bra_dims[0] != ket_dims[0]) {
+        ct_seterr(h, "ct_mps_expectation2: bra and ket left bonds differ");
+        return CT_ERR_SHAPE;
+    }
+    int64_t cap = 1;
+    for (int k = 0; k <= N; ++k)
+        cap = std::max<int64_t>(cap, (mpo_sites ? mpo_dims[k] : 1) * bra_dims[k] * ket_dims[k]);
+    DevBuf e0, e1;
+    CT_CUDA(h, cudaMalloc((void**)&e0.p, (size_t)cap * sizeof(double)));
+    CT_CUDA(h, cudaMalloc((void**)&e1.p, (size_t)cap * sizeof(double)));
+    double* a = e0.p;
+    double* b = e1.p;
+    const int64_t w0 = mpo_sites ? mpo_dims[0] : 1;
+    CT_TRY(ct_identity_env_rect(h, a, w0, ket_dims[0], bra_dims[0]));
+    for (int i = 0; i < N; ++i) {
+        const int64_t wl = mpo_sites ? mpo_dims[i] : 1, wr = mpo_sites ? mpo_dims[i + 1] : 1;
+        CT_TRY(ct_reserve(h, ct_env2_ws_bytes(ket_dims[i], bra_dims[i], d, ket_dims[i + 1], bra_dims[i + 1], wl, wr)));
+        Arena ar(h);
+        CT_TRY(ct_env_left2_run(h, ar, a, ket_sites[i], bra_sites[i], mpo_sites ? mpo_sites[i] : nullptr, b,
+                                ket_dims[i], bra_dims[i], d, ket_dims[i + 1], bra_dims[i + 1], wl, wr));
+        std::swap(a, b);
+    }
+    if ((mpo_sites ? mpo_dims[N] : 1) * bra_dims[N] * ket_dims[N] != 1) {
+        ct_seterr(h, "ct_mps_expectation2: final environment is not a scalar");
+        return CT_ERR_SHAPE;
+    }
+    CT_CUDA(h, cudaMemcpyAsync(value_host, a, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CT_CUDA(h, cudaStreamSynchronize(h->stream));
+    return CT_OK;
+}
+
 // ---------------------------------------------------------------------------
 // seeded initial state: PCG32 (O'Neill) + Box-Muller in float32
 // ---------------------------------------------------------------------------

@@ -7,6 +7,8 @@
 // per bond) and applied in a single pass over the intermediate: each thread
 // owns one column i of in(o, :, i), streams its K inputs once per chunk of 8
 // outputs and keeps the weights (or a chunk of their rows) in shared memory.
+#include <algorithm>
+
 #include "ct_common.cuh"
 
 namespace {
@@ -91,7 +93,71 @@ __global__ void build_wt_right_kernel(const double* W, double* Wt, int64_t wL, i
     Wt[t] = W[((wl * d + s) * d + sp) * wR + wr];
 }
 
+// W[(al, bl), i, o, (ar, br)] = sum_m Wa[al, i, m, ar] Wb[bl, m, o, br]   (MPO composition)
+__global__ void mpo_compose_kernel(const double* Wa, const double* Wb, double* W, int64_t wLa, int64_t d_in,
+                                   int64_t d_mid, int64_t wRa, int64_t wLb, int64_t d_out, int64_t wRb) {
+    const int64_t n = wLa * wLb * d_in * d_out * wRa * wRb;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t q = t;
+        const int64_t br = q % wRb; q /= wRb;
+        const int64_t ar = q % wRa; q /= wRa;
+        const int64_t o = q % d_out; q /= d_out;
+        const int64_t i = q % d_in; q /= d_in;
+        const int64_t bl = q % wLb; q /= wLb;
+        const int64_t al = q;
+        double acc = 0.0;
+        for (int64_t m = 0; m < d_mid; ++m)
+            acc = fma(Wa[((al * d_in + i) * d_mid + m) * wRa + ar], Wb[((bl * d_mid + m) * d_out + o) * wRb + br], acc);
+        W[t] = acc;
+    }
+}
+
+// out[(w, a), t, (v, b)] = sum_s A[a, s, b] W[w, s, t, v]   (MPO applied to an MPS site).
+// One block row per (w, a, t, v): threads run along b, so the reads of A and the
+// writes of out are contiguous; the d weights of the row are broadcast.
+__global__ void __launch_bounds__(256) apply_mpo_kernel(const double* __restrict__ A, const double* __restrict__ W,
+                                                        double* __restrict__ out, int64_t Dl, int64_t d, int64_t Dr,
+                                                        int64_t wL, int64_t d_out, int64_t wR) {
+    const int64_t rows = wL * Dl * d_out * wR;
+    for (int64_t row = blockIdx.y; row < rows; row += gridDim.y) {
+        int64_t q = row;
+        const int64_t v = q % wR; q /= wR;
+        const int64_t t = q % d_out; q /= d_out;
+        const int64_t a = q % Dl;
+        const int64_t w = q / Dl;
+        double* o = out + row * Dr;
+        const double* Ar = A + a * d * Dr;
+        for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < Dr; b += (int64_t)gridDim.x * blockDim.x) {
+            double acc = 0.0;
+            for (int64_t s = 0; s < d; ++s) acc = fma(Ar[s * Dr + b], __ldg(&W[((w * d + s) * d_out + t) * wR + v]), acc);
+            o[b] = acc;
+        }
+    }
+}
+
 }  // namespace
+
+int ct_mpo_compose_launch(ct_handle* h, const double* Wa, const double* Wb, double* Wout, int64_t wLa,
+                          int64_t d_in, int64_t d_mid, int64_t wRa, int64_t wLb, int64_t d_out, int64_t wRb) {
+    const int64_t n = wLa * wLb * d_in * d_out * wRa * wRb;
+    if (n <= 0) return CT_OK;
+    const int64_t g = std::min<int64_t>(ct_cdiv(n, 256), (int64_t)h->num_sms * 8);
+    mpo_compose_kernel<<<(unsigned)g, 256, 0, h->stream>>>(Wa, Wb, Wout, wLa, d_in, d_mid, wRa, wLb, d_out, wRb);
+    ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_apply_mpo_launch(ct_handle* h, const double* A, const double* W, double* out, int64_t Dl, int64_t d,
+                        int64_t Dr, int64_t wL, int64_t d_out, int64_t wR) {
+    const int64_t rows = wL * Dl * d_out * wR;
+    if (rows <= 0 || Dr <= 0) return CT_OK;
+    dim3 grid((unsigned)std::min<int64_t>(ct_cdiv(Dr, 256), 64), (unsigned)std::min<int64_t>(rows, 65535));
+    apply_mpo_kernel<<<grid, 256, 0, h->stream>>>(A, W, out, Dl, d, Dr, wL, d_out, wR);
+    ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
 
 int ct_mpo_apply_f64_launch(ct_handle* h, const MpoDesc& m) {
     if (m.O <= 0 || m.I <= 0 || m.J <= 0) return CT_OK;

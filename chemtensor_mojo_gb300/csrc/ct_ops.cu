@@ -85,43 +85,63 @@ size_t ct_env_ws_bytes(int prec, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, 
     return 2 * ct_bytes(t1, 8) + ct_bytes(wt, 8);
 }
 
-int ct_env_left_run(ct_handle* h, Arena& ar, int prec, const double* Lp, const double* A, const double* W,
-                    double* Ln, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR) {
-    if (prec == CT_PREC_TF32X3) return ct_tc_env_left_run(h, ar, Lp, A, W, Ln, Dl, d, Dr, wL, wR);
-    double* T1 = ar.take<double>(Dl * wL * d * Dr);
-    double* T2 = ar.take<double>(Dl * d * wR * Dr);
-    double* Wt = ar.take<double>((d * wR) * (wL * d));
-    if (!T1 || !T2 || !Wt) return CT_ERR_OOM;
-    CT_TRY(ct_build_wt_left(h, W, Wt, wL, d, wR));
-    const int64_t n1 = d * Dr;
-    {
+size_t ct_env2_ws_bytes(int64_t Dlk, int64_t Dlb, int64_t d, int64_t Drk, int64_t Drb, int64_t wL, int64_t wR) {
+    (void)Dlk;
+    (void)Drb;
+    return ct_bytes(Dlb * wL * d * Drk, 8) + ct_bytes(Dlb * d * wR * Drk, 8) + ct_bytes((wL * d) * (wR * d), 8);
+}
+
+// Left environment with different bra and ket (environments.mojo:535-590), FP64:
+//   Ln[wR, Drk, Drb] = sum L[wL, Dlk, Dlb] Ak[Dlk, s, Drk] W[wL, s, s', wR] Ab[Dlb, s', Drb]
+// With W == null (wL = wR = 1) the MPO step drops out and this is the overlap
+// transfer step L[Dlk, Dlb] -> L[Drk, Drb] of environments.mojo:767-862.
+int ct_env_left2_run(ct_handle* h, Arena& ar, const double* Lp, const double* Ak, const double* Ab,
+                     const double* W, double* Ln, int64_t Dlk, int64_t Dlb, int64_t d, int64_t Drk, int64_t Drb,
+                     int64_t wL, int64_t wR) {
+    if (!W && (wL != 1 || wR != 1)) return CT_ERR_SHAPE;
+    const int64_t n1 = d * Drk;
+    double* T1 = ar.take<double>(Dlb * wL * n1);
+    if (!T1) return CT_ERR_OOM;
+    {   // T1[Dlb, wL, (s Drk)] = sum_Dlk L[wL, Dlk, Dlb] Ak[Dlk, (s Drk)]; batch wL
         GemmDesc g{};
-        g.M = Dl; g.N = n1; g.K = Dl;
-        g.A = Lp; g.sAm = 1; g.sAk = Dl;
-        g.B = A; g.sBk = n1; g.sBn = 1;
+        g.M = Dlb; g.N = n1; g.K = Dlk;
+        g.A = Lp; g.sAm = 1; g.sAk = Dlb;
+        g.B = Ak; g.sBk = n1; g.sBn = 1;
         g.C = T1; g.sCm = wL * n1; g.sCn = 1;
         g.alpha = 1.0; g.beta = 0.0; g.nb1 = wL; g.nb0 = 1;
-        g.sA1 = Dl * Dl; g.sC1 = n1;
+        g.sA1 = Dlk * Dlb; g.sC1 = n1;
         CT_TRY(ct_gemm_f64_launch(h, g));
     }
-    {
+    const double* T2 = T1;   // [(Dlb s'), (wR Drk)]
+    if (W) {
+        double* T2w = ar.take<double>(Dlb * d * wR * Drk);
+        double* Wt = ar.take<double>((d * wR) * (wL * d));
+        if (!T2w || !Wt) return CT_ERR_OOM;
+        CT_TRY(ct_build_wt_left(h, W, Wt, wL, d, wR));
         MpoDesc m{};
-        m.O = Dl; m.K = wL * d; m.J = d * wR; m.I = Dr;
-        m.in = T1; m.sIo = wL * d * Dr; m.sIk = Dr; m.sIi = 1;
-        m.out = T2; m.sOo = d * wR * Dr; m.sOi = 1; m.J0 = m.J; m.sOj1 = 0; m.sOj0 = Dr;
+        m.O = Dlb; m.K = wL * d; m.J = d * wR; m.I = Drk;
+        m.in = T1; m.sIo = wL * d * Drk; m.sIk = Drk; m.sIi = 1;
+        m.out = T2w; m.sOo = d * wR * Drk; m.sOi = 1; m.J0 = m.J; m.sOj1 = 0; m.sOj0 = Drk;
         m.Wt = Wt;
         CT_TRY(ct_mpo_apply_f64_launch(h, m));
+        T2 = T2w;
     }
-    {
+    {   // Ln[(wR Drk), Drb] = sum_(Dlb s') T2[(Dlb s'), (wR Drk)] Ab[(Dlb s'), Drb]
         GemmDesc g{};
-        g.M = wR * Dr; g.N = Dr; g.K = Dl * d;
-        g.A = T2; g.sAm = 1; g.sAk = wR * Dr;
-        g.B = A; g.sBk = Dr; g.sBn = 1;
-        g.C = Ln; g.sCm = Dr; g.sCn = 1;
+        g.M = wR * Drk; g.N = Drb; g.K = Dlb * d;
+        g.A = T2; g.sAm = 1; g.sAk = wR * Drk;
+        g.B = Ab; g.sBk = Drb; g.sBn = 1;
+        g.C = Ln; g.sCm = Drb; g.sCn = 1;
         g.alpha = 1.0; g.beta = 0.0; g.nb1 = 1; g.nb0 = 1;
         CT_TRY(ct_gemm_f64_launch(h, g));
     }
     return CT_OK;
+}
+
+int ct_env_left_run(ct_handle* h, Arena& ar, int prec, const double* Lp, const double* A, const double* W,
+                    double* Ln, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR) {
+    if (prec == CT_PREC_TF32X3) return ct_tc_env_left_run(h, ar, Lp, A, W, Ln, Dl, d, Dr, wL, wR);
+    return ct_env_left2_run(h, ar, Lp, A, A, W, Ln, Dl, Dl, d, Dr, Dr, wL, wR);
 }
 
 int ct_env_right_run(ct_handle* h, Arena& ar, int prec, const double* Rn, const double* A, const double* W,

@@ -32,6 +32,10 @@ int ct_env_left_run(ct_handle* h, Arena& ar, int prec, const double* Lp, const d
                     double* Ln, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR);
 int ct_env_right_run(ct_handle* h, Arena& ar, int prec, const double* Rn, const double* A, const double* W,
                      double* Rp, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR);
+size_t ct_env2_ws_bytes(int64_t Dlk, int64_t Dlb, int64_t d, int64_t Drk, int64_t Drb, int64_t wL, int64_t wR);
+int ct_env_left2_run(ct_handle* h, Arena& ar, const double* Lp, const double* Ak, const double* Ab,
+                     const double* W, double* Ln, int64_t Dlk, int64_t Dlb, int64_t d, int64_t Drk, int64_t Drb,
+                     int64_t wL, int64_t wR);
 size_t ct_theta_ws_bytes(int prec, int64_t Dl, int64_t d, int64_t Dm, int64_t Dr);
 int ct_theta_run(ct_handle* h, int prec, const double* Ai, const double* Aj, double* theta, int64_t Dl,
                  int64_t d, int64_t Dm, int64_t Dr);

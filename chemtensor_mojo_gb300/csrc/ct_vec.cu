@@ -117,6 +117,14 @@ __global__ void identity_env_kernel(double* E, int64_t w, int64_t D) {
     }
 }
 
+__global__ void identity_env_rect_kernel(double* E, int64_t w, int64_t Dk, int64_t Db) {
+    const int64_t n = w * Dk * Db;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = (t / Db) % Dk, c = t % Db;
+        E[t] = (r == c) ? 1.0 : 0.0;
+    }
+}
+
 struct PermArgs {
     int rank;
     int64_t n;
@@ -472,6 +480,14 @@ int ct_identity_env(ct_handle* h, double* E, int64_t w, int64_t D) {
     const int64_t n = w * D * D;
     if (n <= 0) return CT_OK;
     identity_env_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(E, w, D); ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_identity_env_rect(ct_handle* h, double* E, int64_t w, int64_t Dk, int64_t Db) {
+    const int64_t n = w * Dk * Db;
+    if (n <= 0) return CT_OK;
+    identity_env_rect_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(E, w, Dk, Db); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }

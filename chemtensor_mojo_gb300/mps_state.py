@@ -9,6 +9,9 @@ src/state/mpo_state.mojo, plus the seeded initial states.
                                                 reference counterpart)
 * ``mps_to_statevector`` / ``mps_norm``         mps_state.mojo:454-508
 * ``MPOSite`` / ``MatrixProductOperator``       mpo_state.mojo:10-193
+* ``create_identity_mpo``                       mpo_state.mojo:196-241
+* ``create_single_site_op_mpo``                 mpo_state.mojo:243-272
+* ``create_two_site_op_mpo``                    mpo_state.mojo:275-310
 """
 from __future__ import annotations
 
@@ -229,3 +232,40 @@ def mps_to_statevector(psi: MatrixProductState, ctx: DeviceContext | None = None
 
 def mps_norm(psi: MatrixProductState, ctx: DeviceContext | None = None) -> float:
     return mps_to_statevector(psi, ctx).norm(ctx)
+
+
+# -- operator MPOs (host-built, bond dimension 1) ----------------------------------
+def create_identity_mpo(ctx, num_sites: int, physical_dim: int) -> MatrixProductOperator:
+    """Identity on every site, shape [1, d, d, 1] (mpo_state.mojo:196-241)."""
+    if num_sites < 1:
+        raise ValueError("num_sites must be >= 1")
+    if physical_dim < 1:
+        raise ValueError("physical_dim must be >= 1")
+    eye = np.eye(physical_dim).reshape(1, physical_dim, physical_dim, 1)
+    return mpo_from_arrays(ctx, [eye] * num_sites)
+
+
+def create_single_site_op_mpo(ctx, num_sites: int, site_idx: int, op_data: Sequence[float]) -> MatrixProductOperator:
+    """2x2 row-major operator on one site, identity elsewhere (mpo_state.mojo:243-272)."""
+    if num_sites < 1 or site_idx < 0 or site_idx >= num_sites:
+        raise ValueError("create_single_site_op_mpo: invalid site_idx")
+    if len(op_data) != 4:
+        raise ValueError("create_single_site_op_mpo: op_data must be 4 elements (2x2)")
+    arrays = [np.eye(2).reshape(1, 2, 2, 1)] * num_sites
+    arrays = list(arrays)
+    arrays[site_idx] = np.asarray(op_data, dtype=np.float64).reshape(1, 2, 2, 1)
+    return mpo_from_arrays(ctx, arrays)
+
+
+def create_two_site_op_mpo(ctx, num_sites: int, site_i: int, site_j: int, op_i_data: Sequence[float],
+                           op_j_data: Sequence[float]) -> MatrixProductOperator:
+    """O_i O_j with site_i < site_j, identity elsewhere (mpo_state.mojo:275-310)."""
+    if num_sites < 2 or site_i < 0 or site_j >= num_sites or site_i >= site_j:
+        raise ValueError("create_two_site_op_mpo: invalid sites")
+    if len(op_i_data) != 4 or len(op_j_data) != 4:
+        raise ValueError("create_two_site_op_mpo: op data must be 4 elements each")
+    arrays = [np.eye(2).reshape(1, 2, 2, 1)] * num_sites
+    arrays = list(arrays)
+    arrays[site_i] = np.asarray(op_i_data, dtype=np.float64).reshape(1, 2, 2, 1)
+    arrays[site_j] = np.asarray(op_j_data, dtype=np.float64).reshape(1, 2, 2, 1)
+    return mpo_from_arrays(ctx, arrays)

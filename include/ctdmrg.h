@@ -214,6 +214,38 @@ CT_API int ct_mps_expectation(ct_handle* h, int prec, int nsites, int d, const i
                        const double* const* mpo_sites, const int64_t* bond_dims,
                        const double* const* mps_sites, double* energy_host, double* norm_sq_host);
 
+/* ---- observables with two different states (FP64 form) -------------------
+ * One left-environment step with bra != ket:
+ *   Lnext[wR,Drk,Drb] = sum Lprev[wL,Dlk,Dlb] A_ket[Dlk,s,Drk] W[wL,s,s',wR] A_bra[Dlb,s',Drb]
+ * (update_left_environment_two_mps, environments.mojo:535-590).  With
+ * W == NULL (wL = wR = 1) it is the overlap transfer step
+ * Lprev[Dlk,Dlb] -> Lnext[Drk,Drb] of _mps_contraction_step_left
+ * (environments.mojo:767-862).  prec must be CT_PREC_FP64.                   */
+CT_API int ct_env_left2(ct_handle* h, int prec, const double* Lprev, const double* A_ket, const double* A_bra,
+                        const double* W, double* Lnext, int64_t Dl_ket, int64_t Dl_bra, int64_t d,
+                        int64_t Dr_ket, int64_t Dr_bra, int64_t wL, int64_t wR);
+
+/* <bra|mpo|ket> (expectation_value_two_mps, environments.mojo:698-730) or,
+ * with mpo_sites == NULL, <bra|ket> (mps_vdot_direct / mps_overlap,
+ * environments.mojo:971-1025).  The left boundary is the identity over
+ * min(ket_dims[0], bra_dims[0]); the final environment must be a scalar
+ * (CT_ERR_SHAPE otherwise, where the reference raises).                     */
+CT_API int ct_mps_expectation2(ct_handle* h, int prec, int nsites, int d, const int64_t* mpo_dims,
+                               const double* const* mpo_sites, const int64_t* bra_dims,
+                               const double* const* bra_sites, const int64_t* ket_dims,
+                               const double* const* ket_sites, double* value_host);
+
+/* One site of mpo_compose (environments.mojo:1086-1132):
+ *   Wout[(al,bl), i, o, (ar,br)] = sum_m Wa[al,i,m,ar] Wb[bl,m,o,br]        */
+CT_API int ct_mpo_compose_site(ct_handle* h, const double* Wa, const double* Wb, double* Wout, int64_t wLa,
+                               int64_t d_in, int64_t d_mid, int64_t wRa, int64_t wLb, int64_t d_out,
+                               int64_t wRb);
+
+/* One site of apply_mpo (environments.mojo:1135-1189):
+ *   out[(w,a), t, (v,b)] = sum_s A[a,s,b] W[w,s,t,v]                         */
+CT_API int ct_apply_mpo_site(ct_handle* h, const double* A, const double* W, double* out, int64_t Dl,
+                             int64_t d, int64_t Dr, int64_t wL, int64_t d_out, int64_t wR);
+
 /* ---- host-side seeded initial state (rng_c_compat.mojo:14-231) ------------
  * Fills HOST buffers: sites[i] gets dims[i]*d*dims[i+1] doubles holding the
  * float32 values of create_random_mps_c_compatible; dims (length nsites+1)
