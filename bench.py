@@ -35,6 +35,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -74,9 +75,16 @@ def parse():
     ap.add_argument("--L", type=int, default=L_SITES)
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64/roofline/CPU side measurements")
     ap.add_argument("--verbose", action="store_true", help="log every split of the timed sweeps to stderr")
-    ap.add_argument("--mode", default="sweep", choices=["sweep", "heff", "heff-grid", "split", "hubbard"],
+    ap.add_argument("--mode", default="sweep",
+                    choices=["sweep", "heff", "heff-grid", "split", "hubbard", "contractions"],
                     help="heff / split: only centre-bond H_eff applies / warm splits (small, fixed workloads "
-                         "for profilers); heff-grid: H_eff over chi x D x d")
+                         "for profilers); heff-grid: H_eff over chi x D x d; contractions: the MPS/MPO "
+                         "contraction operations of the reference's contraction benchmark")
+    ap.add_argument("--nsites", type=int, default=6, help="contractions: number of sites")
+    ap.add_argument("--d", type=int, default=2, help="contractions: physical dimension")
+    ap.add_argument("--runs", type=int, default=3, help="contractions: timed repetitions per operation")
+    ap.add_argument("--jsonl", default="", help="contractions: append one JSONL record per operation here")
+    ap.add_argument("--ramp-sweeps", default="", help="hubbard: sweeps per ramp stage, e.g. 1,1,1,1")
     return ap.parse_args()
 
 
@@ -167,10 +175,11 @@ def hubbard_mode(args):
 
     1D Fermi-Hubbard chain (Jordan-Wigner), L=48, d=4, t=1, U=8, MPO bond
     dimension 6; seeded Gaussian initial MPS; chi_max ramped 256 -> 512 ->
-    1024 (two sweeps each, 24 Lanczos steps, eps_trunc = 0) in the mixed form
-    with kept bases across the ramp and randomized first-visit splits (two
-    power steps); then one FP64 adjoint-gradient pass at the final state
-    (environment checkpoints every 7 sites).  Reports sweep seconds per chi,
+    1024 (two sweeps each) or, with --chi 2048, 256 -> 512 -> 1024 -> 2048
+    over ten sweeps (2, 2, 3, 3), 24 Lanczos steps, eps_trunc = 0, in the mixed
+    form with kept bases across the ramp and randomized first-visit splits (two
+    power steps); then one adjoint-gradient pass at the final state in the
+    mixed form (environment checkpoints every 7 sites).  Reports sweep seconds per chi,
     the FP64 Rayleigh energy, the gradient residual |grad E| (zero at a
     stationary state), |dE/E| of the mixed form against the FP64 form at
     chi=256 (two sweeps each from the same start, Jacobi first visits in both)
@@ -183,7 +192,14 @@ def hubbard_mode(args):
     from chemtensor_mojo_gb300.autograd import energy_and_gradient
     ctx = ct.get_context(0)
     L = 48
-    ramp = [256, 512, 1024] if args.chi >= 1024 else [c for c in (256, 512, 1024) if c <= args.chi]
+    if args.chi >= 2048:
+        ramp, nsw = [256, 512, 1024, 2048], [2, 2, 3, 3]
+    else:
+        ramp = [256, 512, 1024] if args.chi >= 1024 else [c for c in (256, 512, 1024) if c <= args.chi]
+        nsw = [2] * len(ramp)
+    if args.ramp_sweeps:
+        nsw = [int(x) for x in args.ramp_sweeps.split(",")][:len(ramp)]
+        ramp = ramp[:len(nsw)]
     mpo = ct.create_fermi_hubbard_mpo(ctx, L, 1.0, 8.0)
     arrays, _ = ct.random_mps_c_compatible_arrays(L, 4, ramp[0], 11)
     mps = ct.mps_right_normalize(ctx, ct.mps_from_arrays(ctx, arrays))
@@ -191,49 +207,55 @@ def hubbard_mode(args):
     peak_used = 0
     log = []
     first = True
-    for chi in ramp:
+    for chi, ns in zip(ramp, nsw):
         st = ct.DMRGStats()
-        p = ct.DMRGParams(num_sweeps=2, chi_max=chi, eps_trunc=0.0, max_krylov_iter=LANCZOS, krylov_tol=1e-10,
+        p = ct.DMRGParams(num_sweeps=ns, chi_max=chi, eps_trunc=0.0, max_krylov_iter=LANCZOS, krylov_tol=1e-10,
                           energy_tol=0.0, max_rotations=0, prec="tf32x3", final_rayleigh=True,
-                          keep_bases=not first, cold_power_steps=2)
+                          keep_bases=not first, cold_power_steps=2, verbose=2 if args.verbose else 0)
         E, mps = ct.dmrg_two_site(ctx, mpo, mps, p, st)
         first = False
         free, _ = torch.cuda.mem_get_info()
         peak_used = max(peak_used, total - free)
-        log.append({"chi_max": chi, "seconds_per_sweep": st.seconds_total / 2, "energy_rayleigh": st.energy_rayleigh,
+        log.append({"chi_max": chi, "sweeps": ns, "seconds_per_sweep": st.seconds_total / ns,
+                    "sweep_energies": st.sweep_energies, "energy_rayleigh": st.energy_rayleigh,
                     "subspace_splits": st.subspace_splits, "cold_splits": st.cold_splits,
                     "exact_splits": st.exact_splits, "heff_tflops": st.heff_flops / max(st.seconds_lanczos, 1e-12) / 1e12,
+                    "seconds": {"lanczos": st.seconds_lanczos, "split": st.seconds_svd,
+                                "split_subspace": st.seconds_subspace, "env": st.seconds_env},
                     "max_discarded": st.max_discarded})
-    # mixed vs FP64 form at chi=256, two sweeps each from the same start with
-    # Jacobi first visits in both (so the difference is precision, not the start)
-    acc_e = {}
-    acc_t = {}
-    for pr in ("fp64", "tf32x3"):
-        mps_c = ct.mps_right_normalize(ctx, ct.mps_from_arrays(ctx, arrays))
-        st_c = ct.DMRGStats()
-        E_c, _ = ct.dmrg_two_site(ctx, mpo, mps_c, ct.DMRGParams(
-            num_sweeps=2, chi_max=ramp[0], eps_trunc=0.0, max_krylov_iter=LANCZOS, krylov_tol=1e-10,
-            energy_tol=0.0, max_rotations=0, prec=pr, final_rayleigh=(pr == "tf32x3")), st_c)
-        acc_e[pr] = st_c.energy_rayleigh if pr == "tf32x3" else E_c
-        acc_t[pr] = st_c.seconds_total / 2
-    accuracy = {"chi_max": ramp[0], "sweeps": 2, "E_fp64": acc_e["fp64"], "E_mixed_rayleigh_fp64": acc_e["tf32x3"],
-                "dE_over_E": abs(acc_e["tf32x3"] - acc_e["fp64"]) / abs(acc_e["fp64"]),
-                "seconds_per_sweep": acc_t}
-    sites = [s.tensor.storage[: int(np.prod(s.tensor.shape))].view(*s.tensor.shape) for s in mps.sites]
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    Eg, grads = energy_and_gradient(mpo, sites, checkpoint_every=7, ctx=ctx)
-    torch.cuda.synchronize()
-    tg = time.perf_counter() - t0
-    free, _ = torch.cuda.mem_get_info()
-    peak_used = max(peak_used, total - free)
-    gnorm = float(torch.sqrt(sum((g * g).sum() for g in grads)))
+    accuracy, gradient = None, None
+    if not args.no_extras:
+        # mixed vs FP64 form at chi=256, two sweeps each from the same start with
+        # Jacobi first visits in both (so the difference is precision, not the start)
+        acc_e = {}
+        acc_t = {}
+        for pr in ("fp64", "tf32x3"):
+            mps_c = ct.mps_right_normalize(ctx, ct.mps_from_arrays(ctx, arrays))
+            st_c = ct.DMRGStats()
+            E_c, _ = ct.dmrg_two_site(ctx, mpo, mps_c, ct.DMRGParams(
+                num_sweeps=2, chi_max=ramp[0], eps_trunc=0.0, max_krylov_iter=LANCZOS, krylov_tol=1e-10,
+                energy_tol=0.0, max_rotations=0, prec=pr, final_rayleigh=(pr == "tf32x3")), st_c)
+            acc_e[pr] = st_c.energy_rayleigh if pr == "tf32x3" else E_c
+            acc_t[pr] = st_c.seconds_total / 2
+        accuracy = {"chi_max": ramp[0], "sweeps": 2, "E_fp64": acc_e["fp64"], "E_mixed_rayleigh_fp64": acc_e["tf32x3"],
+                    "dE_over_E": abs(acc_e["tf32x3"] - acc_e["fp64"]) / abs(acc_e["fp64"]),
+                    "seconds_per_sweep": acc_t}
+        sites = [s.tensor.storage[: int(np.prod(s.tensor.shape))].view(*s.tensor.shape) for s in mps.sites]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Eg, grads = energy_and_gradient(mpo, sites, checkpoint_every=7, ctx=ctx, prec="tf32x3")
+        torch.cuda.synchronize()
+        tg = time.perf_counter() - t0
+        free, _ = torch.cuda.mem_get_info()
+        peak_used = max(peak_used, total - free)
+        gnorm = float(torch.sqrt(sum((g * g).sum() for g in grads)))
+        gradient = {"energy": Eg, "seconds": tg, "norm": gnorm, "checkpoint_every": 7, "dtype": "tf32x3"}
     print(json.dumps({"metric": "Fermi-Hubbard L=48 mixed sweep seconds", "unit": "s/sweep", "data": "synthetic",
                       "config": {"workload": "1D Fermi-Hubbard JW L=48 d=4 t=1 U=8 D=6, chi ramp " +
-                                 "->".join(str(c) for c in ramp) + ", 2 sweeps each, lanczos=24, eps=0"},
+                                 "->".join(str(c) for c in ramp) + " (sweeps " + "+".join(str(n) for n in nsw) +
+                                 "), lanczos=24, eps=0"},
                       "ramp": log, "accuracy_vs_fp64": accuracy,
-                      "gradient": {"energy": Eg, "seconds": tg, "norm": gnorm,
-                                                "checkpoint_every": 7, "dtype": "f64"},
+                      "gradient": gradient,
                       "peak_device_bytes": int(peak_used), "device_bytes_before": int(total - free0)}),
           flush=True)
 
@@ -288,6 +310,64 @@ def heff_grid_mode(args):
 
 
 # ---------------------------------------------------------------------------
+def contractions_mode(args):
+    """The contraction operations of bench_contractions.mojo:349-475 on the same inputs
+    (Ising MPO J=1, h=g=0; C-compatible random MPS with seeds 42 and 43 at
+    (nsites, d, chi)), timed with CUDA events: <chi|W|psi> (sign flipped to the C
+    convention), W|psi> (result ||W psi||), <chi|psi>, and the left-environment
+    sweep.  One JSONL record per operation in the reference's record format, and
+    one summary JSON line."""
+    import torch
+    import chemtensor_mojo_gb300 as ct
+    from chemtensor_mojo_gb300 import environments as ct_env
+    ctx = ct.get_context(0)
+    n, d, chi, runs = args.nsites, args.d, args.chi, max(args.runs, 1)
+    mpo = ct.create_ising_1d_mpo(ctx, n, J=1.0, h_longitudinal=0.0, g_transverse=0.0)
+    if d != 2:
+        raise SystemExit("contractions: the Ising MPO has d = 2")
+    psi = ct.create_random_mps_c_compatible(ctx, n, d, chi, 42)
+    phi = ct.create_random_mps_c_compatible(ctx, n, d, chi, 43)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(runs):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) * 1e-3 / runs
+
+    def left_env_sweep():
+        L = ct_env.create_identity_environment(ctx, mpo.bond_dimension(0), psi.bond_dimension(0))
+        for i in range(n):
+            L = ct.update_left_environment(L, psi.sites[i], mpo.sites[i], ctx)
+        return L
+
+    recs = []
+    t = timed(lambda: ct.expectation_value_two_mps(phi, mpo, psi, ctx))
+    recs.append(("mps_mpo_inner", t, -ct.expectation_value_two_mps(phi, mpo, psi, ctx)))
+    t = timed(lambda: ct.apply_mpo(mpo, psi, ctx))
+    op_psi = ct.apply_mpo(mpo, psi, ctx)
+    recs.append(("mps_mpo_apply", t, math.sqrt(max(ct.mps_overlap(op_psi, op_psi, ctx), 0.0))))
+    t = timed(lambda: ct.mps_overlap(phi, psi, ctx))
+    recs.append(("mps_mps", t, ct.mps_overlap(phi, psi, ctx)))
+    t = timed(left_env_sweep)
+    recs.append(("left_env_sweep", t, 0.0))
+    for op, t, res in recs:
+        line = json.dumps({"backend": "gb300", "operation": op, "params": {"nsites": n, "d": d, "chi_max": chi},
+                           "time_seconds": t, "result": res, "runs": runs}, separators=(",", ":"))
+        if args.jsonl:
+            with open(args.jsonl, "a") as f:
+                f.write(line + "\n")
+        print(line, file=sys.stderr)
+    print(json.dumps({"metric": "MPS/MPO contraction seconds", "unit": "s/op", "dtype": "fp64",
+                      "config": {"workload": f"Ising MPO, C-compatible random MPS seeds 42/43, nsites={n} d={d} "
+                                             f"chi_max={chi}"},
+                      "ops": {op: {"seconds": t, "result": res} for op, t, res in recs}, "runs": runs}))
+
+
 def heff_flops(chi_l, chi_r, D=MPO_D, d=D_PHYS):
     return (2.0 * chi_l * D * d * d * chi_r * chi_l + 2.0 * chi_l * d * chi_r * D * d * d * D
             + 2.0 * chi_l * chi_r * d * D * d * d * D + 2.0 * chi_l * d * d * chi_r * D * chi_r)
@@ -429,6 +509,8 @@ def main():
     if args.impl == "reference":
         reference_arm(args, rank)
         return
+    if args.mode == "contractions":
+        return contractions_mode(args)
     if args.mode == "split":
         split_mode(args)
         return

@@ -18,8 +18,9 @@ from .mps_state import MatrixProductOperator
 
 
 def energy_and_gradient(mpo: MatrixProductOperator, sites: Sequence[torch.Tensor], checkpoint_every: int = 0,
-                        ctx=None):
-    """-> (E, [dE/dA_i]) for CUDA float64 site tensors of shape [Dl, d, Dr]."""
+                        ctx=None, prec: str = "fp64"):
+    """-> (E, [dE/dA_i]) for CUDA float64 site tensors of shape [Dl, d, Dr].  prec "tf32x3" runs
+    the environment chain and the one-site effective Hamiltonians on the tensor cores."""
     ctx = ctx or get_context()
     N = len(sites)
     if mpo.num_sites() != N:
@@ -37,24 +38,25 @@ def energy_and_gradient(mpo: MatrixProductOperator, sites: Sequence[torch.Tensor
     mps_pp, k2 = _lib.ptr_array([s.data_ptr() for s in sites_c])
     g_pp, k3 = _lib.ptr_array([g.data_ptr() for g in grads])
     E = C.c_double()
-    ctx.call("ct_energy_grad", _lib.CT_PREC_FP64, N, d, _lib.i64_array(mpo.bond_dims), mpo_pp, _lib.i64_array(bd),
+    ctx.call("ct_energy_grad", _lib.PRECISIONS[prec], N, d, _lib.i64_array(mpo.bond_dims), mpo_pp, _lib.i64_array(bd),
              mps_pp, g_pp, int(checkpoint_every), C.byref(E))
     return E.value, grads
 
 
 class _MPSEnergy(torch.autograd.Function):
     @staticmethod
-    def forward(fctx, mpo, checkpoint_every, *sites):
-        E, grads = energy_and_gradient(mpo, sites, checkpoint_every)
+    def forward(fctx, mpo, checkpoint_every, prec, *sites):
+        E, grads = energy_and_gradient(mpo, sites, checkpoint_every, prec=prec)
         fctx.save_for_backward(*grads)
         return torch.tensor(E, dtype=torch.float64, device=sites[0].device)
 
     @staticmethod
     def backward(fctx, grad_out):
         grads = fctx.saved_tensors
-        return (None, None) + tuple(grad_out * g for g in grads)
+        return (None, None, None) + tuple(grad_out * g for g in grads)
 
 
-def mps_energy(mpo: MatrixProductOperator, sites: Sequence[torch.Tensor], checkpoint_every: int = 0) -> torch.Tensor:
+def mps_energy(mpo: MatrixProductOperator, sites: Sequence[torch.Tensor], checkpoint_every: int = 0,
+               prec: str = "fp64") -> torch.Tensor:
     """E = <psi|H|psi>/<psi|psi>, differentiable in every site tensor."""
-    return _MPSEnergy.apply(mpo, int(checkpoint_every), *sites)
+    return _MPSEnergy.apply(mpo, int(checkpoint_every), prec, *sites)

@@ -379,17 +379,16 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
             ct_seterr(h, "bond %d: device status %d", i, dst);
             return dst;
         }
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, ev_l.a, ev_l.b);
-        st.seconds_lanczos += ms * 1e-3;
+        float ms = 0.f, ms_l = 0.f;
+        cudaEventElapsedTime(&ms_l, ev_l.a, ev_l.b);
+        st.seconds_lanczos += ms_l * 1e-3;
         cudaEventElapsedTime(&ms, ev_s.a, ev_s.b);
         st.seconds_svd += ms * 1e-3;
         if (last_split_subspace) st.seconds_subspace += ms * 1e-3;
         if (P->verbose >= 2)
-            fprintf(stderr, "bond %d %s: %lld x %lld -> chi %lld, %s split %.3f ms\n", i, l2r ? "L->R" : "R->L",
-                    (long long)m, (long long)n, (long long)so.chi,
-                    last_split_subspace ? "subspace" : "exact",
-                    (double)ms);
+            fprintf(stderr, "bond %d %s: %lld x %lld -> chi %lld, lanczos %.3f ms (%d applies), %s split %.3f ms\n",
+                    i, l2r ? "L->R" : "R->L", (long long)m, (long long)n, (long long)so.chi, (double)ms_l, hb.nk,
+                    last_split_subspace ? "subspace" : "exact", (double)ms);
         cudaEventElapsedTime(&ms, ev_e.a, ev_e.b);
         st.seconds_env += ms * 1e-3;
         st.heff_applies += hb.nk;

@@ -8,7 +8,11 @@
 //     dF/dA_i = 2 H1(L_i, W_i, R_{i+1}) A_i       (H real symmetric),
 // with the same for N = <psi|psi> through identity-MPO environments, so
 //     dE/dA_i = 2 (H1 A_i - E N1 A_i) / N.
-// The MPS need not be canonical.  Left environments are kept only every
+// The MPS need not be canonical, nor normalised: every environment is
+// divided by a power of two near its norm after each step (exact), and the
+// exponents, kept on the host, enter the final factors -- the FP32 operand
+// planes of the mixed form would otherwise under- or overflow along a chain of
+// unnormalised tensors.  Left environments are kept only every
 // k-th site (checkpoints) and recomputed one segment at a time during the
 // backward sweep: memory ~ (L/k + k) environments instead of L.
 #include <math.h>
@@ -26,13 +30,11 @@ struct Buf {
     }
 };
 
-__global__ void grad_combine_kernel(int64_t n, const double* hA, const double* nA, const double* sc, double* g) {
-    // sc[0] = F, sc[1] = N  ->  g = 2 (hA - (F/N) nA) / N
-    const double N = sc[1];
-    const double E = sc[0] / N;
-    const double f = 2.0 / N;
+// g = fH hA - fN nA; the host folds 2/N, the energy and the environments'
+// power-of-two scales into the two factors
+__global__ void grad_combine_kernel(int64_t n, const double* hA, const double* nA, double fH, double fN, double* g) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        g[i] = f * (hA[i] - E * nA[i]);
+        g[i] = fH * hA[i] - fN * nA[i];
 }
 
 }  // namespace
@@ -90,10 +92,11 @@ int ct_energy_grad(ct_handle* h, int prec, int N, int d, const int64_t* mpo_dims
         ct_seterr(h, "ct_energy_grad: bad arguments");
         return CT_ERR_INVALID;
     }
-    if (prec != CT_PREC_FP64) {
-        ct_seterr(h, "ct_energy_grad: only the FP64 form is built");
+    if (prec != CT_PREC_FP64 && !(prec == CT_PREC_TF32X3 && ct_tc_available(h))) {
+        ct_seterr(h, "ct_energy_grad: precision %d is not available", prec);
         return CT_ERR_UNSUPPORTED;
     }
+    const bool tc = prec == CT_PREC_TF32X3;
     for (int i = 0; i < N; ++i)
         if (!sites[i] || !grads[i] || !mpo_sites[i]) return CT_ERR_INVALID;
     const int k = (checkpoint_every > 0) ? std::min(checkpoint_every, N) : N;
@@ -116,8 +119,9 @@ int ct_energy_grad(ct_handle* h, int prec, int N, int d, const int64_t* mpo_dims
     }
     for (int i = 0; i < N; ++i) {
         maxsite = std::max(maxsite, (size_t)(bd[i] * d * bd[i + 1]));
-        ws = std::max(ws, ct_env_ws_bytes(CT_PREC_FP64, bd[i], d, bd[i + 1], mpo_dims[i], mpo_dims[i + 1]));
-        ws = std::max(ws, ct_heff1_ws_bytes(bd[i], d, bd[i + 1], mpo_dims[i], mpo_dims[i + 1]));
+        ws = std::max(ws, ct_env_ws_bytes(prec, bd[i], d, bd[i + 1], mpo_dims[i], mpo_dims[i + 1]));
+        ws = std::max(ws, tc ? ct_tc_heff1_ws_bytes(bd[i], d, bd[i + 1], mpo_dims[i], mpo_dims[i + 1])
+                             : ct_heff1_ws_bytes(bd[i], d, bd[i + 1], mpo_dims[i], mpo_dims[i + 1]));
     }
     CT_TRY(ct_reserve(h, ws));
     const int ncp = (N + k - 1) / k;
@@ -139,14 +143,38 @@ int ct_energy_grad(ct_handle* h, int prec, int N, int d, const int64_t* mpo_dims
     CT_CUDA(h, cudaMalloc((void**)&nA.p, maxsite * sizeof(double)));
     CT_CUDA(h, cudaMalloc((void**)&sc.p, 2 * sizeof(double)));
 
+    // exponent e with 2^e near the norm of E (n values); E /= 2^e
+    auto renorm = [&](double* E, int64_t n, int* e_out) -> int {
+        CT_TRY(ct_reduce_nrm2sq(h, n, E, h->d_scalars + SC_TMP0, nullptr));
+        double v = 0.0;
+        CT_CUDA(h, cudaMemcpyAsync(&v, h->d_scalars + SC_TMP0, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CT_CUDA(h, cudaStreamSynchronize(h->stream));
+        if (!std::isfinite(v)) {
+            ct_seterr(h, "ct_energy_grad: environment norm is not finite");
+            return CT_ERR_NONFINITE;
+        }
+        int e = 0;
+        if (v > 0.0) e = ilogb(sqrt(v));
+        if (e != 0) CT_TRY(ct_vec_scale_launch(h, n, ldexp(1.0, -e), E));
+        *e_out = e;
+        return CT_OK;
+    };
+    auto scale_by = [&](double* E, int64_t n, int e) -> int {
+        return e != 0 ? ct_vec_scale_launch(h, n, ldexp(1.0, -e), E) : CT_OK;
+    };
+    // per-step exponents of the left chains (index = environment index) and the
+    // cumulative ones of the left and right chains
+    std::vector<int> stepH(N + 1, 0), stepN(N + 1, 0);
+    std::vector<long long> cumHL(N + 1, 0), cumNL(N + 1, 0), cumHR(N + 1, 0), cumNR(N + 1, 0);
+
     auto left_step = [&](const double* Lh, const double* Ln, int i, double* outH, double* outN) -> int {
         {
             Arena ar(h);
-            CT_TRY(ct_env_left_run(h, ar, CT_PREC_FP64, Lh, sites[i], mpo_sites[i], outH, bd[i], d, bd[i + 1],
+            CT_TRY(ct_env_left_run(h, ar, prec, Lh, sites[i], mpo_sites[i], outH, bd[i], d, bd[i + 1],
                                    mpo_dims[i], mpo_dims[i + 1]));
         }
         Arena ar(h);
-        return ct_env_left_run(h, ar, CT_PREC_FP64, Ln, sites[i], Wid.p, outN, bd[i], d, bd[i + 1], 1, 1);
+        return ct_env_left_run(h, ar, prec, Ln, sites[i], Wid.p, outN, bd[i], d, bd[i + 1], 1, 1);
     };
 
     // forward: left chain with checkpoints at multiples of k
@@ -163,6 +191,10 @@ int ct_energy_grad(ct_handle* h, int prec, int N, int d, const int64_t* mpo_dims
                 CT_TRY(ct_copy(h, cpN[i / k].p, an, (int64_t)nsize(i)));
             }
             CT_TRY(left_step(ah, an, i, bh, bn));
+            CT_TRY(renorm(bh, (int64_t)hsize(i + 1), &stepH[i + 1]));
+            CT_TRY(renorm(bn, (int64_t)nsize(i + 1), &stepN[i + 1]));
+            cumHL[i + 1] = cumHL[i] + stepH[i + 1];
+            cumNL[i + 1] = cumNL[i] + stepN[i + 1];
             std::swap(ah, bh);
             std::swap(an, bn);
         }
@@ -177,7 +209,11 @@ int ct_energy_grad(ct_handle* h, int prec, int N, int d, const int64_t* mpo_dims
         ct_seterr(h, "ct_energy_grad: <psi|psi> = %g", fn[1]);
         return CT_ERR_ZERO_NORM;
     }
-    if (energy_host) *energy_host = fn[0] / fn[1];
+    // F = fn[0] 2^cumHL[N], N = fn[1] 2^cumNL[N]
+    const double Nsc = fn[1];
+    const long long eN = cumNL[N];
+    const double energy = ldexp(fn[0] / fn[1], (int)(cumHL[N] - eN));
+    if (energy_host) *energy_host = energy;
 
     // backward: right chain (the adjoint of the left chain), segments in reverse
     double* rh = RH0.p;
@@ -190,31 +226,44 @@ int ct_energy_grad(ct_handle* h, int prec, int N, int d, const int64_t* mpo_dims
         const int start = c * k, end = std::min(start + k, N);
         CT_TRY(ct_copy(h, segH[0].p, cpH[c].p, (int64_t)hsize(start)));
         CT_TRY(ct_copy(h, segN[0].p, cpN[c].p, (int64_t)nsize(start)));
-        for (int i = start; i < end - 1; ++i)
+        for (int i = start; i < end - 1; ++i) {
             CT_TRY(left_step(segH[i - start].p, segN[i - start].p, i, segH[i - start + 1].p, segN[i - start + 1].p));
+            CT_TRY(scale_by(segH[i - start + 1].p, (int64_t)hsize(i + 1), stepH[i + 1]));
+            CT_TRY(scale_by(segN[i - start + 1].p, (int64_t)nsize(i + 1), stepN[i + 1]));
+        }
         for (int i = end - 1; i >= start; --i) {
             const int64_t Dl = bd[i], Dr = bd[i + 1], wl = mpo_dims[i], wr = mpo_dims[i + 1];
             {
                 Arena ar(h);
-                CT_TRY(ct_heff1_run(h, ar, segH[i - start].p, sites[i], mpo_sites[i], rh, hA.p, Dl, d, Dr, wl, wr));
+                CT_TRY((tc ? ct_tc_heff1_run : ct_heff1_run)(h, ar, segH[i - start].p, sites[i], mpo_sites[i], rh,
+                                                             hA.p, Dl, d, Dr, wl, wr));
             }
             {
                 Arena ar(h);
-                CT_TRY(ct_heff1_run(h, ar, segN[i - start].p, sites[i], Wid.p, rn, nA.p, Dl, d, Dr, 1, 1));
+                CT_TRY((tc ? ct_tc_heff1_run : ct_heff1_run)(h, ar, segN[i - start].p, sites[i], Wid.p, rn, nA.p, Dl,
+                                                             d, Dr, 1, 1));
             }
             const int64_t ns = Dl * d * Dr;
             int g = (int)ct_cdiv(ns, 256);
             if (g > h->num_sms * 16) g = h->num_sms * 16;
             if (g < 1) g = 1;
-            grad_combine_kernel<<<g, 256, 0, h->stream>>>(ns, hA.p, nA.p, sc.p, grads[i]); ct_note_launch();
+            // g = 2 (hA_true - E nA_true) / N_true with X_true = X 2^(left + right exponents)
+            const double fH = ldexp(2.0 / Nsc, (int)(cumHL[i] + cumHR[i + 1] - eN));
+            const double fNn = ldexp(2.0 * energy / Nsc, (int)(cumNL[i] + cumNR[i + 1] - eN));
+            grad_combine_kernel<<<g, 256, 0, h->stream>>>(ns, hA.p, nA.p, fH, fNn, grads[i]); ct_note_launch();
             CT_LAUNCH_CHECK(h);
             if (i > 0) {
                 {
                     Arena ar(h);
-                    CT_TRY(ct_env_right_run(h, ar, CT_PREC_FP64, rh, sites[i], mpo_sites[i], rh2, Dl, d, Dr, wl, wr));
+                    CT_TRY(ct_env_right_run(h, ar, prec, rh, sites[i], mpo_sites[i], rh2, Dl, d, Dr, wl, wr));
                 }
                 Arena ar(h);
-                CT_TRY(ct_env_right_run(h, ar, CT_PREC_FP64, rn, sites[i], Wid.p, rn2, Dl, d, Dr, 1, 1));
+                CT_TRY(ct_env_right_run(h, ar, prec, rn, sites[i], Wid.p, rn2, Dl, d, Dr, 1, 1));
+                int eh = 0, en = 0;
+                CT_TRY(renorm(rh2, (int64_t)hsize(i), &eh));
+                CT_TRY(renorm(rn2, (int64_t)nsize(i), &en));
+                cumHR[i] = cumHR[i + 1] + eh;
+                cumNR[i] = cumNR[i + 1] + en;
                 std::swap(rh, rh2);
                 std::swap(rn, rn2);
             }

@@ -99,6 +99,9 @@ size_t ct_tc_heff_ws_bytes(int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_
 int ct_tc_heff_prepare(ct_handle* h, Arena& ar, HeffPlan& p);
 int ct_tc_heff_run(ct_handle* h, const HeffPlan& p, const double* theta, double* out, const int* skip);
 size_t ct_tc_env_ws_bytes(int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR);
+size_t ct_tc_heff1_ws_bytes(int64_t Dl, int64_t d, int64_t Dr, int64_t wl, int64_t wr);
+int ct_tc_heff1_run(ct_handle* h, Arena& ar, const double* L, const double* A, const double* W, const double* R,
+                    double* out, int64_t Dl, int64_t d, int64_t Dr, int64_t wl, int64_t wr);
 int ct_tc_env_left_run(ct_handle* h, Arena& ar, const double* Lp, const double* A, const double* W, double* Ln,
                        int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR);
 int ct_tc_env_right_run(ct_handle* h, Arena& ar, const double* Rn, const double* A, const double* W, double* Rp,

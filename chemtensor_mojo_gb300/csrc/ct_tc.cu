@@ -1129,6 +1129,62 @@ int ct_tc_heff_run(ct_handle* h, const HeffPlan& p, const double* theta, double*
     return CT_OK;
 }
 
+// One-site effective Hamiltonian (the local adjoint of the environment chain):
+//   out[(Dl' s'), Dr'] = sum L[wl,Dl,Dl'] A[Dl,s,Dr] W[wl,s,s',wr] R[wr,Dr,Dr']
+// the two-site apply's chain with one physical leg: L . A on the tensor cores,
+// the MPO leg into split planes with per-wr padding, then . R.
+size_t ct_tc_heff1_ws_bytes(int64_t Dl, int64_t d, int64_t Dr, int64_t wl, int64_t wr) {
+    const int64_t Dlp = ct_round_up(Dl, TC_BK), Drp = ct_round_up(Dr, TC_BK);
+    return split_bytes(wl * Dl, Dlp) + split_bytes(Dr, wr * Drp) + split_bytes(d * Dr, Dlp) +
+           split_bytes(Dl * d, wr * Drp) + ct_bytes((size_t)(Dl * wl * d * Dr), 4) +
+           ct_bytes((size_t)((d * wr) * (wl * d)), 8) + 1024;
+}
+
+int ct_tc_heff1_run(ct_handle* h, Arena& ar, const double* L, const double* A, const double* W, const double* R,
+                    double* out, int64_t Dl, int64_t d, int64_t Dr, int64_t wl, int64_t wr) {
+    const int64_t Dlp = ct_round_up(Dl, TC_BK), Drp = ct_round_up(Dr, TC_BK);
+    const int64_t n1 = d * Dr, K4 = wr * Drp;
+    SplitOperand Lp = take_split(ar, wl * Dl, Dlp);
+    SplitOperand R4 = take_split(ar, Dr, K4);
+    SplitOperand th = take_split(ar, n1, Dlp);
+    SplitOperand A4 = take_split(ar, Dl * d, K4);
+    float* T1 = ar.take<float>((size_t)(Dl * wl * n1));
+    double* Wt = ar.take<double>((size_t)((d * wr) * (wl * d)));
+    if (!Lp.lo || !R4.lo || !th.lo || !A4.lo || !T1 || !Wt) return CT_ERR_OOM;
+    CT_TRY(ct_build_wt_left(h, W, Wt, wl, d, wr));
+    // L[wl, Dl, Dl'] -> Lp[(wl, Dl')][Dl]
+    CT_TRY(pack_launch(h, pack_desc(L, wl * Dl, Dl, Dl * Dl, 1, Dl, Dl, Lp), false, nullptr));
+    {   // R[wr, Dr, Dr'] -> R4[Dr'][(wr, Dr)] with per-wr padding
+        PackDesc pd{};
+        pd.src = R;
+        pd.rows = Dr; pd.R0 = Dr; pd.s_r1 = 0; pd.s_r0 = 1;
+        pd.K1 = wr; pd.K0 = Dr; pd.K0p = Drp; pd.s_k1 = Dr * Dr; pd.s_k0 = Dr;
+        pd.hi = R4.hi; pd.lo = R4.lo; pd.ldk = K4;
+        pd.scale = 1.0;
+        CT_TRY(pack_launch(h, pd, false, nullptr));
+    }
+    // A[Dl, (s Dr)] -> th[(s Dr)][Dl]
+    CT_TRY(pack_launch(h, pack_desc(A, n1, n1, 0, 1, Dl, n1, th), false, nullptr));
+    {   // T1[Dl'][wl][(s Dr)] (fp32) = Lp . th^T
+        TcEpi e{};
+        e.C = T1; e.out_fp64 = 0; e.M0 = Dl; e.sCm1 = n1; e.sCm0 = wl * n1; e.alpha = 1.0; e.beta = 0.0;
+        CT_TRY(tc_gemm_launch(h, Lp, th, wl * Dl, n1, e, nullptr));
+    }
+    CT_CUDA(h, cudaMemsetAsync(A4.hi, 0, (size_t)(A4.rows * A4.ldk) * 4, h->stream));
+    CT_CUDA(h, cudaMemsetAsync(A4.lo, 0, (size_t)(A4.rows * A4.ldk) * 4, h->stream));
+    {   // A4[(Dl' s')][(wr, Dr)] = Wt . T1
+        MpoTcDesc m{};
+        m.O = Dl; m.K = wl * d; m.J = d * wr; m.I = Dr;
+        m.in = T1; m.sIo = wl * d * Dr; m.sIk = Dr; m.sIi = 1;
+        m.hi = A4.hi; m.lo = A4.lo; m.sOo = d * K4; m.sOi = 1; m.J0 = wr; m.sOj1 = K4; m.sOj0 = Drp;
+        m.Wt = Wt;
+        CT_TRY(mpo_tc_launch(h, m));
+    }
+    TcEpi e{};   // out[(Dl' s')][Dr'] = A4 . R4^T (fp64)
+    e.C = out; e.out_fp64 = 1; e.M0 = Dl * d; e.sCm1 = 0; e.sCm0 = Dr; e.alpha = 1.0; e.beta = 0.0;
+    return tc_gemm_launch(h, A4, R4, Dl * d, Dr, e, nullptr);
+}
+
 size_t ct_tc_env_ws_bytes(int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR) {
     const int64_t Dlp = ct_round_up(Dl, TC_BK), Drp = ct_round_up(Dr, TC_BK);
     const int64_t K3l = ct_round_up(Dl * d, TC_BK), K3r = ct_round_up(d * Dr, TC_BK);

@@ -99,3 +99,33 @@ def test_autograd_function_bose_hubbard(ctx):
         fd = (energy_cpu(plus, mpo_a) - energy_cpu(minus, mpo_a)) / (2 * h)
         g = sites[i].grad[idx].item()
         assert abs(g - fd) <= 1e-6 * gmax
+
+
+@pytest.mark.parametrize("case", ["bose_hubbard", "xxz_ragged"])
+def test_tf32x3_gradient_matches_fp64(ctx, case):
+    """The mixed form of the adjoint (environments and one-site effective Hamiltonians on the
+    tensor cores, TF32x3) against the FP64 adjoint.  Each environment step carries FP32-level
+    rounding (~sqrt(K) 6e-8 relative for K-term sums, K up to 512 here), which random-walks
+    along the chain: over 32 unnormalised random sites that is a few 1e-6 on the energy
+    (2.4e-6 measured).  Bounds: energy 3e-5, gradient 3e-4 relative (normwise).  The FP64
+    adjoint is the one held to the 1e-6 finite-difference bound above."""
+    import chemtensor_mojo_gb300 as ct
+    from chemtensor_mojo_gb300.autograd import energy_and_gradient
+    if case == "bose_hubbard":
+        L, d, chi = 32, 4, 128
+        mpo_a = oh.bose_hubbard(L, d, t=1.0, u=4.0, mu=0.0)
+        mps = [a for a in orng.gaussian_mps(L, d, chi, 3)[0]]
+    else:
+        L = 12
+        mpo_a = oh.heisenberg_xxz(L, J=1.0, D=0.7, h=0.1)
+        rng = np.random.default_rng(4)
+        dims = [1, 2, 4, 8, 16, 33, 45, 37, 16, 8, 4, 2, 1]
+        mps = [rng.standard_normal((dims[i], 2, dims[i + 1])) / np.sqrt(2 * dims[i]) for i in range(L)]
+    mpo = ct.mpo_from_arrays(ctx, mpo_a)
+    E64, g64 = energy_and_gradient(mpo, dev_sites(mps), checkpoint_every=5, ctx=ctx, prec="fp64")
+    Etc, gtc = energy_and_gradient(mpo, dev_sites(mps), checkpoint_every=5, ctx=ctx, prec="tf32x3")
+    num = float(torch.sqrt(sum(((a - b) ** 2).sum() for a, b in zip(gtc, g64))))
+    den = float(torch.sqrt(sum((b ** 2).sum() for b in g64)))
+    print(f"{case}: energy rel diff {abs(Etc - E64) / abs(E64):.3e}, gradient rel diff {num / den:.3e}")
+    assert abs(Etc - E64) <= 3e-5 * abs(E64)
+    assert num <= 3e-4 * den
