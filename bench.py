@@ -216,7 +216,9 @@ def hubbard_mode(args):
         first = False
         free, _ = torch.cuda.mem_get_info()
         peak_used = max(peak_used, total - free)
-        log.append({"chi_max": chi, "sweeps": ns, "seconds_per_sweep": st.seconds_total / ns,
+        log.append({"chi_max": chi, "sweeps": ns,
+                    "seconds_per_sweep": (st.seconds_total - st.seconds_rayleigh) / ns,
+                    "seconds_final_rayleigh_fp64": st.seconds_rayleigh, "completed_rows": st.completed_rows,
                     "sweep_energies": st.sweep_energies, "energy_rayleigh": st.energy_rayleigh,
                     "subspace_splits": st.subspace_splits, "cold_splits": st.cold_splits,
                     "exact_splits": st.exact_splits, "heff_tflops": st.heff_flops / max(st.seconds_lanczos, 1e-12) / 1e12,

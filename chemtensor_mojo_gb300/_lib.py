@@ -51,7 +51,8 @@ class ct_dmrg_stats(C.Structure):
                 ("seconds_env", C.c_double), ("heff_flops", C.c_double), ("env_flops", C.c_double),
                 ("heff_applies", C.c_int64), ("local_updates", C.c_int64), ("max_discarded", C.c_double),
                 ("energy_rayleigh", C.c_double), ("subspace_splits", C.c_int64), ("exact_splits", C.c_int64),
-                ("seconds_subspace", C.c_double), ("cold_splits", C.c_int64)]
+                ("seconds_subspace", C.c_double), ("cold_splits", C.c_int64),
+                ("completed_rows", C.c_int64), ("seconds_rayleigh", C.c_double)]
 
 
 P = C.c_void_p

@@ -259,6 +259,7 @@ struct SvdOut {
     double min_pivot = 0.0;   // subspace split: smallest Cholesky pivot of the first pass,
     double min_pivot2 = 0.0;  // of the second pass,
     int chol_fail = 0;        // and whether a pivot was not positive
+    int replaced = 0;         // rows replaced by the rank completion of a first visit
 };
 // tensor-core path (ct_tc.cu)
 struct TcGemm;

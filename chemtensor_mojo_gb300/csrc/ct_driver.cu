@@ -244,7 +244,7 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
                     bool ok = false;
                     CT_TRY(ct_split_subspace(h, ar, th_opt.p, m, n, c, l2r ? 0 : 1, src.p, own.p,
                                              mps_sites[i], mps_sites[i + 1], h->d_scalars + SC_THETA_NSQ,
-                                             P->eps_trunc, src.disc, P->split_power_steps, &so, &ok));
+                                             P->eps_trunc, src.disc, P->split_power_steps, false, 0, &so, &ok));
                     done_split = ok;
                     last_split_subspace = ok;
                     if (P->verbose >= 2)
@@ -272,16 +272,18 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
                     bool ok = false;
                     CT_TRY(ct_split_subspace(h, ar, th_opt.p, m, n, c, l2r ? 0 : 1, X, own.p, mps_sites[i],
                                              mps_sites[i + 1], h->d_scalars + SC_THETA_NSQ, P->eps_trunc, -1.0,
-                                             P->cold_power_steps, &so, &ok));
+                                             P->cold_power_steps, true, seed, &so, &ok));
                     ar.off = mark;
                     done_split = ok;
                     last_split_subspace = ok;
                     if (P->verbose >= 2)
-                        fprintf(stderr, "bond %d %s: cold subspace split %s (%lld kept rows reused)\n", i,
-                                l2r ? "L->R" : "R->L", ok ? "accepted" : "refused", reuse ? (long long)src.c : 0ll);
+                        fprintf(stderr, "bond %d %s: cold subspace split %s (%lld kept rows reused, %d rows completed)\n",
+                                i, l2r ? "L->R" : "R->L", ok ? "accepted" : "refused", reuse ? (long long)src.c : 0ll,
+                                so.replaced);
                     if (ok) {
                         st.subspace_splits++;
                         st.cold_splits++;
+                        st.completed_rows += so.replaced;
                         own.len = own_len;
                         own.c = c;
                         own.disc = -1.0;   // no reference: the next visit must not be judged against it
@@ -324,7 +326,7 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
                     bool ok = false;
                     CT_TRY(ct_split_subspace(h, ar3, th_opt.p, m, n, c0, l2r ? 0 : 1, basis, bc->p,
                                              mps_sites[i], mps_sites[i + 1], h->d_scalars + SC_THETA_NSQ, 0.0,
-                                             -1.0, 0, &s1, &ok));
+                                             -1.0, 0, false, 0, &s1, &ok));
                     if (ok) {
                         so = s0;
                         done_split = true;
@@ -418,10 +420,12 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
     *energy_host = energy;
     st.energy_rayleigh = NAN;
     if (P->final_rayleigh) {
+        const auto t_rq = std::chrono::steady_clock::now();
         double e = 0.0, nsq = 0.0;
         CT_TRY(ct_mps_expectation(h, CT_PREC_FP64, N, d, mpo_dims, mpo_sites, bd, (const double* const*)mps_sites,
                                   &e, &nsq));
         st.energy_rayleigh = e / nsq;
+        st.seconds_rayleigh = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_rq).count();
     }
     if (sweeps_done_host) *sweeps_done_host = sweeps_done;
     if (discarded_host)

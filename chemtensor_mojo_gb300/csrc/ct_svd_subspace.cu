@@ -41,6 +41,17 @@
 // tensor-core GEMM; the residual is orthogonal to the kept part, so the
 // products' rounding enters only at second order).
 //
+// Rank completion (first visits only).  When theta's numerical rank is below
+// c -- the first visit of a bond at a larger chi_max, where theta still
+// carries the old bond's rank up to small Lanczos corrections -- rows of
+// X theta^T have no direction left outside the rows before them.  With
+// completion enabled, a first-pass pivot below MIN_PIVOT marks its row instead
+// of failing (the row's factor entry becomes 1), the marked rows of the pass-1
+// output are replaced by fresh Gaussian rows, and the second pass runs the full
+// Cholesky.  The replacements stand in for directions that carry less than
+// MIN_PIVOT of the row's weight; the discarded weight is still measured from
+// the residual.
+//
 // The split is refused (the caller falls back to the Jacobi SVD) when the
 // Cholesky factorisation breaks down, when the discarded weight exceeds
 // 4x that of the previous visit of the bond plus 1e-8 (the cached basis no
@@ -52,9 +63,35 @@ namespace {
 
 constexpr int CH_NB = 64;            // Cholesky block
 constexpr int FL_CHOL_FAIL = 100;    // d_flags slot: non-positive pivot seen
+constexpr int FL_DEF_COUNT = 101;    // d_flags slot: rows marked for replacement in a first pass
 // smallest accepted Cholesky pivot of a first pass (the squared share of a
 // normalised row outside the span of the rows before it)
 constexpr double MIN_PIVOT = 1e-12;
+
+// counter-based N(0,1) values: splitmix64 of (seed, index), Box-Muller
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double randn_at(uint64_t seed, uint64_t t) {
+    const uint64_t a = mix64(seed ^ mix64(t * 2)), b = mix64(seed ^ mix64(t * 2 + 1));
+    const double u1 = ((double)(a >> 11) + 1.0) * (1.0 / 9007199254740993.0);   // (0, 1]
+    const double u2 = (double)(b >> 11) * (1.0 / 9007199254740992.0);
+    return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+// rows[k] (k < count) of Y (rows x len) <- Gaussian rows; one block per listed row
+__global__ void replace_rows_kernel(double* Y, int64_t len, const int* rows, const int* count, int cap,
+                                    uint64_t seed) {
+    const int n = min(*count, cap);
+    for (int k = blockIdx.x; k < n; k += gridDim.x) {
+        const int64_t r = rows[k];
+        for (int64_t i = threadIdx.x; i < len; i += blockDim.x)
+            Y[r * len + i] = randn_at(seed, (uint64_t)(r * len + i));
+    }
+}
 
 __global__ void row_normalize_kernel(double* Y, int64_t rows, int64_t len) {
     const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
@@ -94,7 +131,8 @@ __global__ void chol_prepare_kernel(double* G, double* Linv, int64_t c, int64_t 
 // flagged; the smallest pivot goes to *minpiv (bit pattern, atomicMin; pivots
 // are >= 0 when recorded).  256 threads: 8 warps own the rows of the update.
 __global__ void __launch_bounds__(256) chol_diag_kernel(double* G, double* Linv, int64_t ld,
-                                                        unsigned long long* minpiv, int* fail) {
+                                                        unsigned long long* minpiv, int* fail, int* defrows,
+                                                        int* defcount, int64_t row0, double floor) {
     using T = double;
     extern __shared__ __align__(16) unsigned char chol_smem_raw[];   // two CH_NB x (CH_NB + 1) tiles
     T(*A)[CH_NB + 1] = reinterpret_cast<T(*)[CH_NB + 1]>(chol_smem_raw);
@@ -112,11 +150,18 @@ __global__ void __launch_bounds__(256) chol_diag_kernel(double* G, double* Linv,
     for (int j = 0; j < CH_NB; ++j) {
         if (t == 0) {
             double p = (double)A[j][j];
-            if (!(p > 0.0) || !isfinite(p)) {
+            if (floor > 0.0 && isfinite(p) && p < floor) {
+                // no direction left outside the rows before: mark the row for replacement
+                const int k = atomicAdd(defcount, 1);
+                defrows[k] = (int)(row0 + j);
+                p = 1.0;
+            } else if (!(p > 0.0) || !isfinite(p)) {
                 *fail = 1;
                 p = 1.0;
+                mp = fmin(mp, p);
+            } else {
+                mp = fmin(mp, p);
             }
-            mp = fmin(mp, p);
             const T dj = (T)sqrt(p);
             A[j][j] = dj;
             rinv = (T)1 / dj;
@@ -204,8 +249,16 @@ int fac_gemm(ct_handle* h, int64_t M, int64_t N, int64_t K, const double* A, int
 // The large products run as whole FP64 GEMMs, the 64 x 64 leaves in one CTA.
 // S is scratch of (n/2)^2 doubles; it is free again whenever a recursive
 // call runs.
+// Rows whose pivot falls below `floor` (> 0) are recorded in defrows (row0 is
+// the global index of the block's first row) instead of failing.
+struct CholMarks {
+    int* rows = nullptr;
+    int* count = nullptr;
+    double floor = 0.0;
+};
+
 int chol_inv(ct_handle* h, double* G, double* Linv, int64_t ld, int64_t n, double* S,
-             unsigned long long* d_minpiv, int* d_fail) {
+             unsigned long long* d_minpiv, int* d_fail, const CholMarks& mk, int64_t row0) {
     if (n <= CH_NB) {
         constexpr int smem = 2 * CH_NB * (CH_NB + 1) * (int)sizeof(double);
         static int attr_dev = -1;
@@ -213,7 +266,9 @@ int chol_inv(ct_handle* h, double* G, double* Linv, int64_t ld, int64_t n, doubl
             CT_CUDA(h, cudaFuncSetAttribute(chol_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
             attr_dev = h->device;
         }
-        chol_diag_kernel<<<1, 256, smem, h->stream>>>(G, Linv, ld, d_minpiv, d_fail); ct_note_launch();
+        chol_diag_kernel<<<1, 256, smem, h->stream>>>(G, Linv, ld, d_minpiv, d_fail, mk.rows, mk.count, row0,
+                                                      mk.rows ? mk.floor : 0.0);
+        ct_note_launch();
         CT_LAUNCH_CHECK(h);
         return CT_OK;
     }
@@ -222,14 +277,14 @@ int chol_inv(ct_handle* h, double* G, double* Linv, int64_t ld, int64_t n, doubl
     double* G22 = G21 + n1;
     double* I21 = Linv + n1 * ld;
     double* I22 = I21 + n1;
-    CT_TRY(chol_inv(h, G, Linv, ld, n1, S, d_minpiv, d_fail));
+    CT_TRY(chol_inv(h, G, Linv, ld, n1, S, d_minpiv, d_fail, mk, row0));
     // L21 = G21 inv(L11)^T -> S -> G21
     CT_TRY(fac_gemm(h, n2, n1, n1, G21, ld, Linv, ld, 1, S, n1, 1.0, 0.0, 0));
     CT_CUDA(h, cudaMemcpy2DAsync(G21, (size_t)ld * 8, S, (size_t)n1 * 8, (size_t)n1 * 8, (size_t)n2,
                                  cudaMemcpyDeviceToDevice, h->stream));
     // G22 -= L21 L21^T (lower tiles only)
     CT_TRY(fac_gemm(h, n2, n2, n1, G21, ld, G21, ld, 1, G22, ld, -1.0, 1.0, 1));
-    CT_TRY(chol_inv(h, G22, I22, ld, n2, S, d_minpiv, d_fail));
+    CT_TRY(chol_inv(h, G22, I22, ld, n2, S, d_minpiv, d_fail, mk, row0 + n1));
     // inv(L)21 = -inv(L22) (L21 inv(L11))
     CT_TRY(fac_gemm(h, n2, n1, n1, G21, ld, Linv, ld, 0, S, n1, 1.0, 0.0, 0));
     CT_TRY(fac_gemm(h, n2, n1, n2, I22, ld, S, n1, 0, I21, ld, -1.0, 0.0, 2));
@@ -263,6 +318,7 @@ struct OrthBufs {
     double* Linv;   // cp x cp
     double* S;      // (cp / 2)^2 + CH_NB^2
     int64_t cp;
+    int* defrows;   // cp: rows marked by a first pass with completion
 };
 
 constexpr double ORTH_CORR_MAX = 1e-4;    // largest |Q Q^T - I| the first-order step takes
@@ -316,14 +372,17 @@ int orth_correct(ct_handle* h, Arena& ar, const double* Q, double* out, int64_t 
 // orthonormal to FP64 rounding.  Pivots of pass 1 go to d_minpiv[0], of pass 2
 // to d_minpiv[1].
 int orth_rows(ct_handle* h, Arena& ar, double* Z, double* W, int64_t c, int64_t len, const OrthBufs& ob,
-              bool two_pass, unsigned long long* d_minpiv, int* d_fail) {
+              bool two_pass, unsigned long long* d_minpiv, int* d_fail, bool complete, uint64_t seed,
+              int* replaced) {
     const int64_t cp = ob.cp;
     row_normalize_kernel<<<(unsigned)ct_cdiv(c * 32, 256), 256, 0, h->stream>>>(Z, c, len); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     double* src = Z;
     double* dst = W;
+    int* d_count = h->d_flags + FL_DEF_COUNT;
+    int nrep = 0;
     for (int pass = 0; pass < (two_pass ? 2 : 1); ++pass) {
-        if (pass == 1) {
+        if (pass == 1 && nrep == 0) {
             bool done = false;
             CT_TRY(orth_correct(h, ar, src, dst, c, len, ob, d_minpiv + 1, &done));
             if (done) {
@@ -334,8 +393,28 @@ int orth_rows(ct_handle* h, Arena& ar, double* Z, double* W, int64_t c, int64_t 
         chol_prepare_kernel<<<grid_n(h, cp * cp), 256, 0, h->stream>>>(ob.G, ob.Linv, c, cp); ct_note_launch();
         CT_LAUNCH_CHECK(h);
         CT_TRY(fac_gemm(h, c, c, len, src, len, src, len, 1, ob.G, cp, 1.0, 0.0, 1));
-        CT_TRY(chol_inv(h, ob.G, ob.Linv, cp, cp, ob.S, d_minpiv + pass, d_fail));
+        CholMarks mk;
+        if (pass == 0 && complete) {
+            CT_CUDA(h, cudaMemsetAsync(d_count, 0, sizeof(int), h->stream));
+            mk.rows = ob.defrows;
+            mk.count = d_count;
+            mk.floor = MIN_PIVOT;
+        }
+        CT_TRY(chol_inv(h, ob.G, ob.Linv, cp, cp, ob.S, d_minpiv + pass, d_fail, mk, 0));
         CT_TRY(fac_gemm(h, c, len, c, ob.Linv, cp, src, len, 0, dst, len, 1.0, 0.0, 2));
+        if (pass == 0 && complete) {
+            CT_CUDA(h, cudaMemcpyAsync(&nrep, d_count, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+            CT_CUDA(h, cudaStreamSynchronize(h->stream));
+            if (nrep > 0) {
+                const unsigned g = (unsigned)std::min<int64_t>(nrep, (int64_t)h->num_sms * 4);
+                replace_rows_kernel<<<g, 256, 0, h->stream>>>(dst, len, ob.defrows, d_count, (int)cp, seed);
+                ct_note_launch();
+                CT_LAUNCH_CHECK(h);
+                row_normalize_kernel<<<(unsigned)ct_cdiv(c * 32, 256), 256, 0, h->stream>>>(dst, c, len);
+                ct_note_launch();
+                CT_LAUNCH_CHECK(h);
+            }
+        }
         double* t = src;
         src = dst;
         dst = t;
@@ -343,6 +422,7 @@ int orth_rows(ct_handle* h, Arena& ar, double* Z, double* W, int64_t c, int64_t 
     // the result is in src: W after one pass, Z after two
     if (src != W)
         CT_CUDA(h, cudaMemcpyAsync(W, src, (size_t)(c * len) * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    if (replaced) *replaced += nrep;
     (void)ar;
     return CT_OK;
 }
@@ -353,7 +433,7 @@ size_t ct_split_subspace_ws_bytes(int64_t m, int64_t n, int64_t c) {
     const int64_t big = m > n ? m : n;
     const int64_t cp = ct_round_up(c, CH_NB);
     size_t b = 2 * ct_bytes(c * big, 8) + 2 * ct_bytes(cp * cp, 8) + ct_bytes(cp * cp / 4 + CH_NB * CH_NB, 8) +
-               ct_bytes(m * n, 8) + 4096;
+               ct_bytes(m * n, 8) + ct_bytes(cp, 4) + 4096;
     size_t g = ct_tc_gemm_ws_bytes(c, big, big);
     const size_t more[] = {ct_tc_gemm_ws_bytes(c, c, big), ct_tc_gemm_ws_bytes(big, c, big),
                            ct_tc_gemm_ws_bytes(c, big, c), ct_tc_gemm_ws_bytes(m, n, c),
@@ -377,14 +457,20 @@ struct SplitBufs {
 // The warm split (products with theta on the tensor cores, orthonormalisation in FP64).
 int split_attempt(ct_handle* h, Arena& ar, const SplitBufs& sb, const double* M, int64_t m, int64_t n, int64_t c,
                   int mode, const double* basis_in, double* basis_out, double* Aout, double* Bout,
-                  const double* d_total, double eps_trunc, double disc_ref, int power_steps, SvdOut* out,
-                  SplitVerdict* verdict) {
+                  const double* d_total, double eps_trunc, double disc_ref, int power_steps, bool complete,
+                  uint64_t seed, SvdOut* out, SplitVerdict* verdict) {
     const size_t mark = ar.off;
+    unsigned long long* d_piv = (unsigned long long*)(h->d_scalars + SC_SPLIT_PIV);   // [0] pass 1, [1] pass 2
+    int* d_fail = h->d_flags + FL_CHOL_FAIL;
     double* Z = sb.Z;
     double* W = sb.W;
     const OrthBufs& ob = sb.ob;
-    unsigned long long* d_piv = (unsigned long long*)(h->d_scalars + SC_SPLIT_PIV);   // [0] pass 1, [1] pass 2
-    int* d_fail = h->d_flags + FL_CHOL_FAIL;
+    int replaced = 0;
+    uint64_t call = 0;
+    auto orth = [&](double* Zr, double* Wr, int64_t len, bool two) {
+        return orth_rows(h, ar, Zr, Wr, c, len, ob, two, d_piv, d_fail, complete, seed + 0x9E37ull * ++call,
+                         &replaced);
+    };
     split_flags_init_kernel<<<1, 32, 0, h->stream>>>(d_piv, d_fail); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     // X: c rows over n (left-to-right) or over m (right-to-left).  The power
@@ -394,17 +480,17 @@ int split_attempt(ct_handle* h, Arena& ar, const SplitBufs& sb, const double* M,
         if (mode == 0) {
             CT_TRY(ct_tc_gemm(h, ar, 0, 1, c, m, n, 1.0, X, n, M, n, 0.0, Z, m));   // X theta^T
             ar.off = mark;
-            CT_TRY(orth_rows(h, ar, Z, W, c, m, ob, false, d_piv, d_fail));
+            CT_TRY(orth(Z, W, m, false));
             CT_TRY(ct_tc_gemm(h, ar, 0, 0, c, n, m, 1.0, W, m, M, n, 0.0, Z, n));   // . theta
             ar.off = mark;
-            CT_TRY(orth_rows(h, ar, Z, W, c, n, ob, false, d_piv, d_fail));
+            CT_TRY(orth(Z, W, n, false));
         } else {
             CT_TRY(ct_tc_gemm(h, ar, 0, 0, c, n, m, 1.0, X, m, M, n, 0.0, Z, n));   // X theta
             ar.off = mark;
-            CT_TRY(orth_rows(h, ar, Z, W, c, n, ob, false, d_piv, d_fail));
+            CT_TRY(orth(Z, W, n, false));
             CT_TRY(ct_tc_gemm(h, ar, 0, 1, c, m, n, 1.0, W, n, M, n, 0.0, Z, m));   // . theta^T
             ar.off = mark;
-            CT_TRY(orth_rows(h, ar, Z, W, c, m, ob, false, d_piv, d_fail));
+            CT_TRY(orth(Z, W, m, false));
         }
         X = W;
     }
@@ -412,7 +498,7 @@ int split_attempt(ct_handle* h, Arena& ar, const SplitBufs& sb, const double* M,
         // Q = orth(X theta^T) -> basis_out; A = Q^T; B = Q theta
         CT_TRY(ct_tc_gemm(h, ar, 0, 1, c, m, n, 1.0, X, n, M, n, 0.0, Z, m));
         ar.off = mark;
-        CT_TRY(orth_rows(h, ar, Z, basis_out, c, m, ob, true, d_piv, d_fail));
+        CT_TRY(orth(Z, basis_out, m, true));
         CT_TRY(ct_tc_gemm(h, ar, 0, 0, c, n, m, 1.0, basis_out, m, M, n, 0.0, Bout, n));
         ar.off = mark;
         transpose_copy_kernel<<<grid_n(h, c * m), 256, 0, h->stream>>>(basis_out, c, m, Aout); ct_note_launch();
@@ -421,7 +507,7 @@ int split_attempt(ct_handle* h, Arena& ar, const SplitBufs& sb, const double* M,
         // V = orth(X theta) -> B and basis_out; A = theta V^T
         CT_TRY(ct_tc_gemm(h, ar, 0, 0, c, n, m, 1.0, X, m, M, n, 0.0, Z, n));
         ar.off = mark;
-        CT_TRY(orth_rows(h, ar, Z, Bout, c, n, ob, true, d_piv, d_fail));
+        CT_TRY(orth(Z, Bout, n, true));
         CT_CUDA(h, cudaMemcpyAsync(basis_out, Bout, (size_t)(c * n) * sizeof(double), cudaMemcpyDeviceToDevice,
                                    h->stream));
         CT_TRY(ct_tc_gemm(h, ar, 0, 1, m, c, n, 1.0, M, n, Bout, n, 0.0, Aout, c));
@@ -451,7 +537,10 @@ int split_attempt(ct_handle* h, Arena& ar, const SplitBufs& sb, const double* M,
     out->min_pivot = piv1;
     out->min_pivot2 = piv2;
     out->chol_fail = fail;
-    if (fail || !(piv1 >= MIN_PIVOT) || !(piv2 > 0.5)) {
+    out->replaced = replaced;
+    // a second pass over nearly orthonormal rows has pivots near 1; completed
+    // rows are random and keep (len - c) / len of their weight outside the rest
+    if (fail || !(piv1 >= MIN_PIVOT) || !(piv2 > (replaced ? 1e-3 : 0.5))) {
         *verdict = SPLIT_BREAKDOWN;
     } else if (disc_ref >= 0.0 && disc > 4.0 * disc_ref + 1e-8) {
         *verdict = SPLIT_STALE;   // much more weight lost than at the previous visit of the bond
@@ -467,8 +556,8 @@ int split_attempt(ct_handle* h, Arena& ar, const SplitBufs& sb, const double* M,
 
 int ct_split_subspace(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t c, int mode,
                       const double* basis_in, double* basis_out, double* Aout, double* Bout,
-                      const double* d_total, double eps_trunc, double disc_ref, int power_steps, SvdOut* out,
-                      bool* accepted) {
+                      const double* d_total, double eps_trunc, double disc_ref, int power_steps, bool complete,
+                      uint64_t seed, SvdOut* out, bool* accepted) {
     *accepted = false;
     const int64_t big = m > n ? m : n;
     SplitBufs sb{};
@@ -479,29 +568,19 @@ int ct_split_subspace(ct_handle* h, Arena& ar, const double* M, int64_t m, int64
     sb.ob.Linv = ar.take<double>(sb.ob.cp * sb.ob.cp);
     sb.ob.S = ar.take<double>(sb.ob.cp * sb.ob.cp / 4 + CH_NB * CH_NB);
     sb.R = ar.take<double>(m * n);
-    if (!sb.Z || !sb.W || !sb.ob.G || !sb.ob.Linv || !sb.ob.S || !sb.R) return CT_ERR_OOM;
+    sb.ob.defrows = ar.take<int>(sb.ob.cp);
+    if (!sb.Z || !sb.W || !sb.ob.G || !sb.ob.Linv || !sb.ob.S || !sb.R || !sb.ob.defrows) return CT_ERR_OOM;
     SplitVerdict v = SPLIT_BREAKDOWN;
     CT_TRY(split_attempt(h, ar, sb, M, m, n, c, mode, basis_in, basis_out, Aout, Bout, d_total, eps_trunc,
-                         disc_ref, power_steps, out, &v));
+                         disc_ref, power_steps, complete, seed, out, &v));
     *accepted = (v == SPLIT_OK);
     return CT_OK;
 }
 
 namespace {
-// counter-based N(0,1) fill: splitmix64 of (seed, index), Box-Muller
-__device__ __forceinline__ uint64_t mix64(uint64_t z) {
-    z += 0x9E3779B97F4A7C15ull;
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-}
 __global__ void randn_fill_kernel(double* X, int64_t n, uint64_t seed) {
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-        const uint64_t a = mix64(seed ^ mix64((uint64_t)t * 2)), b = mix64(seed ^ mix64((uint64_t)t * 2 + 1));
-        const double u1 = ((double)(a >> 11) + 1.0) * (1.0 / 9007199254740993.0);   // (0, 1]
-        const double u2 = (double)(b >> 11) * (1.0 / 9007199254740992.0);
-        X[t] = sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
-    }
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        X[t] = randn_at(seed, (uint64_t)t);
 }
 }  // namespace
 

@@ -186,6 +186,8 @@ typedef struct ct_dmrg_stats {
     int64_t exact_splits;      /* Jacobi-SVD splits                              */
     double seconds_subspace;   /* part of seconds_svd spent in subspace splits   */
     int64_t cold_splits;       /* subspace splits started from random rows       */
+    int64_t completed_rows;    /* rows a first visit's rank completion replaced  */
+    double seconds_rayleigh;   /* the final FP64 <H> (final_rayleigh), included in seconds_total */
 } ct_dmrg_stats;
 
 /* Runs the sweeps in place.  mps_sites[i] are caller-owned device buffers of

@@ -324,3 +324,36 @@ def test_svd_split_warm_entry(ctx, l2r):
     canon = a.T if l2r else b
     # same row space: projecting the kept rows on the canonical rows loses nothing
     assert np.abs(kept @ canon.T @ canon - kept).max() < 1e-10
+
+
+def test_dmrg_cold_split_rank_completion(ctx):
+    """A chi ramp with d = 4 and a step smaller than d (Bose-Hubbard L=12, chi 32 -> 64): on the
+    first left-to-right visit at chi = 64, theta is (4 Dl) x (4 Dr) with the right bond still at
+    32, so its numerical rank is about 32 while 64 states are kept.  The cold subspace split
+    completes the missing rows with random ones instead of falling back to the Jacobi SVD: rows
+    are completed, the sites stay right-canonical, and after the ramp the FP64 Rayleigh energy
+    matches the FP64 form (same ramp, Jacobi splits) to 1e-8."""
+    ct = ct_mod()
+    L, d = 12, 4
+    mpo_a = oh.bose_hubbard(L, d, t=1.0, u=4.0, mu=0.0)
+    sites, _ = orng.create_random_mps_c_compatible(L, d, 32, 7)
+    mps_a = od.right_normalize(sites)
+    res = {}
+    for prec, cold in (("fp64", -1), ("tf32x3", 2)):
+        mps = ct.mps_from_arrays(ctx, mps_a)
+        stages = []
+        for k, (chi, ns) in enumerate(((32, 2), (64, 3))):
+            st = ct.DMRGStats()
+            p = ct.DMRGParams(num_sweeps=ns, chi_max=chi, eps_trunc=0.0, max_krylov_iter=20, krylov_tol=1e-10,
+                              energy_tol=0.0, max_rotations=0, prec=prec, final_rayleigh=True,
+                              keep_bases=k > 0, cold_power_steps=cold)
+            E, mps = ct.dmrg_two_site(ctx, ct.mpo_from_arrays(ctx, mpo_a), mps, p, st)
+            stages.append(st)
+        res[prec] = (stages, mps)
+    st_b = res["tf32x3"][0][1]
+    assert st_b.completed_rows > 0
+    for a in res["tf32x3"][1].to_numpy()[1:]:
+        mat = a.reshape(a.shape[0], -1)
+        assert np.abs(mat @ mat.T - np.eye(a.shape[0])).max() < 1e-12
+    e64 = res["fp64"][0][1].energy_rayleigh
+    assert abs(st_b.energy_rayleigh - e64) <= 1e-8 * abs(e64)
