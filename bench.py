@@ -59,8 +59,8 @@ RAMP = [64, 256, 1024]
 # the difference measures precision rather than early-trajectory noise
 ACC_RAMP = (64, 256, 256, 256, 256)
 # dram__bytes_read.sum + dram__bytes_write.sum of one centre-bond H_eff GEMM launch
-# (5120 x 4096 x 1024, chi=1024) from ncu; profiles/tc_gemm_kernel_heff_chi1024.md
-TC_GEMM_TRAFFIC_BYTES = (78.5 + 55.7) * 1e6
+# (5120 x 4096 x 1024 at chi=1024, 128x256 tiles) from an ncu --set full capture
+TC_GEMM_TRAFFIC_BYTES = (79.3 + 46.4) * 1e6
 METRIC = "DMRG sweep s & H_eff TFLOP/s, mixed-prec vs FP64 on GPU at |dE/E|<=1e-9"
 
 
