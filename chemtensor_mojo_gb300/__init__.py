@@ -9,11 +9,12 @@ the library or a CUDA device is missing.
 from ._lib import CTDMRGError, load as load_library  # noqa: F401
 from .dense_tensor import (DenseTensor, DeviceContext, create_dense_tensor, create_dense_tensor_from_data,  # noqa
                            create_dense_tensor_random, create_dense_tensor_uninitialized, dense_tensor_dot,
-                           dense_tensor_svd_trunc, get_context)
+                           dense_tensor_qr, dense_tensor_svd_trunc, get_context)
 from .mps_state import (MatrixProductOperator, MatrixProductState, MPOSite, MPSSite, create_identity_mpo,  # noqa
                         create_product_mps, create_random_mps_c_compatible, create_single_site_op_mpo,
                         create_two_site_op_mpo, create_uniform_mps, mpo_from_arrays, mps_from_arrays, mps_norm,
-                        mps_right_normalize, mps_to_statevector, random_mps_c_compatible_arrays)
+                        mps_local_orthonormalize_qr, mps_orthogonalize_qr, mps_right_normalize,
+                        mps_to_statevector, random_mps_c_compatible_arrays)
 from .hamiltonians import (create_bose_hubbard_mpo, create_fermi_hubbard_mpo, create_heisenberg_mpo,  # noqa
                            create_heisenberg_xxz_mpo, create_ising_1d_mpo, create_spin_half_xxz_mpo,
                            create_transverse_ising_mpo)

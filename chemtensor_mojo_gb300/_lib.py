@@ -97,6 +97,7 @@ SIGNATURES = {
                             C.POINTER(D)],
     "ct_mpo_compose_site": [P, P, P, P, I64, I64, I64, I64, I64, I64, I64],
     "ct_apply_mpo_site": [P, P, P, P, I64, I64, I64, I64, I64, I64],
+    "ct_qr": [P, P, I64, I64, P, P, C.POINTER(I32)],
     "ct_random_mps_host": [I32, I32, I32, C.c_uint64, C.POINTER(I64), PP],
     "ct_rng_randnf_host": [C.c_uint64, I64, C.POINTER(C.c_float)],
     "ct_tc_gemm_time": [P, I64, I64, I64, I32, C.POINTER(D)],

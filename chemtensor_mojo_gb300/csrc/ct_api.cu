@@ -529,6 +529,27 @@ int ct_svd_trunc(ct_handle* h, const double* M, int64_t m, int64_t n, int64_t ch
     return CT_OK;
 }
 
+int ct_qr(ct_handle* h, const double* A, int64_t m, int64_t n, double* Q, double* R, int* completed_host) {
+    CT_NULLCHK(h, h);
+    if (m < 0 || n < 0) return CT_ERR_SHAPE;
+    if (completed_host) *completed_host = 0;
+    if (m == 0 || n == 0) return CT_OK;
+    CT_NULLCHK(h, A);
+    CT_NULLCHK(h, Q);
+    CT_NULLCHK(h, R);
+    if (!ct_tc_available(h)) {
+        ct_seterr(h, "ct_qr: the orthonormalisation's correction step needs the sm_103a tensor-core path");
+        return CT_ERR_UNSUPPORTED;
+    }
+    CT_TRY(ct_reserve(h, ct_qr_ws_bytes(m, n)));
+    Arena ar(h);
+    int done = 0;
+    CT_TRY(ct_qr_run(h, ar, A, m, n, Q, R, &done));
+    CT_TRY(check_status(h));
+    if (completed_host) *completed_host = done;
+    return CT_OK;
+}
+
 int ct_svd_split(ct_handle* h, int prec, const double* theta, int64_t Dl, int64_t d, int64_t Dr, int64_t chi_max,
                  double eps_trunc, int left_to_right, double* A_out, double* B_out, double* S_out, int64_t* chi_host,
                  double* discarded_host) {

@@ -84,6 +84,9 @@ size_t ct_split_subspace_ws_bytes(int64_t m, int64_t n, int64_t c);
 // basis_out <- V rows.  disc_ref: discarded weight at the previous truncating
 // visit of the bond (< 0: unknown).  *accepted = false: outputs are not valid,
 // use the SVD.
+// thin QR A[m,n] = Q[m,k] R[k,n] in FP64 (ct_svd_subspace.cu)
+size_t ct_qr_ws_bytes(int64_t m, int64_t n);
+int ct_qr_run(ct_handle* h, Arena& ar, const double* A, int64_t m, int64_t n, double* Q, double* R, int* completed);
 int ct_split_subspace(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t c, int mode,
                       const double* basis_in, double* basis_out, double* Aout, double* Bout,
                       const double* d_total, double eps_trunc, double disc_ref, int power_steps, bool complete,

@@ -577,6 +577,78 @@ int ct_split_subspace(ct_handle* h, Arena& ar, const double* M, int64_t m, int64
     return CT_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Thin QR on the device (dense_tensor_qr, dense_tensor.mojo:1333-1433): A[m,n]
+// = Q[m,k] R[k,n], k = min(m,n), Q with orthonormal columns, R upper
+// triangular (trapezoidal when n > m) with a non-negative diagonal -- LAPACK's
+// Householder QR returns the same factors up to the signs of Q's columns and
+// R's rows.  The first k columns of A, as rows, go through the FP64
+// CholeskyQR of the subspace split with rank completion; R = Q^T A in FP64.
+// A column whose part outside the columns before it is below 1e-6 of its
+// norm (a first-pass pivot below 1e-12) gets a completed Q column inside the
+// same Gram-Schmidt order, so the spans stay nested and R triangular: exactly
+// dependent columns (zero, repeated, linear combinations) are reproduced to
+// FP64 rounding, a nearly dependent one to its part below that threshold.
+// ---------------------------------------------------------------------------
+namespace {
+// Z[j][i] = A[i][j], j < k  (the first k columns of A[m,n] as rows)
+__global__ void cols_to_rows_kernel(const double* A, int64_t m, int64_t n, int64_t k, double* Z) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < k * m; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = t / m, i = t % m;
+        Z[t] = A[i * n + j];
+    }
+}
+// R[i][j] = 0 for j < i
+__global__ void zero_strict_lower_kernel(double* R, int64_t k, int64_t n) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < k * n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / n, j = t % n;
+        if (j < i) R[t] = 0.0;
+    }
+}
+}  // namespace
+
+size_t ct_qr_ws_bytes(int64_t m, int64_t n) {
+    const int64_t k = std::min(m, n), cp = ct_round_up(k, CH_NB);
+    return 2 * ct_bytes(k * m, 8) + 2 * ct_bytes(cp * cp, 8) +
+           ct_bytes(cp * cp / 4 + CH_NB * CH_NB, 8) + ct_bytes(cp, 4) + ct_tc_gemm_ws_bytes(k, m, k) + 4096;
+}
+
+int ct_qr_run(ct_handle* h, Arena& ar, const double* A, int64_t m, int64_t n, double* Q, double* R,
+              int* completed) {
+    const int64_t k = std::min(m, n);
+    OrthBufs ob;
+    ob.cp = ct_round_up(k, CH_NB);
+    double* Z = ar.take<double>(k * m);
+    double* W = ar.take<double>(k * m);
+    ob.G = ar.take<double>(ob.cp * ob.cp);
+    ob.Linv = ar.take<double>(ob.cp * ob.cp);
+    ob.S = ar.take<double>(ob.cp * ob.cp / 4 + CH_NB * CH_NB);
+    ob.defrows = ar.take<int>(ob.cp);
+    if (!Z || !W || !ob.G || !ob.Linv || !ob.S || !ob.defrows) return CT_ERR_OOM;
+    unsigned long long* d_piv = (unsigned long long*)(h->d_scalars + SC_SPLIT_PIV);
+    int* d_fail = h->d_flags + FL_CHOL_FAIL;
+    split_flags_init_kernel<<<1, 32, 0, h->stream>>>(d_piv, d_fail); ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    cols_to_rows_kernel<<<grid_n(h, k * m), 256, 0, h->stream>>>(A, m, n, k, Z); ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    int nrep = 0;
+    CT_TRY(orth_rows(h, ar, Z, W, k, m, ob, true, d_piv, d_fail, true, 0x51ED270B0ull, &nrep));
+    CT_TRY(fac_gemm(h, k, n, m, W, m, A, n, 0, R, n, 1.0, 0.0, 0));   // R = Q^T A
+    transpose_copy_kernel<<<grid_n(h, k * m), 256, 0, h->stream>>>(W, k, m, Q); ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    zero_strict_lower_kernel<<<grid_n(h, k * n), 256, 0, h->stream>>>(R, k, n); ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    int fail = 0;
+    CT_CUDA(h, cudaMemcpyAsync(&fail, d_fail, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CT_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (completed) *completed = nrep;
+    if (fail) {
+        ct_seterr(h, "ct_qr: the Cholesky factorisation met a non-finite pivot");
+        return CT_ERR_NONFINITE;
+    }
+    return CT_OK;
+}
+
 namespace {
 __global__ void randn_fill_kernel(double* X, int64_t n, uint64_t seed) {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)

@@ -276,6 +276,24 @@ def dense_tensor_dot(C_out: DenseTensor, A: DenseTensor, B: DenseTensor, ctx: De
              _ptr(C_out.storage), C.c_int64(n))
 
 
+def dense_tensor_qr(tensor: DenseTensor, ctx: DeviceContext | None = None):
+    """Thin QR on the device (dense_tensor.mojo:1333-1433) -> (Q [m,k], R [k,n]), k = min(m,n).
+
+    FP64.  diag(R) >= 0; LAPACK's Householder factors equal these up to the signs of Q's
+    columns and R's rows.  A rank-2 tensor is required, as in the reference."""
+    ctx = ctx or get_context()
+    if len(tensor.shape) != 2:
+        raise ValueError(f"QR decomposition requires a 2D matrix, got rank {len(tensor.shape)}")
+    m, n = tensor.shape
+    k = min(m, n)
+    dev = tensor.storage.device
+    Q = torch.empty(max(m * k, 1), dtype=torch.float64, device=dev)
+    R = torch.empty(max(k * n, 1), dtype=torch.float64, device=dev)
+    done = C.c_int()
+    ctx.call("ct_qr", _ptr(tensor.storage), C.c_int64(m), C.c_int64(n), _ptr(Q), _ptr(R), C.byref(done))
+    return DenseTensor(Q[:m * k], [m, k]), DenseTensor(R[:k * n], [k, n])
+
+
 def dense_tensor_svd_trunc(tensor: DenseTensor, ctx: DeviceContext | None = None, chi_max: int = 1 << 30,
                            eps_trunc: float = 1e-12):
     """Truncated thin SVD of a 2-D tensor on the device -> (U, S, Vt, chi_kept)."""

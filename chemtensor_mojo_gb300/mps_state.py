@@ -12,6 +12,11 @@ src/state/mpo_state.mojo, plus the seeded initial states.
 * ``create_identity_mpo``                       mpo_state.mojo:196-241
 * ``create_single_site_op_mpo``                 mpo_state.mojo:243-272
 * ``create_two_site_op_mpo``                    mpo_state.mojo:275-310
+* ``mps_local_orthonormalize_qr``               mps_state.mojo:307-379
+* ``mps_orthogonalize_qr``                      mps_state.mojo:382-451
+* ``MatrixProductState.left_canonicalize`` / ``right_canonicalize``
+                                                QR sweeps on the device (mps_state.mojo:170-217
+                                                is the reference's unfinished version)
 """
 from __future__ import annotations
 
@@ -23,7 +28,7 @@ import torch
 
 from . import _lib
 from .dense_tensor import (DenseTensor, DeviceContext, create_dense_tensor_from_data, dense_tensor_dot,
-                           create_dense_tensor, get_context, _ptr)
+                           dense_tensor_qr, create_dense_tensor, get_context, _ptr)
 
 
 class MPSSite:
@@ -88,6 +93,50 @@ class MatrixProductState:
 
     def to_numpy(self) -> List[np.ndarray]:
         return [s.tensor.to_numpy() for s in self.sites]
+
+    def left_canonicalize(self, ctx: DeviceContext | None = None) -> None:
+        """QR sweep left to right: every site but the last becomes left-orthonormal, R moves
+        into the next site, and the last site is normalised (in place)."""
+        ctx = ctx or get_context()
+        for i in range(self.length - 1):
+            A = self.sites[i].tensor
+            Dl, d, Dr = A.shape
+            Q, R = dense_tensor_qr(A.reshape([Dl * d, Dr]), ctx)
+            k = Q.shape[1]
+            self.sites[i] = MPSSite(Q.reshape([Dl, d, k]))
+            nxt = self.sites[i + 1].tensor
+            _, d2, Dr2 = nxt.shape
+            out = create_dense_tensor(ctx, [k, d2 * Dr2])
+            dense_tensor_dot(out, R, nxt.reshape([Dr, d2 * Dr2]), ctx)
+            self.sites[i + 1] = MPSSite(out.reshape([k, d2, Dr2]))
+            self.bond_dims[i + 1] = k
+        last = self.sites[self.length - 1].tensor
+        nrm = last.norm(ctx)
+        if nrm > 0:
+            last.scale_in_place(1.0 / nrm, ctx)
+
+    def right_canonicalize(self, ctx: DeviceContext | None = None) -> None:
+        """QR sweep right to left on the transposed sites (an LQ): every site but the first
+        becomes right-orthonormal and the first site is normalised (in place)."""
+        ctx = ctx or get_context()
+        for i in range(self.length - 1, 0, -1):
+            A = self.sites[i].tensor
+            Dl, d, Dr = A.shape
+            At = A.reshape([Dl, d * Dr]).transpose([1, 0], ctx)        # [d*Dr, Dl]
+            Q, R = dense_tensor_qr(At, ctx)                              # A^T = Q R -> A = R^T Q^T
+            k = Q.shape[1]
+            self.sites[i] = MPSSite(Q.transpose([1, 0], ctx).reshape([k, d, Dr]))
+            prev = self.sites[i - 1].tensor
+            Dl0, d0, _ = prev.shape
+            Rt = R.transpose([1, 0], ctx)                                # [Dl, k]
+            out = create_dense_tensor(ctx, [Dl0 * d0, k])
+            dense_tensor_dot(out, prev.reshape([Dl0 * d0, Dl]), Rt, ctx)
+            self.sites[i - 1] = MPSSite(out.reshape([Dl0, d0, k]))
+            self.bond_dims[i] = k
+        first = self.sites[0].tensor
+        nrm = first.norm(ctx)
+        if nrm > 0:
+            first.scale_in_place(1.0 / nrm, ctx)
 
 
 class MPOSite:
@@ -269,3 +318,46 @@ def create_two_site_op_mpo(ctx, num_sites: int, site_i: int, site_j: int, op_i_d
     arrays[site_i] = np.asarray(op_i_data, dtype=np.float64).reshape(1, 2, 2, 1)
     arrays[site_j] = np.asarray(op_j_data, dtype=np.float64).reshape(1, 2, 2, 1)
     return mpo_from_arrays(ctx, arrays)
+
+
+# -- QR construction from a dense state (mps_state.mojo:307-451) -------------------
+def mps_local_orthonormalize_qr(ctx, block: DenseTensor):
+    """Left-orthonormalise one site of a block [left, phys, rest...] -> (MPSSite [left, phys, k],
+    remainder [k, rest...]) with k = min(left*phys, prod(rest)) (mps_state.mojo:307-379)."""
+    ctx = ctx or get_context()
+    shape = list(block.shape)
+    if len(shape) < 3:
+        raise ValueError("mps_local_orthonormalize_qr requires rank >= 3 (left, physical, remainder)")
+    left, phys, tail = shape[0], shape[1], shape[2:]
+    right = int(np.prod(tail))
+    if right < 1:
+        raise ValueError("Right block dimension must be >= 1 in mps_local_orthonormalize_qr")
+    Q, R = dense_tensor_qr(block.reshape([left * phys, right]), ctx)
+    k = Q.shape[1]
+    return MPSSite(Q.reshape([left, phys, k])), R.reshape([k] + tail)
+
+
+def mps_orthogonalize_qr(ctx, full_state: DenseTensor) -> MatrixProductState:
+    """Dense state [d, d, ..., d] -> left-canonical MPS by successive QR; the last site is
+    normalised (mps_state.mojo:382-451)."""
+    ctx = ctx or get_context()
+    dims = list(full_state.shape)
+    if len(dims) == 0:
+        raise ValueError("full_state must have rank >= 1 to build an MPS")
+    d = dims[0]
+    for idx, x in enumerate(dims):
+        if x != d:
+            raise ValueError(f"All physical dimensions must match the first axis ({d}), but axis {idx} has size {x}")
+    remainder = full_state.reshape([1] + dims)
+    sites = []
+    for _ in range(len(dims) - 1):
+        site, remainder = mps_local_orthonormalize_qr(ctx, remainder)
+        sites.append(site)
+    if len(remainder.shape) != 2:
+        raise ValueError(f"Unexpected remainder rank {len(remainder.shape)} while constructing final MPS site")
+    final = remainder.reshape([remainder.shape[0], remainder.shape[1], 1])
+    nrm = final.norm(ctx)
+    if nrm > 0:
+        final.scale_in_place(1.0 / nrm, ctx)
+    sites.append(MPSSite(final))
+    return MatrixProductState(sites)

@@ -128,6 +128,14 @@ CT_API int ct_lanczos2(ct_handle* h, int prec, const double* theta_in, double* t
  * capacity k = min(m,n) for chi), chi chosen by the reference rule.         */
 CT_API int ct_svd_trunc(ct_handle* h, const double* M, int64_t m, int64_t n, int64_t chi_max,
                  double eps_trunc, double* U, double* S, double* Vt, int64_t* chi_host);
+/* Thin QR of a row-major A[m,n] on the device, FP64 (dense_tensor_qr,
+ * dense_tensor.mojo:1333-1433): Q[m,k] with orthonormal columns, R[k,n] upper
+ * triangular (trapezoidal for n > m), k = min(m,n), diag(R) >= 0.  LAPACK's
+ * Householder factors equal these up to the signs of Q's columns and R's rows
+ * (the reference's own tests check the properties only).  Columns dependent on
+ * the ones before them get completed Q columns; *completed_host (may be NULL)
+ * returns how many.                                                          */
+CT_API int ct_qr(ct_handle* h, const double* A, int64_t m, int64_t n, double* Q, double* R, int* completed_host);
 /* Two-site split (split_two_site_theta_svd, dmrg.mojo:143-252).
  * A_out[Dl,d,chi], B_out[chi,d,Dr] (capacity min(Dl*d, d*Dr) for chi),
  * S_out (may be NULL) gets the kept singular values, descending.
