@@ -52,7 +52,8 @@ class ct_dmrg_stats(C.Structure):
                 ("heff_applies", C.c_int64), ("local_updates", C.c_int64), ("max_discarded", C.c_double),
                 ("energy_rayleigh", C.c_double), ("subspace_splits", C.c_int64), ("exact_splits", C.c_int64),
                 ("seconds_subspace", C.c_double), ("cold_splits", C.c_int64),
-                ("completed_rows", C.c_int64), ("seconds_rayleigh", C.c_double)]
+                ("completed_rows", C.c_int64), ("seconds_rayleigh", C.c_double),
+                ("stale_retries", C.c_int64)]
 
 
 P = C.c_void_p

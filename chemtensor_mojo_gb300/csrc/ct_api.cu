@@ -604,7 +604,7 @@ int ct_svd_split_warm(ct_handle* h, const double* theta, int64_t Dl, int64_t d, 
     bool ok = false;
     if (power_steps < 0) return CT_ERR_INVALID;
     CT_TRY(ct_split_subspace(h, ar, theta, m, n, chi, left_to_right ? 0 : 1, basis_in, basis_out, A_out, B_out,
-                             h->d_scalars + SC_THETA_NSQ, 0.0, -1.0, power_steps, false, 0, &o, &ok));
+                             h->d_scalars + SC_THETA_NSQ, 0.0, -1.0, 0.0, 0.0, power_steps, false, 0, &o, &ok));
     CT_TRY(check_status(h));
     *accepted = ok ? 1 : 0;
     if (discarded_host)

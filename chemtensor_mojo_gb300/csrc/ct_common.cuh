@@ -90,10 +90,11 @@ enum {
     SC_MISC = 768,         // scratch (<= 128): Thomas coefficients, reorthogonalisation
     SC_SVD_FROB2 = 968,    // mixed SVD: |M|_F^2
     SC_SPLIT_PIV = 970,    // subspace split: smallest Cholesky pivot of each pass (2)
-    SC_ORTH_EMAX = 972     // subspace split: largest |Q Q^T - I| seen by the second pass
+    SC_ORTH_EMAX = 972,    // subspace split: largest |Q Q^T - I| seen by the second pass
+    SC_SVD_MINKEPT = 973   // Jacobi split: smallest kept singular value
 };
 static_assert(SC_MISC + CT_MAX_KRYLOV_SLOTS <= SC_SVD_FROB2 && SC_SPLIT_PIV + 2 <= SC_ORTH_EMAX &&
-                  SC_ORTH_EMAX + 1 <= CT_NSCALARS,
+                  SC_ORTH_EMAX < SC_SVD_MINKEPT && SC_SVD_MINKEPT + 1 <= CT_NSCALARS,
               "scalar slots overlap or overflow d_scalars");
 // int slots inside d_flags
 enum { FL_STOP = 0, FL_NUMITER = 1, FL_ROT = 2, FL_CHI = 3, FL_TMP = 4, FL_CNT = 8 };
@@ -260,6 +261,7 @@ struct SvdOut {
     double min_pivot2 = 0.0;  // of the second pass,
     int chol_fail = 0;        // and whether a pivot was not positive
     int replaced = 0;         // rows replaced by the rank completion of a first visit
+    int stale = 0;            // refused: more weight lost than the staleness bound allows
 };
 // tensor-core path (ct_tc.cu)
 struct TcGemm;

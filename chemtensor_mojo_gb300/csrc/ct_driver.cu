@@ -189,6 +189,11 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         need = std::max(need, l2r ? ct_env_ws_bytes(prec, Dl, d, chi_ub, wL, wM)
                                   : ct_env_ws_bytes(prec, chi_ub, d, Dr, wM, wR));
         CT_TRY(ct_reserve(h, need));
+        // The mixed form always reorthogonalises its Krylov basis: with TF32-level
+        // H_eff rounding the plain recursion of the reference loses orthogonality on
+        // some bonds and returns a poorer Ritz vector (measured on the XXZ chain at
+        // chi = 256: single sweeps 1e-8 to 3.5e-5 above the FP64 form without it, all
+        // within 5.7e-10 with it).  The FP64 form keeps the reference's plain Lanczos.
         // theta (dmrg.mojo:93-140)
         CT_CUDA(h, cudaEventRecord(ev_l.a, h->stream));
         CT_TRY(ct_theta_run(h, prec, mps_sites[i], mps_sites[i + 1], th.p, Dl, d, Dm, Dr));
@@ -197,7 +202,7 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
             LanczosResult lr;
             CT_TRY(ct_lanczos_run(h, ar, prec, th.p, th_opt.p, Lenv[i].p, Renv[i + 2].p, mpo_sites[i],
                                   mpo_sites[i + 1], Dl, d, Dr, wL, wM, wR, P->max_krylov_iter, P->krylov_tol,
-                                  P->max_rotations, P->reorth, &lr));
+                                  P->max_rotations, (P->reorth || prec == CT_PREC_TF32X3) ? 1 : 0, &lr));
         }
         CT_CUDA(h, cudaEventRecord(ev_l.b, h->stream));
         // split (dmrg.mojo:143-252): |theta|^2 then SVD
@@ -241,10 +246,24 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
                 }
                 own.len = own.c = -1;
                 if (use_subspace && src.p && src.len == src_len && src.c == c) {
+                    // accepted when it loses at most 1.5x the weight of the bond's previous
+                    // truncating visit (+1e-12); otherwise one retry with a power step more,
+                    // accepted within 4x + 1e-8, before the Jacobi SVD
                     bool ok = false;
                     CT_TRY(ct_split_subspace(h, ar, th_opt.p, m, n, c, l2r ? 0 : 1, src.p, own.p,
                                              mps_sites[i], mps_sites[i + 1], h->d_scalars + SC_THETA_NSQ,
-                                             P->eps_trunc, src.disc, P->split_power_steps, false, 0, &so, &ok));
+                                             P->eps_trunc, src.disc, 1.5, 1e-12, P->split_power_steps, false, 0,
+                                             &so, &ok));
+                    if (!ok && so.stale) {
+                        if (P->verbose >= 2)
+                            fprintf(stderr, "bond %d %s: subspace split stale (kept %.12g of %.12g), retrying\n", i,
+                                    l2r ? "L->R" : "R->L", so.sum_s2_kept, so.sum_s2_all);
+                        CT_TRY(ct_split_subspace(h, ar, th_opt.p, m, n, c, l2r ? 0 : 1, src.p, own.p,
+                                                 mps_sites[i], mps_sites[i + 1], h->d_scalars + SC_THETA_NSQ,
+                                                 P->eps_trunc, src.disc, 4.0, 1e-8, P->split_power_steps + 1, false,
+                                                 0, &so, &ok));
+                        st.stale_retries++;
+                    }
                     done_split = ok;
                     last_split_subspace = ok;
                     if (P->verbose >= 2)
@@ -271,8 +290,8 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
                     CT_TRY(ct_cold_basis(h, reuse ? src.p : nullptr, reuse ? src.c : 0, c, src_len, seed, X));
                     bool ok = false;
                     CT_TRY(ct_split_subspace(h, ar, th_opt.p, m, n, c, l2r ? 0 : 1, X, own.p, mps_sites[i],
-                                             mps_sites[i + 1], h->d_scalars + SC_THETA_NSQ, P->eps_trunc, -1.0,
-                                             P->cold_power_steps, true, seed, &so, &ok));
+                                             mps_sites[i + 1], h->d_scalars + SC_THETA_NSQ, P->eps_trunc, -1.0, 0.0,
+                                             0.0, P->cold_power_steps, true, seed, &so, &ok));
                     ar.off = mark;
                     done_split = ok;
                     last_split_subspace = ok;
@@ -326,7 +345,7 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
                     bool ok = false;
                     CT_TRY(ct_split_subspace(h, ar3, th_opt.p, m, n, c0, l2r ? 0 : 1, basis, bc->p,
                                              mps_sites[i], mps_sites[i + 1], h->d_scalars + SC_THETA_NSQ, 0.0,
-                                             -1.0, 0, false, 0, &s1, &ok));
+                                             -1.0, 0.0, 0.0, 0, false, 0, &s1, &ok));
                     if (ok) {
                         so = s0;
                         done_split = true;

@@ -89,8 +89,9 @@ size_t ct_qr_ws_bytes(int64_t m, int64_t n);
 int ct_qr_run(ct_handle* h, Arena& ar, const double* A, int64_t m, int64_t n, double* Q, double* R, int* completed);
 int ct_split_subspace(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t c, int mode,
                       const double* basis_in, double* basis_out, double* Aout, double* Bout,
-                      const double* d_total, double eps_trunc, double disc_ref, int power_steps, bool complete,
-                      uint64_t seed, SvdOut* out, bool* accepted);
+                      const double* d_total, double eps_trunc, double disc_ref, double stale_mult,
+                      double stale_abs, int power_steps, bool complete, uint64_t seed, SvdOut* out,
+                      bool* accepted);
 // first-visit start basis: kept rows (may be null) then random Gaussian rows
 int ct_cold_basis(ct_handle* h, const double* prev, int64_t c_prev, int64_t c, int64_t len, uint64_t seed,
                   double* X);

@@ -52,11 +52,11 @@
 // MIN_PIVOT of the row's weight; the discarded weight is still measured from
 // the residual.
 //
-// The split is refused (the caller falls back to the Jacobi SVD) when the
-// Cholesky factorisation breaks down, when the discarded weight exceeds
-// 4x that of the previous visit of the bond plus 1e-8 (the cached basis no
-// longer tracks the dominant subspace), or when it is <= eps_trunc (then the
-// rule may keep fewer states and needs the spectrum).
+// The split is refused (the caller retries or falls back to the Jacobi SVD)
+// when the Cholesky factorisation breaks down, when the discarded weight
+// exceeds stale_mult x that of the previous visit of the bond plus stale_abs
+// (the cached basis no longer tracks the dominant subspace), or when it is
+// <= eps_trunc (then the rule may keep fewer states and needs the spectrum).
 #include "ct_ops.cuh"
 
 namespace {
@@ -457,8 +457,8 @@ struct SplitBufs {
 // The warm split (products with theta on the tensor cores, orthonormalisation in FP64).
 int split_attempt(ct_handle* h, Arena& ar, const SplitBufs& sb, const double* M, int64_t m, int64_t n, int64_t c,
                   int mode, const double* basis_in, double* basis_out, double* Aout, double* Bout,
-                  const double* d_total, double eps_trunc, double disc_ref, int power_steps, bool complete,
-                  uint64_t seed, SvdOut* out, SplitVerdict* verdict) {
+                  const double* d_total, double eps_trunc, double disc_ref, double stale_mult, double stale_abs,
+                  int power_steps, bool complete, uint64_t seed, SvdOut* out, SplitVerdict* verdict) {
     const size_t mark = ar.off;
     unsigned long long* d_piv = (unsigned long long*)(h->d_scalars + SC_SPLIT_PIV);   // [0] pass 1, [1] pass 2
     int* d_fail = h->d_flags + FL_CHOL_FAIL;
@@ -542,8 +542,9 @@ int split_attempt(ct_handle* h, Arena& ar, const SplitBufs& sb, const double* M,
     // rows are random and keep (len - c) / len of their weight outside the rest
     if (fail || !(piv1 >= MIN_PIVOT) || !(piv2 > (replaced ? 1e-3 : 0.5))) {
         *verdict = SPLIT_BREAKDOWN;
-    } else if (disc_ref >= 0.0 && disc > 4.0 * disc_ref + 1e-8) {
-        *verdict = SPLIT_STALE;   // much more weight lost than at the previous visit of the bond
+    } else if (disc_ref >= 0.0 && disc > stale_mult * disc_ref + stale_abs) {
+        *verdict = SPLIT_STALE;   // more weight lost than at the previous visit of the bond allows
+        out->stale = 1;
     } else if (eps_trunc > 0.0 && disc <= eps_trunc) {
         *verdict = SPLIT_EPS;     // eps binds: the rule may keep fewer states
     } else {
@@ -556,8 +557,9 @@ int split_attempt(ct_handle* h, Arena& ar, const SplitBufs& sb, const double* M,
 
 int ct_split_subspace(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_t n, int64_t c, int mode,
                       const double* basis_in, double* basis_out, double* Aout, double* Bout,
-                      const double* d_total, double eps_trunc, double disc_ref, int power_steps, bool complete,
-                      uint64_t seed, SvdOut* out, bool* accepted) {
+                      const double* d_total, double eps_trunc, double disc_ref, double stale_mult,
+                      double stale_abs, int power_steps, bool complete, uint64_t seed, SvdOut* out,
+                      bool* accepted) {
     *accepted = false;
     const int64_t big = m > n ? m : n;
     SplitBufs sb{};
@@ -571,8 +573,9 @@ int ct_split_subspace(ct_handle* h, Arena& ar, const double* M, int64_t m, int64
     sb.ob.defrows = ar.take<int>(sb.ob.cp);
     if (!sb.Z || !sb.W || !sb.ob.G || !sb.ob.Linv || !sb.ob.S || !sb.R || !sb.ob.defrows) return CT_ERR_OOM;
     SplitVerdict v = SPLIT_BREAKDOWN;
+    out->stale = 0;
     CT_TRY(split_attempt(h, ar, sb, M, m, n, c, mode, basis_in, basis_out, Aout, Bout, d_total, eps_trunc,
-                         disc_ref, power_steps, complete, seed, out, &v));
+                         disc_ref, stale_mult, stale_abs, power_steps, complete, seed, out, &v));
     *accepted = (v == SPLIT_OK);
     return CT_OK;
 }

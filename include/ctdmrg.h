@@ -158,7 +158,7 @@ typedef struct ct_dmrg_params {
     int verbose;
     int prec;            /* ct_prec                                            */
     int max_rotations;   /* 200 = reference Jacobi cap; 0 = converged          */
-    int reorth;          /* full FP64 reorthogonalisation                      */
+    int reorth;          /* full FP64 reorthogonalisation (always on in the mixed form) */
     int final_rayleigh;  /* also return <psi|H|psi>/<psi|psi> of the final MPS,
                             contracted in FP64 (stats.energy_rayleigh)          */
     int keep_bases;      /* mixed form: the first half-sweep's large splits may
@@ -196,6 +196,7 @@ typedef struct ct_dmrg_stats {
     int64_t cold_splits;       /* subspace splits started from random rows       */
     int64_t completed_rows;    /* rows a first visit's rank completion replaced  */
     double seconds_rayleigh;   /* the final FP64 <H> (final_rayleigh), included in seconds_total */
+    int64_t stale_retries;     /* warm splits retried with one more power step   */
 } ct_dmrg_stats;
 
 /* Runs the sweeps in place.  mps_sites[i] are caller-owned device buffers of
