@@ -198,18 +198,41 @@ __global__ void lanczos_next_kernel(int64_t n, const double* w, double* vnext, c
         vnext[i] = w[i] * inv;
 }
 
-// reorthogonalisation: coeff[v] = <V[v], w>  (partials laid out [block][nvec])
+// reorthogonalisation: coeff[v] = <V[v], w>  (partials laid out [block][nvec]).  MD_VB
+// vectors per pass over w: w is read nvec / MD_VB times instead of nvec times, and
+// the MD_VB block sums share one reduction.
+constexpr int MD_VB = 8;
 __global__ void __launch_bounds__(RT) multidot_kernel(int64_t n, const double* w, const double* V, int64_t ldv,
                                                       int nvec, double* partials, const int* skip) {
     if (ct_skip(skip)) return;
-    __shared__ double sm[32];
+    __shared__ double sm[MD_VB][RT / 32];
     const int64_t stride = (int64_t)gridDim.x * RT;
-    for (int v = 0; v < nvec; ++v) {
-        double acc = 0.0;
-        const double* x = V + (int64_t)v * ldv;
-        for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) acc = fma(x[i], w[i], acc);
-        acc = ct_block_sum<RT>(acc, sm);
-        if (threadIdx.x == 0) partials[(int64_t)blockIdx.x * nvec + v] = acc;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int v0 = 0; v0 < nvec; v0 += MD_VB) {
+        const int nv = min(MD_VB, nvec - v0);
+        double acc[MD_VB];
+#pragma unroll
+        for (int k = 0; k < MD_VB; ++k) acc[k] = 0.0;
+        const double* x = V + (int64_t)v0 * ldv;
+        for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) {
+            const double wi = w[i];
+#pragma unroll
+            for (int k = 0; k < MD_VB; ++k)
+                if (k < nv) acc[k] = fma(x[(int64_t)k * ldv + i], wi, acc[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < MD_VB; ++k) acc[k] = ct_warp_sum(acc[k]);
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < MD_VB; ++k) sm[k][wid] = acc[k];
+        }
+        __syncthreads();
+        if (threadIdx.x < nv) {
+            double r = 0.0;
+            for (int q = 0; q < RT / 32; ++q) r += sm[threadIdx.x][q];
+            partials[(int64_t)blockIdx.x * nvec + v0 + threadIdx.x] = r;
+        }
+        __syncthreads();
     }
 }
 __global__ void __launch_bounds__(RT) multidot_finish(const double* partials, int np, int nvec, double* coeff,
