@@ -46,7 +46,7 @@ enum ct_status {
     CT_ERR_NOCONV = -4,      /* an iterative device solver hit its iteration cap */
     CT_ERR_ZERO_NORM = -5,   /* Lanczos start vector has zero norm               */
     CT_ERR_SHAPE = -6,       /* inconsistent shapes                              */
-    CT_ERR_UNSUPPORTED = -7, /* shape/precision not supported by this build      */
+    CT_ERR_UNSUPPORTED = -7, /* shape/precision not supported by this library    */
     CT_ERR_NONFINITE = -8,   /* NaN/Inf met in a reduction                       */
     CT_ERR_EMPTY = -9,       /* truncation kept zero singular values             */
     CT_ERR_TOO_LARGE = -10   /* problem exceeds the static scratch of a no-alloc entry */
@@ -266,12 +266,16 @@ CT_API int ct_random_mps_host(int nsites, int d, int chi_max, uint64_t seed, int
 /* first n values of randnf() for a seed (used by tests)                    */
 CT_API int ct_rng_randnf_host(uint64_t seed, int64_t n, float* out);
 
-/* ---- adjoint (no reference counterpart; spec item) ------------------
+/* ---- adjoint energy gradient (no reference counterpart) -------------------
  * Gradient of E(A) = <psi|H|psi>/<psi|psi> with respect to every site tensor
  * of a (not necessarily canonical) MPS, by the hand-written adjoint of the
  * environment chain.  grad_sites[i] are caller-owned device buffers shaped
  * like mps_sites[i].  checkpoint_every > 0 stores only every k-th left
- * environment and recomputes the others (memory ~ L/k environments).      */
+ * environment and recomputes the others (memory ~ L/k environments).
+ * prec CT_PREC_FP64: FP64 throughout.  CT_PREC_TF32X3: environments and
+ * one-site effective Hamiltonians on the tensor cores (FP32-level products).
+ * Every environment is rescaled by a power of two after each step, so
+ * unnormalised chains neither under- nor overflow.                        */
 CT_API int ct_energy_grad(ct_handle* h, int prec, int nsites, int d, const int64_t* mpo_dims,
                    const double* const* mpo_sites, const int64_t* bond_dims,
                    const double* const* mps_sites, double* const* grad_sites,

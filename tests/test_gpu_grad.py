@@ -3,7 +3,7 @@ central finite differences and against 2 (H_eff theta - E theta) / <psi|psi>.
 
 Tolerance: the adjoint is exact up to FP64 rounding, finite differences with
 step 1e-6 carry O(h^2) truncation and O(eps/h) rounding, so the comparison is
-held to 1e-6 relative (the benchmark spec's bound).
+held to 1e-6 relative.
 """
 import numpy as np
 import pytest
