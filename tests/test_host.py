@@ -96,3 +96,42 @@ def test_bond_capacities():
     assert bond_capacities([1] * 9, 2, 5) == [1, 2, 4, 5, 5, 5, 4, 2, 1]
     dims = orng.bond_dims_c_style(12, 2, 32)
     assert bond_capacities(dims, 2, 32) == dims
+
+
+def _c_struct_fields(name):
+    """(type, field) pairs of a typedef'd struct in ctdmrg.h, in declaration order."""
+    text = (ROOT / "include" / "ctdmrg.h").read_text()
+    m = re.search(r"typedef\s+struct\s*(?:\w+\s*)?\{([^{}]*)\}\s*" + name + r"\s*;", text)
+    assert m, name
+    body = re.sub(r"/\*.*?\*/", "", m.group(1), flags=re.S)
+    return [(t, f) for t, f in re.findall(r"(int64_t|int|double)\s+(\w+)\s*;", body)]
+
+
+@pytest.mark.parametrize("cname,pyname", [("ct_dmrg_params", "ct_dmrg_params"), ("ct_dmrg_stats", "ct_dmrg_stats")])
+def test_ctypes_structs_match_header(cname, pyname):
+    """The ctypes mirrors of the parameter and statistics structs have the header's fields, in
+    order and with the same C types (an ABI drift here would corrupt every sweep call)."""
+    from chemtensor_mojo_gb300 import _lib
+    ctype = {"int": C.c_int, "int64_t": C.c_int64, "double": C.c_double}
+    cfields = _c_struct_fields(cname)
+    pyfields = getattr(_lib, pyname)._fields_
+    assert [f for _, f in cfields] == [f for f, _ in pyfields]
+    for (t, f), (pf, pt) in zip(cfields, pyfields):
+        assert C.sizeof(ctype[t]) == C.sizeof(pt) and ctype[t]._type_ == pt._type_, f
+
+
+def test_python_stats_mirror_the_c_struct():
+    """Every field of ct_dmrg_stats reaches DMRGStats."""
+    from chemtensor_mojo_gb300 import _lib
+    from chemtensor_mojo_gb300.dmrg import DMRGStats
+    names = {f for f, _ in _lib.ct_dmrg_stats._fields_}
+    assert names <= set(DMRGStats().__dict__)
+
+
+def test_flop_counts_match_oracle():
+    import bench
+    from oracle import dmrg as od
+    for chi_l, chi_r in ((1024, 1024), (512, 1024), (64, 16)):
+        assert bench.heff_flops(chi_l, chi_r) == pytest.approx(od.heff_flops(chi_l, chi_r, 5, 2))
+    # the centre-bond apply of the benchmark: 86.7 GFLOP
+    assert bench.heff_flops(1024, 1024) == pytest.approx(86.7e9, rel=2e-3)
