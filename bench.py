@@ -43,7 +43,14 @@ import sys
 import threading
 import time
 
-import numpy as np
+# The reference arm times the CPU oracle with every host core.  A launcher that pins BLAS to
+# one thread per rank (torchrun sets OMP_NUM_THREADS=1) is overridden here, before NumPy
+# loads its BLAS; only rank 0 of that arm does any work.
+if "--impl" in sys.argv and "reference" in sys.argv:
+    for _var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[_var] = str(os.cpu_count() or 1)
+
+import numpy as np  # noqa: E402
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
@@ -467,6 +474,15 @@ def cpu_local_update_seconds(chi, seed=0):
     return time.perf_counter() - t0
 
 
+def cpu_threads() -> int:
+    """Threads the oracle's BLAS runs with: the pinned count when one is set, else every core."""
+    for var in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
+        v = os.environ.get(var)
+        if v and v.isdigit() and int(v) > 0:
+            return int(v)
+    return os.cpu_count() or 1
+
+
 def reference_arm(args, rank):
     """CPU oracle port of the reference path: sampled centre-bond updates, extrapolated."""
     if rank != 0:
@@ -483,7 +499,7 @@ def reference_arm(args, rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"heisenberg_xxz L={args.L} d=2 D=5 chi={chi} lanczos={LANCZOS}",
                    "model": "spin-1/2 XXZ Delta=1 (reference XXZ MPO, J=-1/4)", "parallelism": "replicas"},
-        "cpu_baseline": {"value": per_sweep, "unit": "s/sweep", "cores": os.cpu_count(), "kind": "port",
+        "cpu_baseline": {"value": per_sweep, "unit": "s/sweep", "cores": cpu_threads(), "kind": "port",
                          "sample": f"{args.steps} centre-bond local updates at chi={chi}, FLOP-weighted x{weight:.1f}"
                                    " to a sweep (extrapolated)"},
         "e2e": {"value": per_sweep, "unit": "s/sweep", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -720,7 +736,7 @@ def main():
                     "GEMMs of H_eff, environments and splits",
         }
     if "cpu_sweep_s" in extras:
-        line["cpu_baseline"] = {"value": extras["cpu_sweep_s"], "unit": "s/sweep", "cores": os.cpu_count(),
+        line["cpu_baseline"] = {"value": extras["cpu_sweep_s"], "unit": "s/sweep", "cores": cpu_threads(),
                                 "kind": "port", "sample": extras["cpu_sample"]}
     print(json.dumps(line), flush=True)
 
