@@ -45,6 +45,12 @@ struct ct_handle {
     // FP64 GEMM split-K partial sums (grown on demand, freed by ct_destroy)
     double* splitk = nullptr;
     size_t splitk_cap = 0;   // doubles
+    // allocation-free mode (the stack handle of ct_heff2_apply_noalloc): the
+    // launchers never call cudaMalloc; split-K partials come from the fixed
+    // region below, and K is split only as far as that region holds
+    bool no_alloc = false;
+    double* splitk_fixed = nullptr;
+    size_t splitk_fixed_cap = 0;   // doubles
     // stream-K scratch of the persistent tensor-core GEMM (lazily sized, freed by ct_destroy)
     float* tc_sk_part = nullptr;
     int* tc_sk_flag = nullptr;

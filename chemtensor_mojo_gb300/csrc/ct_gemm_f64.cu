@@ -177,7 +177,15 @@ int ct_gemm_f64_launch(ct_handle* h, const GemmDesc& g) {
     if (nb == 1 && tiles < sms && g.K >= 64) {
         int64_t ks = ct_cdiv(sms, tiles);
         if (ks > g.K / 32) ks = g.K / 32;
-        if (ks > 1) {
+        if (h->no_alloc) {
+            // partials only in the caller's fixed region, as many K pieces as it holds
+            const int64_t fit = (int64_t)(h->splitk_fixed_cap / (size_t)(g.M * g.N));
+            if (ks > fit) ks = fit;
+            if (ks > 1) {
+                gg.ksplit = ks;
+                gg.part = h->splitk_fixed;
+            }
+        } else if (ks > 1) {
             const size_t need = (size_t)(ks * g.M * g.N);
             if (h->splitk_cap < need) {
                 if (h->splitk) cudaFree(h->splitk);

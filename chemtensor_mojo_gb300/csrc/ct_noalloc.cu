@@ -13,7 +13,11 @@
 // symbol itself as a device pointer).  Make that first call before any stream
 // capture.  All calls share the one array, so calls whose kernels overlap on
 // the GPU race on it.  Every element a call reads is written earlier in the
-// same call, so no part of the array needs clearing between calls.
+// same call (the split-K partial sums included: each K piece writes its whole
+// M x N slice before the reduction reads it), so no part of the array needs
+// clearing between calls.  No allocation happens anywhere on this path: the
+// handle below is flagged no-alloc, so the FP64 GEMM launcher takes its split-K
+// scratch from the array instead of growing a handle-owned buffer.
 #include <mutex>
 
 #include "ct_ops.cuh"
@@ -59,10 +63,16 @@ extern "C" int ct_heff2_apply_noalloc(void* stream, const double* theta, const d
         }
         base = g_scratch_ptr[dev];
     }
-    // a handle on the stack: it carries the stream and the SM count, owns nothing
+    // a handle on the stack: it carries the stream and the SM count, owns nothing,
+    // and its no-alloc mode keeps the GEMM launcher away from cudaMalloc: the FP64
+    // GEMM's split-K partial sums go to the part of the array past W12, and K is
+    // split only as far as that part holds (not at all when it is too small)
     ct_handle h;
     h.device = dev;
     h.stream = static_cast<cudaStream_t>(stream);
+    h.no_alloc = true;
+    h.splitk_fixed = base + n_t1 + n_t3 + n_w12;
+    h.splitk_fixed_cap = (size_t)((int64_t)CT_NOALLOC_SCRATCH_DOUBLES - (n_t1 + n_t3 + n_w12));
     if (cudaDeviceGetAttribute(&h.num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
         (void)cudaGetLastError();
         return CT_ERR_CUDA;

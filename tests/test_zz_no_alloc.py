@@ -5,8 +5,11 @@ example a Mojo/MAX host whose allocator owns every buffer): its scratch is a
 static device array.  Two calls in a row, with different shapes, must agree
 with the allocating entry point ct_heff2_apply on the same inputs to the
 FP64 tolerance of the other contraction tests (1e-12 relative); oversized
-problems are refused with CT_ERR_TOO_LARGE.  This file sorts last so that a
-failure here stops a -x run only after every other test has run.
+problems are refused with CT_ERR_TOO_LARGE.  The first shape is one whose
+last GEMM splits K over the SMs, the step that used to grow a handle-owned
+buffer: fifty calls on it must leave the device's free memory where it was.
+This file sorts last so that a failure here stops a -x run only after every
+other test has run.
 """
 import ctypes as C
 
@@ -57,6 +60,20 @@ def test_noalloc_heff_matches_allocating_entry_point():
             r, o = ref.cpu().numpy(), out.cpu().numpy()
             assert np.all(np.isfinite(o))
             assert np.linalg.norm(o - r) <= 1e-12 * np.linalg.norm(r)
+        # no allocation: (24,2,40,5,5,5) makes the last GEMM M=96, N=40, K=200, six
+        # 32x32 tiles, so K is split six ways; its partial sums must come from the
+        # static array.  A cudaMalloc per call would lower the free memory.
+        dims = (24, 2, 40, 5, 5, 5)
+        th, L, R, W1, W2 = _inputs(1, *dims)
+        out = torch.empty(24 * 4 * 40, dtype=torch.float64, device="cuda")
+        args = [_ptr(t) for t in (th, L, R, W1, W2, out)] + [C.c_int64(x) for x in dims]
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info()
+        for _ in range(50):
+            _lib.check(lib.ct_heff2_apply_noalloc(stream, *args), "ct_heff2_apply_noalloc")
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        assert free1 >= free0 - (1 << 20), f"device free memory fell by {free0 - free1} bytes over 50 calls"
         # a size past the limit: refused before any work
         big = (256, 2, 256, 5, 5, 5)
         th, L, R, W1, W2 = _inputs(3, *big)
