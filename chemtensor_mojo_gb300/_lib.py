@@ -72,6 +72,7 @@ SIGNATURES = {
     "ct_version": [],
     "ct_workspace_bytes": [P, C.POINTER(I64)],
     "ct_set_workspace_limit": [P, I64],
+    "ct_set_svd_max_sweeps": [P, I32],
     "ct_svd_sweeps": [P, C.POINTER(I32), C.POINTER(I64)],
     "ct_gemm": [P, I32, I32, I32, I64, I64, I64, D, P, I64, P, I64, D, P, I64],
     "ct_permute": [P, P, P, I32, C.POINTER(I64), C.POINTER(C.c_int32)],

@@ -226,6 +226,13 @@ int ct_set_workspace_limit(ct_handle* h, int64_t bytes) {
     return CT_OK;
 }
 
+int ct_set_svd_max_sweeps(ct_handle* h, int max_sweeps) {
+    CT_NULLCHK(h, h);
+    if (max_sweeps < 0) return CT_ERR_INVALID;
+    h->svd_max_sweeps = max_sweeps;
+    return CT_OK;
+}
+
 // ---------------------------------------------------------------------------
 // dense tensor core
 // ---------------------------------------------------------------------------
@@ -522,6 +529,9 @@ int ct_svd_trunc(ct_handle* h, const double* M, int64_t m, int64_t n, int64_t ch
     CT_NULLCHK(h, Vt);
     CT_TRY(ct_reserve(h, ct_svd_ws_bytes(m, n, 2)));
     Arena ar(h);
+    // a NaN or infinite entry is an error (LAPACK's dgesdd fails on it, svd.mojo:74-76)
+    CT_TRY(ct_reduce_nrm2sq(h, m * n, M, h->d_scalars + SC_DOT, nullptr));
+    CT_TRY(ct_check_finite(h, h->d_scalars + SC_DOT, nullptr));
     SvdOut o;
     CT_TRY(ct_svd_run(h, ar, M, m, n, chi_max, eps_trunc, 2, U, Vt, S, &o));
     CT_TRY(check_status(h));
@@ -569,6 +579,7 @@ int ct_svd_split(ct_handle* h, int prec, const double* theta, int64_t Dl, int64_
     Arena ar(h);
     // |theta|^2 in FP64 on the device (dmrg.mojo:176)
     CT_TRY(ct_reduce_nrm2sq(h, m * n, theta, h->d_scalars + SC_THETA_NSQ, nullptr));
+    CT_TRY(ct_check_finite(h, h->d_scalars + SC_THETA_NSQ, nullptr));
     double tn = 0.0;
     CT_CUDA(h, cudaMemcpyAsync(&tn, h->d_scalars + SC_THETA_NSQ, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     SvdOut o;
@@ -600,6 +611,7 @@ int ct_svd_split_warm(ct_handle* h, const double* theta, int64_t Dl, int64_t d, 
     CT_TRY(ct_reserve(h, ct_split_subspace_ws_bytes(m, n, chi)));
     Arena ar(h);
     CT_TRY(ct_reduce_nrm2sq(h, m * n, theta, h->d_scalars + SC_THETA_NSQ, nullptr));
+    CT_TRY(ct_check_finite(h, h->d_scalars + SC_THETA_NSQ, nullptr));
     SvdOut o;
     bool ok = false;
     if (power_steps < 0) return CT_ERR_INVALID;

@@ -39,6 +39,9 @@ struct ct_handle {
         double disc = -1.0;   // discarded weight of the split that wrote it
     };
     std::vector<BasisCache> basis_cache;
+    // cap on the one-sided Jacobi sweeps of every SVD on this handle (0 = the
+    // kernels' own caps); a split that needs more ends with CT_ERR_NOCONV
+    int svd_max_sweeps = 0;
     // diagnostics: Jacobi sweeps of the last SVD split, and the running total
     int last_svd_sweeps = 0;
     int64_t total_svd_sweeps = 0;
@@ -185,6 +188,12 @@ __device__ __forceinline__ double ct_block_sum(double v, double* sm) {
     return r;
 }
 
+// Sort key of a singular value for the descending rank kernels: NaN sorts last.
+// Ranking compares keys with '>' and '==' (ties by index), which is a strict total
+// order only without NaN; with it every comparison is false, several entries get
+// the same rank and parts of the permutation are never written.
+__device__ __forceinline__ double ct_rank_key(double s) { return isnan(s) ? -INFINITY : s; }
+
 __device__ __forceinline__ void ct_set_status(int* st, int code) {
     if (st) atomicCAS(st, 0, code);
 }
@@ -240,6 +249,9 @@ int ct_reduce_nrm2sq(ct_handle* h, int64_t n, const double* x, double* d_out, co
 int ct_scale_by_inv_sqrt(ct_handle* h, int64_t n, const double* x, double* y,
                          const double* d_nsq, const int* skip, int zero_code);
 int ct_fill(ct_handle* h, double* x, int64_t n, double v);
+// sets the status word to CT_ERR_NONFINITE when the device scalar *d_x is NaN or
+// infinite (enqueued, no synchronisation; the caller's next status check sees it)
+int ct_check_finite(ct_handle* h, const double* d_x, const int* skip);
 int ct_copy(ct_handle* h, double* dst, const double* src, int64_t n);
 int ct_permute_launch(ct_handle* h, const double* in, double* out, int rank, const int64_t* shape,
                       const int32_t* perm);

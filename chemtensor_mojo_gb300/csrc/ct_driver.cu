@@ -207,6 +207,7 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         CT_CUDA(h, cudaEventRecord(ev_l.b, h->stream));
         // split (dmrg.mojo:143-252): |theta|^2 then SVD
         CT_TRY(ct_reduce_nrm2sq(h, m * n, th_opt.p, h->d_scalars + SC_THETA_NSQ, nullptr));
+        CT_TRY(ct_check_finite(h, h->d_scalars + SC_THETA_NSQ, nullptr));
         struct {
             double e;
             double tn;
@@ -374,6 +375,15 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
         CT_CUDA(h, cudaEventRecord(ev_s.b, h->stream));
         const int64_t chi = so.chi;
         if (chi <= 0) {
+            // a device error (a non-finite theta, say) takes precedence over the empty truncation
+            int dst0 = 0;
+            CT_CUDA(h, cudaStreamSynchronize(h->stream));
+            CT_CUDA(h, cudaMemcpy(&dst0, h->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+            if (dst0 != 0) {
+                cudaMemset(h->d_status, 0, sizeof(int));
+                ct_seterr(h, "bond %d: device status %d", i, dst0);
+                return dst0;
+            }
             ct_seterr(h, "bond %d: truncation kept no singular values", i);
             return CT_ERR_EMPTY;
         }

@@ -77,7 +77,8 @@ __device__ __forceinline__ double block_sum(double v, double* sm) {
 // T = float (mixed form: FP32 data, FP64 reductions) or double (plain form)
 template <typename T>
 __global__ void __launch_bounds__(NT) jacobi_coop_kernel(T* X, int64_t len, T* Q, int64_t nvec, double tol,
-                                                        double floor_rel, const double* frob2, Sync s) {
+                                                        double floor_rel, const double* frob2, int max_sweeps,
+                                                        Sync s) {
     __shared__ double sm[32];
     __shared__ double rot_cs, rot_sn;
     __shared__ int do_rot;
@@ -85,7 +86,7 @@ __global__ void __launch_bounds__(NT) jacobi_coop_kernel(T* X, int64_t len, T* Q
     const double floor = floor_rel * (*frob2);
     int sweep = 0;
     bool ok = true;
-    for (; sweep < MAX_SWEEPS && ok; ++sweep) {
+    for (; sweep < max_sweeps && ok; ++sweep) {
         for (int r = 0; r < P - 1 && ok; ++r) {
             for (int k = blockIdx.x; k < P / 2; k += gridDim.x) {
                 int p, q;
@@ -147,7 +148,7 @@ __global__ void __launch_bounds__(NT) jacobi_coop_kernel(T* X, int64_t len, T* Q
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *s.sweeps = sweep;
-        if (ok && sweep >= MAX_SWEEPS && *(volatile int*)&s.rot[MAX_SWEEPS - 1] != 0)
+        if (ok && sweep >= max_sweeps && *(volatile int*)&s.rot[max_sweeps - 1] != 0)
             ct_set_status(s.status, CT_ERR_NOCONV);
     }
 }
@@ -179,7 +180,9 @@ int run(ct_handle* h, T* X, int64_t len, T* Q, int64_t nvec, double tol, double 
     int64_t grid = (int64_t)occ * h->num_sms;
     if (grid > pairs) grid = pairs;
     if (grid < 1) grid = 1;
-    void* args[] = {&X, &len, &Q, &nvec, &tol, &floor_rel, (void*)&frob2, &s};
+    // the handle's sweep cap (ct_set_svd_max_sweeps) never exceeds the kernel's own
+    int max_sweeps = (h->svd_max_sweeps > 0 && h->svd_max_sweeps < MAX_SWEEPS) ? h->svd_max_sweeps : MAX_SWEEPS;
+    void* args[] = {&X, &len, &Q, &nvec, &tol, &floor_rel, (void*)&frob2, &max_sweeps, &s};
     CT_CUDA(h, cudaLaunchCooperativeKernel((const void*)jacobi_coop_kernel<T>, dim3((unsigned)grid), dim3(NT), args,
                                            0, h->stream));
     ct_note_launch();

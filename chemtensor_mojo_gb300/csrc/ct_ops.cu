@@ -234,8 +234,10 @@ int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, do
     CT_TRY(ct_heff_prepare(h, ar, plan, prec, L, R, W1, W2, Dl, d, Dr, wL, wM, wR));
     const int* stop = h->d_flags + FL_STOP;
     CT_TRY(ct_lanczos_init(h, max_iter));
-    // v0 = theta / |theta|  (zero norm -> CT_ERR_ZERO_NORM, dmrg.mojo:605-611)
+    // v0 = theta / |theta|  (zero norm -> CT_ERR_ZERO_NORM, dmrg.mojo:605-611; a NaN
+    // or infinite norm -> CT_ERR_NONFINITE, where the reference would carry NaN on)
     CT_TRY(ct_reduce_nrm2sq(h, N, theta_in, h->d_scalars + SC_NORM, nullptr));
+    CT_TRY(ct_check_finite(h, h->d_scalars + SC_NORM, nullptr));
     CT_TRY(ct_scale_by_inv_sqrt(h, N, theta_in, V, h->d_scalars + SC_NORM, nullptr, CT_ERR_ZERO_NORM));
     const double thr = 100.0 * (double)N * 2.2204460492503131e-16;
     // algorithmic FLOPs of one apply (the reference's four contractions)
@@ -263,6 +265,8 @@ int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, do
         CT_TRY(ct_lanczos_alpha(h, N, vj, w, j, stop));
     }
     CT_TRY(ct_tridiag_eig(h, max_iter, tol, max_rotations));
+    // non-finite environments or MPO tensors surface here, in the eigenvalue
+    CT_TRY(ct_check_finite(h, h->d_scalars + SC_ENERGY, nullptr));
     CT_TRY(ct_ritz(h, N, V, N, w));
     CT_TRY(ct_reduce_nrm2sq(h, N, w, h->d_scalars + SC_NORM, nullptr));
     CT_TRY(ct_scale_by_inv_sqrt(h, N, w, theta_out, h->d_scalars + SC_NORM, nullptr, 0));

@@ -146,10 +146,10 @@ __global__ void svd_norms_kernel(const double* X, int64_t len, int64_t ldx, int6
 __global__ void svd_rank_kernel(const double* sig, int64_t nvec, int* perm) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nvec) return;
-    const double sj = sig[j];
+    const double sj = ct_rank_key(sig[j]);
     int64_t rank = 0;
     for (int64_t i = 0; i < nvec; ++i) {
-        const double si = sig[i];
+        const double si = ct_rank_key(sig[i]);
         if (si > sj || (si == sj && i < j)) ++rank;
     }
     perm[rank] = (int)j;
@@ -320,7 +320,9 @@ static int svd_run_geometry(ct_handle* h, Arena& ar, const double* M, int64_t m,
                                                 200 * 1024));
                 attr = true;
             }
-            svd_small_kernel<<<1, SVD_NT, small_bytes, h->stream>>>(X, len, ldx, Q, (int)nvec, tol, SVD_MAX_SWEEPS,
+            const int cap = (h->svd_max_sweeps > 0 && h->svd_max_sweeps < SVD_MAX_SWEEPS) ? h->svd_max_sweeps
+                                                                                            : SVD_MAX_SWEEPS;
+            svd_small_kernel<<<1, SVD_NT, small_bytes, h->stream>>>(X, len, ldx, Q, (int)nvec, tol, cap,
                                                                     h->d_status); ct_note_launch();
             CT_LAUNCH_CHECK(h);
         } else {

@@ -53,10 +53,10 @@ __global__ void norms32_kernel(const float* X, int64_t len, int64_t nvec, double
 __global__ void rank_desc_kernel(const double* sig, int64_t n, int* perm) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    const double sj = sig[j];
+    const double sj = ct_rank_key(sig[j]);
     int64_t rank = 0;
     for (int64_t i = 0; i < n; ++i) {
-        const double si = sig[i];
+        const double si = ct_rank_key(sig[i]);
         if (si > sj || (si == sj && i < j)) ++rank;
     }
     perm[rank] = (int)j;

@@ -109,6 +109,11 @@ __global__ void scale_inv_sqrt_kernel(int64_t n, const double* x, double* y, con
         y[i] = x[i] * inv;
 }
 
+__global__ void check_finite_kernel(const double* x, int* status, const int* skip) {
+    if (ct_skip(skip)) return;
+    if (!isfinite(*x)) ct_set_status(status, CT_ERR_NONFINITE);
+}
+
 __global__ void identity_env_kernel(double* E, int64_t w, int64_t D) {
     const int64_t n = w * D * D;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
@@ -290,6 +295,18 @@ __global__ void tridiag_jacobi_kernel(double* scalars, int* flags, int* status, 
         if (lane == 0) ct_set_status(status, CT_ERR_INVALID);
         return;
     }
+    // a NaN or infinite alpha / beta (non-finite environments or MPO tensors) is an
+    // error, not an eigenvalue: the rotations would compare NaN with every pivot
+    bool bad = false;
+    for (int i = lane; i < n; i += 32)
+        bad |= !isfinite(scalars[SC_ALPHA + i]) || (i + 1 < n && !isfinite(scalars[SC_BETA + i]));
+    if (__any_sync(0xffffffffu, bad)) {
+        if (lane == 0) {
+            ct_set_status(status, CT_ERR_NONFINITE);
+            scalars[SC_ENERGY] = NAN;
+        }
+        return;
+    }
     double* A = tsm;           // n x n
     double* V = tsm + n * n;   // n x n
     for (int t = lane; t < n * n; t += 32) {
@@ -393,9 +410,20 @@ __global__ void tridiag_bisect_kernel(double* scalars, const int* flags, int* st
         if (lane == 0) ct_set_status(status, CT_ERR_INVALID);
         return;
     }
+    bool bad = false;
     for (int i = lane; i < n; i += 32) {
         a[i] = scalars[SC_ALPHA + i];
         b[i] = (i + 1 < n) ? scalars[SC_BETA + i] : 0.0;
+        bad |= !isfinite(a[i]) || !isfinite(b[i]);
+    }
+    // non-finite alpha / beta: fmin / fmax of the Gershgorin bounds would skip the
+    // NaN and the multisection would return a finite, meaningless eigenvalue
+    if (__any_sync(0xffffffffu, bad)) {
+        if (lane == 0) {
+            ct_set_status(status, CT_ERR_NONFINITE);
+            scalars[SC_ENERGY] = NAN;
+        }
+        return;
     }
     __syncwarp();
     if (lane == 0) {
@@ -489,6 +517,12 @@ int ct_scale_by_inv_sqrt(ct_handle* h, int64_t n, const double* x, double* y, co
 int ct_fill(ct_handle* h, double* x, int64_t n, double v) {
     if (n <= 0) return CT_OK;
     fill_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(x, n, v); ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_check_finite(ct_handle* h, const double* d_x, const int* skip) {
+    check_finite_kernel<<<1, 1, 0, h->stream>>>(d_x, h->d_status, skip); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }

@@ -47,7 +47,7 @@ enum ct_status {
     CT_ERR_ZERO_NORM = -5,   /* Lanczos start vector has zero norm               */
     CT_ERR_SHAPE = -6,       /* inconsistent shapes                              */
     CT_ERR_UNSUPPORTED = -7, /* shape/precision not supported by this library    */
-    CT_ERR_NONFINITE = -8,   /* NaN/Inf met in a reduction                       */
+    CT_ERR_NONFINITE = -8,   /* NaN/Inf in an input norm or an eigenvalue         */
     CT_ERR_EMPTY = -9,       /* truncation kept zero singular values             */
     CT_ERR_TOO_LARGE = -10   /* problem exceeds the static scratch of a no-alloc entry */
 };
@@ -74,6 +74,12 @@ CT_API int ct_workspace_bytes(ct_handle* h, int64_t* bytes_out);
 CT_API int ct_svd_sweeps(ct_handle* h, int* last_host, int64_t* total_host);
 /* cap on handle-owned scratch in bytes (0 = unlimited); growth beyond it -> CT_ERR_OOM */
 CT_API int ct_set_workspace_limit(ct_handle* h, int64_t bytes);
+/* cap on the one-sided Jacobi sweeps of every SVD on this handle (0 = the
+ * built-in caps, 60 for one-CTA problems and 48 for the cooperative kernel;
+ * larger values are clamped to those).  A split that has not converged within
+ * the cap returns CT_ERR_NOCONV, the counterpart of LAPACK dgesdd's info > 0,
+ * which the reference turns into an error (src/mylinalg/svd.mojo:74-76).     */
+CT_API int ct_set_svd_max_sweeps(ct_handle* h, int max_sweeps);
 
 /* ---- dense tensor core (src/m_tensor/dense_tensor.mojo) --------------------
  * Row-major C[m,n] = alpha * op(A) op(B) + beta * C, op = identity or transpose.
