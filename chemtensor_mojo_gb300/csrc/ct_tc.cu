@@ -605,6 +605,244 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
 }
 
+// Chunked accumulation.  The tensor cores add into the FP32 accumulator with
+// truncation (round toward zero): every MMA shrinks the running sum's magnitude
+// by a fraction of an ulp, so a product summed over K in one accumulator comes
+// out too small by ~6e-9 per unit of K (-3e-5 relative at K = 5120).  This
+// variant bounds the number of adds into any accumulator: each tile's K range is
+// cut into chunks of `kc` k-blocks (kc * 32 of K); every chunk starts a fresh
+// TMEM accumulator, alternating between two BN-column buffers, and the epilogue
+// warps add the chunks in FP32 registers with round-to-nearest, whose errors
+// have no sign preference.  The bias left is that of one chunk, kc times that of
+// one 32-wide k-block (~1.8e-7).
+//   * one CTA per SM walks tiles c, c + G, ... (no stream-K);
+//   * warps: 0 TMA producer, 1 TMEM allocator + MMA issuer, 2..9 epilogue;
+//     epilogue warp w reads TMEM lane quadrant w % 4 (the quadrant a warp may
+//     access) and column half (w - 2) / 4 of the tile, holding BN / 2 FP32
+//     running sums per thread;
+//   * acc_full[b] is committed by the MMA thread after a chunk's last MMA,
+//     acc_empty[b] released by the eight epilogue warps once the chunk is in
+//     registers, so the MMAs of chunk i + 1 run while chunk i is read; a tile's
+//     stores overlap the next tile's first two chunks.
+constexpr int TC_THREADS_CH = 320;
+
+__device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t (&r)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Registers: each SM sub-partition holds 16K of them and 10 warps put 3 on some
+// sub-partitions, so a thread gets at most 168; the 128 x 256 tile's 128 running
+// sums per thread fit when TMEM is read 8 columns at a time.
+template <int BN, int STAGES>
+__global__ void __launch_bounds__(TC_THREADS_CH, 1)
+    tc_gemm_chunk_kernel(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
+                         const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl, int M,
+                         int N, int Kpad, int kc, TcEpi epi, const int* skip, int* status) {
+    using L = TcSmem<BN, STAGES>;
+    constexpr int HC = BN / 2;   // columns per epilogue warp
+    if (ct_skip(skip)) return;
+    extern __shared__ uint8_t tc_smem_raw[];
+    uint8_t* smem = tc_smem_raw + ((1024u - (smem_u32(tc_smem_raw) & 1023u)) & 1023u);
+    uint64_t* full = (uint64_t*)(smem + L::TILE_BYTES);
+    uint64_t* empty = full + STAGES;
+    uint64_t* acc_full = empty + STAGES;
+    uint64_t* acc_empty = acc_full + 2;
+    uint32_t* tmem_slot = (uint32_t*)(acc_empty + 2);
+    volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tiles_n = (N + BN - 1) / BN;
+    const int tiles = tiles_n * ((M + TC_BM - 1) / TC_BM);
+    const int nkb = Kpad / TC_BK;
+    const int c = blockIdx.x, G = gridDim.x;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 8);
+        }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"((uint32_t)(2 * BN))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int g = 0;
+            bool ok = true;
+            for (int t = c; t < tiles && ok; t += G) {
+                const int m0 = (t / tiles_n) * TC_BM, n0 = (t % tiles_n) * BN;
+                for (int kb = 0; kb < nkb; ++kb, ++g) {
+                    const int s = g % STAGES;
+                    const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
+                    if (g >= STAGES && !mbar_wait(&empty[s], ph ^ 1u, abort_flag)) {
+                        *abort_flag = 1;
+                        ct_set_status(status, CT_ERR_CUDA);
+                        ok = false;
+                        break;
+                    }
+                    uint8_t* st = smem + s * L::STAGE_BYTES;
+                    mbar_expect_tx(&full[s], L::STAGE_BYTES);
+                    const int x = kb * TC_BK;
+                    tma_load_2d(st, &tmAh, x, m0, &full[s]);
+                    tma_load_2d(st + L::A_BYTES, &tmAl, x, m0, &full[s]);
+                    tma_load_2d(st + 2 * L::A_BYTES, &tmBh, x, n0, &full[s]);
+                    tma_load_2d(st + 2 * L::A_BYTES + L::B_BYTES, &tmBl, x, n0, &full[s]);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_tf32(TC_BM, BN);
+            int g = 0, gc = 0;
+            bool ok = true;
+            for (int t = c; t < tiles && ok; t += G) {
+                for (int kb0 = 0; kb0 < nkb && ok; kb0 += kc, ++gc) {
+                    const int b = gc & 1, u = gc >> 1;
+                    if (u > 0 && !mbar_wait(&acc_empty[b], (uint32_t)((u - 1) & 1), abort_flag)) {
+                        *abort_flag = 1;
+                        ct_set_status(status, CT_ERR_CUDA);
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t dt = tmem + (uint32_t)(b * BN);
+                    const int kb1 = kb0 + kc < nkb ? kb0 + kc : nkb;
+                    for (int kb = kb0; kb < kb1; ++kb, ++g) {
+                        const int s = g % STAGES;
+                        const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
+                        if (!mbar_wait(&full[s], ph, abort_flag)) {
+                            *abort_flag = 1;
+                            ct_set_status(status, CT_ERR_CUDA);
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t a_hi = smem_u32(smem + s * L::STAGE_BYTES);
+                        const uint32_t a_lo = a_hi + L::A_BYTES;
+                        const uint32_t b_hi = a_hi + 2 * L::A_BYTES;
+                        const uint32_t b_lo = b_hi + L::B_BYTES;
+#pragma unroll
+                        for (int kk = 0; kk < TC_BK / 8; ++kk) {
+                            const uint32_t off = kk * 32;
+                            const uint32_t acc0 = (kb > kb0 || kk > 0) ? 1u : 0u;
+                            mma_tf32(dt, sw128_desc(a_lo + off), sw128_desc(b_hi + off), idesc, acc0);
+                            mma_tf32(dt, sw128_desc(a_hi + off), sw128_desc(b_lo + off), idesc, 1u);
+                            mma_tf32(dt, sw128_desc(a_hi + off), sw128_desc(b_hi + off), idesc, 1u);
+                        }
+                        mma_commit(&empty[s]);
+                    }
+                    if (ok) mma_commit(&acc_full[b]);
+                }
+            }
+        }
+    } else {
+        const int q = warp & 3;              // TMEM lane quadrant of this warp
+        const int hf = (warp - 2) >> 2;      // column half of the tile
+        const int row = q * 32 + lane;
+        float sum[HC];
+        int gc = 0;
+        bool ok = true;
+        for (int t = c; t < tiles && ok; t += G) {
+#pragma unroll
+            for (int j = 0; j < HC; ++j) sum[j] = 0.f;
+            for (int kb0 = 0; kb0 < nkb; kb0 += kc, ++gc) {
+                const int b = gc & 1, u = gc >> 1;
+                if (!mbar_wait(&acc_full[b], (uint32_t)(u & 1), abort_flag)) {
+                    *abort_flag = 1;
+                    ct_set_status(status, CT_ERR_CUDA);
+                    ok = false;
+                    break;
+                }
+                __syncwarp();
+                tc_fence_after();
+                const uint32_t tq = tmem + (uint32_t)(b * BN + hf * HC) + ((uint32_t)(q * 32) << 16);
+#pragma unroll
+                for (int cc = 0; cc < HC; cc += 8) {
+                    uint32_t r[8];
+                    tmem_ld8_nowait(tq + (uint32_t)cc, r);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) sum[cc + j] += __uint_as_float(r[j]);
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&acc_empty[b]);
+            }
+            if (!ok) break;
+            const int m0 = (t / tiles_n) * TC_BM;
+            const int n0 = (t % tiles_n) * BN + hf * HC;
+            const int64_t m = (int64_t)m0 + row;
+            if (m >= M) continue;
+            const int64_t rbase = (m / epi.M0) * epi.sCm1 + (m % epi.M0) * epi.sCm0;
+#pragma unroll
+            for (int cc = 0; cc < HC; cc += 16) {
+                const int64_t nb = (int64_t)n0 + cc;
+                if (epi.vec && nb + 16 <= N) {
+                    if (epi.out_fp64) {
+                        double2* Cd = (double2*)((double*)epi.C + rbase + nb);
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            double2 o;
+                            o.x = epi.alpha * (double)sum[cc + 2 * j];
+                            o.y = epi.alpha * (double)sum[cc + 2 * j + 1];
+                            if (epi.beta != 0.0) {
+                                const double2 c0 = Cd[j];
+                                o.x = fma(epi.beta, c0.x, o.x);
+                                o.y = fma(epi.beta, c0.y, o.y);
+                            }
+                            Cd[j] = o;
+                        }
+                    } else {
+                        float4* Cf = (float4*)((float*)epi.C + rbase + nb);
+                        const float a = (float)epi.alpha;
+#pragma unroll
+                        for (int j = 0; j < 4; ++j)
+                            Cf[j] = make_float4(a * sum[cc + 4 * j], a * sum[cc + 4 * j + 1], a * sum[cc + 4 * j + 2],
+                                                a * sum[cc + 4 * j + 3]);
+                    }
+                    continue;
+                }
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int64_t n = nb + j;
+                    if (n >= N) break;
+                    if (epi.out_fp64) {
+                        double* Cd = (double*)epi.C + rbase;
+                        double v = epi.alpha * (double)sum[cc + j];
+                        if (epi.beta != 0.0) v = fma(epi.beta, Cd[n], v);
+                        Cd[n] = v;
+                    } else {
+                        ((float*)epi.C)[rbase + n] = (float)epi.alpha * sum[cc + j];
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)(2 * BN))
+                     : "memory");
+    }
+}
+
 // ---------------------------------------------------------------------------
 // operand packer: FP64 source -> split TF32 planes [rows][ldk], K-major.
 // row r = r1 * R0 + r0 ; col k = k1 * K0p + k0 (k0 < K0 valid, K0..K0p zero)
@@ -852,6 +1090,15 @@ bool tc_use_stream_k() {
     return v;
 }
 
+// K-blocks (32 of K each) per TMEM accumulator of the chunked kernel: CTDMRG_TC_KCHUNK=n, read
+// on every launch like CTDMRG_TC_BN; 0 selects the single-accumulator persistent kernel.
+int tc_kchunk() {
+    const char* e = getenv("CTDMRG_TC_KCHUNK");
+    if (!e) return 2;
+    const int k = atoi(e);
+    return k < 0 ? 0 : (k > 1024 ? 1024 : k);
+}
+
 // Wide tiles when their whole waves cost less.  Time per tile ~ BN at equal K; at K <= 2048 the
 // wide tile's fixed per-tile cost (pipeline fill, epilogue) is spread over twice the MMAs, measured
 // as 1.12x the narrow tile's rate per flop (5120x4096x1024: 0.164 vs 0.166 ms; 2048x2048x1024:
@@ -888,10 +1135,18 @@ int tc_gemm_run(ct_handle* h, const SplitOperand& A, const SplitOperand& B, int6
                                         L::TOTAL));
         CT_CUDA(h, cudaFuncSetAttribute(tc_gemm_persist_kernel<BN, STAGES>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, L::TOTAL));
+        CT_CUDA(h, cudaFuncSetAttribute(tc_gemm_chunk_kernel<BN, STAGES>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, L::TOTAL));
         attr_dev = h->device;
     }
     const int64_t tiles = ct_cdiv(N, BN) * ct_cdiv(M, TC_BM);
-    if (tc_use_persistent()) {
+    const int kc = tc_kchunk();
+    if (tc_use_persistent() && kc > 0 && !tc_use_stream_k()) {
+        const int64_t grid = tiles < h->num_sms ? tiles : h->num_sms;
+        tc_gemm_chunk_kernel<BN, STAGES><<<(unsigned)grid, TC_THREADS_CH, L::TOTAL, h->stream>>>(
+            ta_h, ta_l, tb_h, tb_l, (int)M, (int)N, (int)A.ldk, kc, epi, skip, h->d_status);
+        ct_note_launch();
+    } else if (tc_use_persistent()) {
         const int64_t grid = tiles < h->num_sms ? tiles : h->num_sms;
         // stream-K when the tiles leave a partial last wave and every CTA's share
         // of k-blocks covers at least one whole tile (so a tile has at most two owners)

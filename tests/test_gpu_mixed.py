@@ -73,6 +73,54 @@ def test_tc_gemm_tile_widths(ctx, monkeypatch, bn, m, n, k):
     assert rel(tC.to_numpy(), ref) < TOL
 
 
+def _tc_gemm(ctx, A, B):
+    import ctypes as C
+    import torch
+    m, k = A.shape
+    n = B.shape[1]
+    tA, tB, tC = dt(ctx, A), dt(ctx, B), dt(ctx, np.zeros((m, n)))
+    ctx.call("ct_gemm", 1, 0, 0, C.c_int64(m), C.c_int64(n), C.c_int64(k), C.c_double(1.0),
+             C.c_void_p(tA.storage.data_ptr()), C.c_int64(k), C.c_void_p(tB.storage.data_ptr()), C.c_int64(n),
+             C.c_double(0.0), C.c_void_p(tC.storage.data_ptr()), C.c_int64(n))
+    torch.cuda.synchronize()
+    return tC.to_numpy()
+
+
+@pytest.mark.parametrize("bn", ["128", "256"])
+@pytest.mark.parametrize("kc", ["1", "2", "3", "64"])
+@pytest.mark.parametrize("m,n,k", [(128, 256, 32), (300, 520, 200), (257, 1000, 1000)])
+def test_tc_gemm_chunked(ctx, monkeypatch, bn, kc, m, n, k):
+    """The chunked-accumulation kernel (CTDMRG_TC_KCHUNK k-blocks per TMEM
+    accumulator) on ragged shapes, chunk counts that do and do not divide K, and
+    both tile widths."""
+    monkeypatch.setenv("CTDMRG_TC_BN", bn)
+    monkeypatch.setenv("CTDMRG_TC_KCHUNK", kc)
+    rng = np.random.default_rng(m + 3 * n + k)
+    A = rng.standard_normal((m, k))
+    B = rng.standard_normal((k, n))
+    assert rel(_tc_gemm(ctx, A, B), A @ B) < TOL
+
+
+def test_tc_gemm_accumulation_bias(ctx, monkeypatch):
+    """All-positive operands, K = 5120: every partial sum has the same sign, so the
+    truncating FP32 accumulation of the tensor cores shrinks the product coherently.
+    In one accumulator that is ~3e-5 of the result; with a fresh accumulator every
+    64 of K (the default) and the chunks added in FP32 with round-to-nearest it
+    stays below 1e-6."""
+    rng = np.random.default_rng(17)
+    A = rng.random((256, 5120))
+    B = rng.random((5120, 256))
+    ref = A @ B
+    monkeypatch.setenv("CTDMRG_TC_KCHUNK", "0")
+    bias_single = float(np.mean(_tc_gemm(ctx, A, B) / ref - 1.0))
+    monkeypatch.delenv("CTDMRG_TC_KCHUNK")
+    out = _tc_gemm(ctx, A, B)
+    bias_chunked = float(np.mean(out / ref - 1.0))
+    assert bias_single < -5e-6, bias_single
+    assert abs(bias_chunked) < 1e-6, bias_chunked
+    assert np.max(np.abs(out / ref - 1.0)) < 2e-6
+
+
 def test_dense_tensor_dot_tf32x3(ctx):
     ct = ct_mod()
     rng = np.random.default_rng(11)
