@@ -46,7 +46,16 @@ import time
 # The reference arm times the CPU oracle with every host core.  A launcher that pins BLAS to
 # one thread per rank (torchrun sets OMP_NUM_THREADS=1) is overridden here, before NumPy
 # loads its BLAS; only rank 0 of that arm does any work.
-if "--impl" in sys.argv and "reference" in sys.argv:
+def _impl_from_argv(argv):
+    for k, a in enumerate(argv):
+        if a == "--impl" and k + 1 < len(argv):
+            return argv[k + 1]
+        if a.startswith("--impl="):
+            return a.split("=", 1)[1]
+    return "ours"
+
+
+if _impl_from_argv(sys.argv[1:]) == "reference":
     for _var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
         os.environ[_var] = str(os.cpu_count() or 1)
 
@@ -83,7 +92,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the FP64/roofline/CPU side measurements")
     ap.add_argument("--verbose", action="store_true", help="log every split of the timed sweeps to stderr")
     ap.add_argument("--mode", default="sweep",
-                    choices=["sweep", "heff", "heff-grid", "split", "hubbard", "contractions"],
+                    choices=["sweep", "heff", "heff-grid", "split", "hubbard", "contractions", "fp64-ref",
+                             "lanczos"],
                     help="heff / split: only centre-bond H_eff applies / warm splits (small, fixed workloads "
                          "for profilers); heff-grid: H_eff over chi x D x d; contractions: the MPS/MPO "
                          "contraction operations of the reference's contraction benchmark")
@@ -92,6 +102,8 @@ def parse():
     ap.add_argument("--runs", type=int, default=3, help="contractions: timed repetitions per operation")
     ap.add_argument("--jsonl", default="", help="contractions: append one JSONL record per operation here")
     ap.add_argument("--ramp-sweeps", default="", help="hubbard: sweeps per ramp stage, e.g. 1,1,1,1")
+    ap.add_argument("--out", default="", help="fp64-ref: also write the JSON line to this file")
+    ap.add_argument("--forms", default="fp64,tf32x3", help="fp64-ref: forms to run")
     return ap.parse_args()
 
 
@@ -125,6 +137,78 @@ def heff_mode(args):
                       "dtype": args.prec, "config": {"workload": f"centre-bond H_eff chi={chi} D=5 d=2"},
                       "steps": args.steps, "warmup": args.warmup,
                       "gpu_launches": _lib.launch_count() - n0}), flush=True)
+
+
+def lanczos_mode(args):
+    """W + K centre-bond Lanczos runs (ct_lanczos2, 24 steps, reorthogonalised) at
+    (chi, D=5, d=2) on random symmetric L, R [5, chi, chi], W [5, 2, 2, 5] and theta
+    (profiling workload).  Reports seconds per run, the H_eff share, and the
+    Krylov vector work's algorithmic bytes over its CUDA-event time (GB/s).  One
+    JSON line."""
+    import ctypes as C
+    import torch
+    import chemtensor_mojo_gb300 as ct
+    from chemtensor_mojo_gb300 import _lib
+    ctx = ct.get_context(0)
+    chi = args.chi
+    mpo = ct.create_spin_half_xxz_mpo(ctx, 8, 1.0)
+    W = mpo.sites[3]
+    g = torch.Generator(device="cpu").manual_seed(9)
+    dev = ctx.torch_device
+
+    def sym(t):
+        return (0.5 * (t + t.transpose(1, 2))).contiguous()
+
+    th = ct.DenseTensor(torch.randn(chi * 4 * chi, generator=g, dtype=torch.float64).to(dev), [chi, 2, 2, chi])
+    Le = ct.DenseTensor(sym(torch.randn(MPO_D, chi, chi, generator=g, dtype=torch.float64)).reshape(-1).to(dev),
+                        [MPO_D, chi, chi])
+    Re = ct.DenseTensor(sym(torch.randn(MPO_D, chi, chi, generator=g, dtype=torch.float64)).reshape(-1).to(dev),
+                        [MPO_D, chi, chi])
+
+    def run():
+        return ct.lanczos_two_site_optimize(th, Le, Re, W, W, ctx, max_iter=LANCZOS, tol=1e-10, prec=args.prec,
+                                            max_rotations=0, reorth=True)
+
+    for _ in range(args.warmup):
+        run()
+    torch.cuda.synchronize()
+    ctx.call("ct_kernel_timing", 1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = _lib.launch_count()
+    e0.record()
+    for _ in range(args.steps):
+        E, _ = run()
+    e1.record()
+    torch.cuda.synchronize()
+    launches = _lib.launch_count() - n0
+
+    def read_class(cls):
+        n_kt, ms_kt, fl_kt = C.c_int64(), C.c_double(), C.c_double()
+        ctx.call("ct_kernel_timing_read_class", cls, C.byref(n_kt), C.byref(ms_kt), C.byref(fl_kt))
+        return n_kt.value, ms_kt.value * 1e-3, fl_kt.value
+
+    _, heff_s, _ = read_class(1)
+    nvec, vec_s, vec_bytes = read_class(3)
+    ctx.call("ct_kernel_timing", 0)
+    s = e0.elapsed_time(e1) * 1e-3 / max(args.steps, 1)
+    peaks = read_peaks()
+    print(json.dumps({"metric": "Lanczos run seconds", "value": s, "unit": "s/run", "dtype": args.prec,
+                      "config": {"workload": f"centre-bond Lanczos chi={chi} D=5 d=2, {LANCZOS} steps, "
+                                             "reorthogonalised"},
+                      "energy": E, "heff_s_per_run": heff_s / max(args.steps, 1),
+                      "vector_s_per_run": vec_s / max(args.steps, 1), "vector_steps": nvec,
+                      "vector_bytes_per_run": vec_bytes / max(args.steps, 1),
+                      "lanczos_gbs": vec_bytes / max(vec_s, 1e-12) / 1e9,
+                      "lanczos_frac_of_hbm": vec_bytes / max(vec_s, 1e-12) / 1e9 / peaks.get("hbm_gbs", 6800.0),
+                      "steps": args.steps, "warmup": args.warmup, "gpu_launches": launches}), flush=True)
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
 
 
 def split_mode(args):
@@ -267,6 +351,68 @@ def hubbard_mode(args):
                       "gradient": gradient,
                       "peak_device_bytes": int(peak_used), "device_bytes_before": int(total - free0)}),
           flush=True)
+
+
+ACC_SEED = 7
+
+
+def schedule_run(ctx, ct, mpo, arrays, schedule, prec):
+    """One call of dmrg_two_site per sweep of `schedule` (chi_max per sweep) from the
+    right-normalised MPS of `arrays`; the FP64 Rayleigh quotient of the MPS after each
+    sweep, contracted on the device.  Per sweep: chi_max, Lanczos energy, Rayleigh
+    energy, seconds (the call's wall clock without the Rayleigh contraction), splits."""
+    mps = ct.mps_right_normalize(ctx, ct.mps_from_arrays(ctx, arrays))
+    out = []
+    for k, c in enumerate(schedule):
+        st = ct.DMRGStats()
+        E, mps = ct.dmrg_two_site(ctx, mpo, mps, ct.DMRGParams(
+            num_sweeps=1, chi_max=c, eps_trunc=EPS, max_krylov_iter=LANCZOS, krylov_tol=1e-10, energy_tol=0.0,
+            max_rotations=0, prec=prec, final_rayleigh=True, keep_bases=(prec == "tf32x3" and k > 0)), st)
+        out.append({"chi_max": c, "energy_lanczos": E, "energy_rayleigh": st.energy_rayleigh,
+                    "seconds": st.seconds_total - st.seconds_rayleigh, "seconds_rayleigh": st.seconds_rayleigh,
+                    "seconds_lanczos": st.seconds_lanczos, "seconds_split": st.seconds_svd,
+                    "seconds_env": st.seconds_env, "max_discarded": st.max_discarded,
+                    "subspace_splits": st.subspace_splits, "exact_splits": st.exact_splits})
+    return out
+
+
+def fp64_ref_mode(args):
+    """The plain FP64 form against the mixed form at the headline size.
+
+    Heisenberg chain L=64 (D=5, d=2), seeded Gaussian start (seed 7), right-
+    normalised; chi_max 64, 256, then --steps sweeps at --chi (1024), one call
+    per sweep, 24 Lanczos steps, eps_trunc = 0, converged eigensolve, in both
+    forms.  Reports each form's seconds per sweep at --chi (measured, not
+    estimated) and, per sweep, |dE/E| between the FP64 Rayleigh quotients of the
+    two forms' MPS.  The FP64 form's trajectory is deterministic (fixed-order
+    reductions), so its energies serve later runs of the mixed form on the same
+    schedule as the reference (--out writes the JSON line to a file).
+    """
+    import chemtensor_mojo_gb300 as ct
+    ctx = ct.get_context(0)
+    L = args.L
+    mpo = ct.create_spin_half_xxz_mpo(ctx, L, 1.0)
+    arrays, _ = ct.random_mps_c_compatible_arrays(L, D_PHYS, RAMP[0], ACC_SEED)
+    schedule = [64, 256] + [args.chi] * max(args.steps, 1)
+    runs = {pr: schedule_run(ctx, ct, mpo, arrays, schedule, pr) for pr in args.forms.split(",")}
+    line = {"metric": "FP64 vs mixed two-site sweep at chi_max", "unit": "s/sweep", "data": "synthetic",
+            "config": {"workload": f"heisenberg_xxz L={L} d=2 D=5 seed={ACC_SEED} chi schedule "
+                                   f"{','.join(map(str, schedule))} lanczos={LANCZOS} eps={EPS}",
+                       "eigensolver": "converged tridiagonal"},
+            "schedule": schedule, "runs": runs}
+    at = [k for k, c in enumerate(schedule) if c == args.chi]
+    for pr, r in runs.items():
+        line[f"{pr}_s_per_sweep_at_chi"] = float(np.mean([r[k]["seconds"] for k in at]))
+    if "fp64" in runs and "tf32x3" in runs:
+        a, b = runs["tf32x3"], runs["fp64"]
+        line["dE_over_E_each_sweep"] = [abs(x["energy_rayleigh"] - y["energy_rayleigh"]) / abs(y["energy_rayleigh"])
+                                        for x, y in zip(a, b)]
+        line["dE_over_E_at_chi"] = max(line["dE_over_E_each_sweep"][k] for k in at)
+        line["speedup_mixed_vs_fp64_at_chi"] = line["fp64_s_per_sweep_at_chi"] / line["tf32x3_s_per_sweep_at_chi"]
+    print(json.dumps(line), flush=True)
+    if args.out:
+        with open(args.out, "w") as f:
+            f.write(json.dumps(line) + "\n")
 
 
 def heff_grid_mode(args):
@@ -538,6 +684,12 @@ def main():
     if args.mode == "heff-grid":
         heff_grid_mode(args)
         return
+    if args.mode == "fp64-ref":
+        fp64_ref_mode(args)
+        return
+    if args.mode == "lanczos":
+        lanczos_mode(args)
+        return
     if args.mode == "heff":
         heff_mode(args)
         return
@@ -597,6 +749,9 @@ def main():
     # large splits of the first half-sweep start from the kept bond bases
     tp = params(chi, args.steps)
     tp.keep_bases = True
+    # the reported energy is the FP64 Rayleigh quotient of the final MPS, contracted
+    # on the device inside the timed call (its cost is part of `value`)
+    tp.final_rayleigh = True
     tp.verbose = 2 if args.verbose else 0
     cp = tp.to_c()
     h2d = sum(h.numel() * 8 for h in host_sites) + sum(h.numel() * 8 for h in host_mpo)
@@ -634,6 +789,7 @@ def main():
     kt = None
     kt_heff = None
     kt_centre = None
+    kt_vec = None
     if kt_on:
         def read_class(cls):
             n_kt, ms_kt, fl_kt = C.c_int64(), C.c_double(), C.c_double()
@@ -642,6 +798,7 @@ def main():
         kt = read_class(0)        # every TF32x3 GEMM launch
         kt_heff = read_class(1)   # every whole H_eff apply inside Lanczos
         kt_centre = read_class(2)  # the applies at the largest size (centre bonds at chi_max)
+        kt_vec = read_class(3)     # Krylov vector work of every Lanczos step (flops field: bytes)
         ctx.call("ct_kernel_timing", 0)
     if dist is not None:
         dist.barrier()
@@ -653,12 +810,7 @@ def main():
     per_sweep = dev_s / (K * world)
     heff_tflops = stats.heff_flops / max(stats.seconds_lanczos, 1e-12) / 1e12
     final_dims = [int(x) for x in bd]
-    # FP64 Rayleigh quotient of the final state (outside the timed region)
-    e_rq = C.c_double()
-    n_rq = C.c_double()
-    ctx.call("ct_mps_expectation", _lib.CT_PREC_FP64, L, d, _lib.i64_array(mpo.bond_dims), mpo_pp, bd, mps_pp,
-             C.byref(e_rq), C.byref(n_rq))
-    energy_rq = e_rq.value / n_rq.value
+    energy_rq = stats.energy_rayleigh
 
     extras = {}
     if rank == 0 and not args.no_extras:
@@ -683,7 +835,8 @@ def main():
                    "global_batch": 1, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (MPS + environments + Krylov basis >> 129 MB)",
                    "eigensolver": "converged tridiagonal Jacobi"},
-        "energy": energy_rq, "energy_lanczos": Ec.value, "sweep_energies_lanczos": list(sweeps_e)[:done.value],
+        "energy": energy_rq, "energy_note": "FP64 Rayleigh quotient of the final MPS, inside the timed call",
+        "seconds_final_rayleigh": stats.seconds_rayleigh, "energy_lanczos": Ec.value, "sweep_energies_lanczos": list(sweeps_e)[:done.value],
         "bond_dims_final": final_dims,
         "heff_tflops": heff_tflops, "heff_applies": stats.heff_applies, "local_updates": stats.local_updates,
         "phase_seconds": {"lanczos": stats.seconds_lanczos, "svd": stats.seconds_svd,
@@ -735,6 +888,17 @@ def main():
             "note": "lanczos_other = Krylov vector kernels, eigensolve, Ritz vector; tc_gemm_s_all counts the "
                     "GEMMs of H_eff, environments and splits",
         }
+    if kt_vec and kt_vec["launches"] > 0 and kt_vec["ms"] > 0:
+        hbm = peaks.get("hbm_gbs", 6800.0)
+        gbs = kt_vec["flops"] / (kt_vec["ms"] * 1e-3) / 1e9
+        line["lanczos_vector"] = {
+            "gbs": gbs, "frac_of_hbm": gbs / hbm, "hbm_peak_gbs": hbm,
+            "peak_src": "measured" if "hbm_gbs" in peaks else "fallback",
+            "seconds": kt_vec["ms"] * 1e-3, "steps": kt_vec["launches"], "bytes": kt_vec["flops"],
+            "note": "every reorthogonalised Lanczos step of the timed sweeps: alpha (v_j, w read), recurrence "
+                    "(w, v_j, v_{j-1} read, w written), Gram-Schmidt dots (w and j+1 basis vectors read), update "
+                    "(read again, w written), next vector (w read, v written); 8 B per element, CUDA events on "
+                    "the launching stream"}
     if "cpu_sweep_s" in extras:
         line["cpu_baseline"] = {"value": extras["cpu_sweep_s"], "unit": "s/sweep", "cores": cpu_threads(),
                                 "kind": "port", "sample": extras["cpu_sample"]}

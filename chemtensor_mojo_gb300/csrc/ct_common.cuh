@@ -75,8 +75,10 @@ struct ct_handle {
 };
 
 // live timing classes; KT_HEFF_LARGEST is derived: the H_eff applies with the
-// largest FLOP count seen (the centre bond at chi_max)
-enum { KT_TC_GEMM = 0, KT_HEFF_APPLY = 1, KT_HEFF_LARGEST = 2, KT_NCLASSES = 4 };
+// largest FLOP count seen (the centre bond at chi_max).  KT_LANCZOS_VEC: the
+// Krylov vector work of each reorthogonalised Lanczos step (alpha, recurrence,
+// Gram-Schmidt pass, next vector), its "flops" field holding algorithmic bytes.
+enum { KT_TC_GEMM = 0, KT_HEFF_APPLY = 1, KT_HEFF_LARGEST = 2, KT_LANCZOS_VEC = 3, KT_NCLASSES = 4 };
 // start a timed region of class cls (slot = -1 when timing is off); end it after the launches
 int ct_ktime_begin(ct_handle* h, int cls, double flops, int* slot);
 int ct_ktime_end(ct_handle* h, int slot);
@@ -265,8 +267,10 @@ int ct_lanczos_update(ct_handle* h, int64_t n, double* w, const double* vj, cons
 int ct_lanczos_next(ct_handle* h, int64_t n, const double* w, double* vnext, int j, const int* skip);
 int ct_lanczos_alpha(ct_handle* h, int64_t n, const double* vj, const double* w, int j,
                      const int* skip);
-int ct_lanczos_reorth(ct_handle* h, int64_t n, double* w, const double* V, int64_t ldv, int nvec,
-                      double* coeff_scratch, const int* skip);
+int ct_lanczos_reorth_pass(ct_handle* h, int64_t n, double* w, const double* V, int64_t ldv, int j,
+                           double beta_threshold, const int* skip);
+int ct_lanczos_update_nonorm(ct_handle* h, int64_t n, double* w, const double* vj, const double* vjm1, int j,
+                             const int* skip);
 int ct_tridiag_eig(ct_handle* h, int max_iter, double tol, int max_rotations);
 int ct_ritz(ct_handle* h, int64_t n, const double* V, int64_t ldv, double* out);
 

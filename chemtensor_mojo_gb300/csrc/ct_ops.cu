@@ -250,9 +250,26 @@ int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, do
         CT_TRY(ct_ktime_begin(h, KT_HEFF_APPLY, heff_flops, &ks));
         CT_TRY(ct_heff_run(h, plan, vj, w, stop));
         CT_TRY(ct_ktime_end(h, ks));
+        if (reorth) {
+            // the reference recurrence, then one Gram-Schmidt pass against the whole
+            // Krylov basis (ct_lanczos_reorth_pass), then v_{j+1} = w / beta_j.
+            // Algorithmic bytes of the vector work: alpha reads v_j and w, the
+            // recurrence reads w, v_j, v_{j-1} and writes w, the pass reads w and j + 1
+            // vectors twice and writes w, the next vector reads w and writes v_{j+1}.
+            const double bytes = 8.0 * (double)N * (double)(2 + (j > 0 ? 4 : 3) + (j + 2) + (j + 3) + 2);
+            int kv = -1;
+            CT_TRY(ct_ktime_begin(h, KT_LANCZOS_VEC, bytes, &kv));
+            CT_TRY(ct_lanczos_alpha(h, N, vj, w, j, stop));
+            CT_TRY(ct_lanczos_update_nonorm(h, N, w, vj, vjm1, j, stop));
+            CT_TRY(ct_lanczos_reorth_pass(h, N, w, V, N, j, thr, stop));
+            CT_TRY(ct_lanczos_next(h, N, w, V + (int64_t)(j + 1) * N, j, stop));
+            CT_TRY(ct_ktime_end(h, kv));
+            continue;
+        }
+        // the reference's recurrence (dmrg.mojo:612-689): alpha, w -= alpha v_j + beta v_{j-1},
+        // beta = |w|, v_{j+1} = w / beta
         CT_TRY(ct_lanczos_alpha(h, N, vj, w, j, stop));
         CT_TRY(ct_lanczos_update(h, N, w, vj, vjm1, j, thr, stop));
-        if (reorth) CT_TRY(ct_lanczos_reorth_beta(h, N, w, V, N, j + 1, j, thr, stop));
         CT_TRY(ct_lanczos_next(h, N, w, V + (int64_t)(j + 1) * N, j, stop));
     }
     {   // final alpha-only iteration, only when no breakdown (dmrg.mojo:691-703)

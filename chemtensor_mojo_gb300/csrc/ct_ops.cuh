@@ -51,8 +51,6 @@ int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, do
 int ct_vec_axpy_launch(ct_handle* h, int64_t n, double alpha, const double* x, double* y);
 int ct_vec_scale_launch(ct_handle* h, int64_t n, double alpha, double* x);
 int ct_lanczos_init(ct_handle* h, int max_iter);
-int ct_lanczos_reorth_beta(ct_handle* h, int64_t n, double* w, const double* V, int64_t ldv, int nvec, int j,
-                           double beta_threshold, const int* skip);
 
 // SVD workspace (ct_svd.cu)
 size_t ct_svd_ws_bytes(int64_t m, int64_t n, int mode);

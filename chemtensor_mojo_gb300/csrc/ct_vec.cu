@@ -15,7 +15,7 @@ namespace {
 
 constexpr int RT = 256;
 
-__device__ __forceinline__ bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+__host__ __device__ __forceinline__ bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
 // ---- phase 1: per-block partial sums --------------------------------------
 // mode 0: sum x*y, mode 1: sum x*x
@@ -203,33 +203,76 @@ __global__ void lanczos_next_kernel(int64_t n, const double* w, double* vnext, c
         vnext[i] = w[i] * inv;
 }
 
-// reorthogonalisation: coeff[v] = <V[v], w>  (partials laid out [block][nvec]).  MD_VB
-// vectors per pass over w: w is read nvec / MD_VB times instead of nvec times, and
-// the MD_VB block sums share one reduction.
-constexpr int MD_VB = 8;
-__global__ void __launch_bounds__(RT) multidot_kernel(int64_t n, const double* w, const double* V, int64_t ldv,
-                                                      int nvec, double* partials, const int* skip) {
+// ---- reorthogonalisation pass of the Lanczos step: fused Gram-Schmidt kernels ----
+// After the reference recurrence w = H v_j - alpha_j v_j - beta_{j-1} v_{j-1}, w is
+// orthogonalised once more against the whole Krylov basis V[0..j] in two passes:
+//   A  c_k = <V_k, w> for k <= j                 (w read once per 16 basis vectors)
+//   B  w <- w - sum_k c_k V_k with |w|^2, beta_j = |w| and the breakdown test
+// and the next-vector kernel scales v_{j+1} = w / beta_j.  For v_j and v_{j-1}
+// this is Gram-Schmidt twice (the recurrence is the first pass), for the older
+// vectors, which carry only small components, once.  (Gram-Schmidt of H v_j
+// alone, with alpha_j and beta_{j-1} as two of its coefficients, reads w less
+// often but was measured to break the mixed form's sweeps -- energies below the
+// ground state on the Heisenberg chain, L = 20, chi = 128 -- while the FP64 form
+// and isolated solves were right; it is not used.)  Each reduction finishes in
+// the block that arrives last (fixed-order sums over the block partials, so the
+// result is reproducible) instead of a separate one-block launch.  Loads are 16
+// bytes (double2) when n is even and every vector is 16-byte aligned, which holds
+// for theta = Dl d^2 Dr with d even; otherwise the scalar path runs.
+constexpr int CGS_VB = 16;
+
+// true in every thread of the block that arrives last; partials written by the
+// other blocks are then visible to it (threadfence-reduction pattern)
+__device__ __forceinline__ bool last_block_arrived(unsigned* counter) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last) __threadfence();
+    return last;
+}
+
+// pass A: coeff[v] = <V[v], w> for v < nvec
+__global__ void __launch_bounds__(RT) cgs_dots_kernel(int64_t n, const double* __restrict__ w,
+                                                      const double* __restrict__ V, int64_t ldv, int nvec, int vec2,
+                                                      double* partials, unsigned* counter, double* coeff,
+                                                      const int* skip) {
     if (ct_skip(skip)) return;
-    __shared__ double sm[MD_VB][RT / 32];
-    const int64_t stride = (int64_t)gridDim.x * RT;
+    __shared__ double sm[CGS_VB][RT / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int v0 = 0; v0 < nvec; v0 += MD_VB) {
-        const int nv = min(MD_VB, nvec - v0);
-        double acc[MD_VB];
+    for (int v0 = 0; v0 < nvec; v0 += CGS_VB) {
+        const int nv = min(CGS_VB, nvec - v0);
+        double acc[CGS_VB];
 #pragma unroll
-        for (int k = 0; k < MD_VB; ++k) acc[k] = 0.0;
+        for (int k = 0; k < CGS_VB; ++k) acc[k] = 0.0;
         const double* x = V + (int64_t)v0 * ldv;
-        for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) {
-            const double wi = w[i];
+        if (vec2) {
+            const int64_t n2 = n / 2, stride = (int64_t)gridDim.x * RT;
+            const double2* w2 = reinterpret_cast<const double2*>(w);
+            for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n2; i += stride) {
+                const double2 wi = w2[i];
 #pragma unroll
-            for (int k = 0; k < MD_VB; ++k)
-                if (k < nv) acc[k] = fma(x[(int64_t)k * ldv + i], wi, acc[k]);
+                for (int k = 0; k < CGS_VB; ++k)
+                    if (k < nv) {
+                        const double2 a = reinterpret_cast<const double2*>(x + (int64_t)k * ldv)[i];
+                        acc[k] = fma(a.x, wi.x, fma(a.y, wi.y, acc[k]));
+                    }
+            }
+        } else {
+            const int64_t stride = (int64_t)gridDim.x * RT;
+            for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) {
+                const double wi = w[i];
+#pragma unroll
+                for (int k = 0; k < CGS_VB; ++k)
+                    if (k < nv) acc[k] = fma(x[(int64_t)k * ldv + i], wi, acc[k]);
+            }
         }
 #pragma unroll
-        for (int k = 0; k < MD_VB; ++k) acc[k] = ct_warp_sum(acc[k]);
+        for (int k = 0; k < CGS_VB; ++k) acc[k] = ct_warp_sum(acc[k]);
         if (lane == 0) {
 #pragma unroll
-            for (int k = 0; k < MD_VB; ++k) sm[k][wid] = acc[k];
+            for (int k = 0; k < CGS_VB; ++k) sm[k][wid] = acc[k];
         }
         __syncthreads();
         if (threadIdx.x < nv) {
@@ -239,36 +282,79 @@ __global__ void __launch_bounds__(RT) multidot_kernel(int64_t n, const double* w
         }
         __syncthreads();
     }
-}
-__global__ void __launch_bounds__(RT) multidot_finish(const double* partials, int np, int nvec, double* coeff,
-                                                      const int* skip) {
-    if (ct_skip(skip)) return;
-    __shared__ double sm[32];
-    for (int v = 0; v < nvec; ++v) {
-        double acc = 0.0;
-        for (int b = threadIdx.x; b < np; b += RT) acc += partials[(int64_t)b * nvec + v];
-        acc = ct_block_sum<RT>(acc, sm);
-        if (threadIdx.x == 0) coeff[v] = acc;
+    if (!last_block_arrived(counter)) return;
+    // last block: one warp per coefficient, lanes stride over the block partials
+    for (int v = wid; v < nvec; v += RT / 32) {
+        double r = 0.0;
+        for (int b = lane; b < (int)gridDim.x; b += 32) r += __ldcg(partials + (int64_t)b * nvec + v);
+        r = ct_warp_sum(r);
+        if (lane == 0) coeff[v] = r;
     }
+    if (threadIdx.x == 0) *counter = 0u;
 }
-__global__ void __launch_bounds__(RT) multiaxpy_norm_kernel(int64_t n, double* w, const double* V, int64_t ldv,
-                                                            int nvec, const double* coeff, double* partials,
-                                                            const int* skip) {
+
+// pass B: w -= sum_v coeff[v] V[v] with |w|^2; the last block forms beta_j = |w|
+// and makes the breakdown test beta < thr (dmrg.mojo:630-673)
+__global__ void __launch_bounds__(RT) cgs_update_kernel(int64_t n, double* __restrict__ w,
+                                                        const double* __restrict__ V, int64_t ldv, int nvec, int vec2,
+                                                        const double* coeff, double* partials, unsigned* counter,
+                                                        double* scalars, int* flags, int j, double thr,
+                                                        const int* skip) {
     if (ct_skip(skip)) return;
     __shared__ double sm[32];
     __shared__ double c[CT_MAX_KRYLOV];
     for (int v = threadIdx.x; v < nvec; v += RT) c[v] = coeff[v];
     __syncthreads();
-    double acc = 0.0;
+    double nn = 0.0;
     const int64_t stride = (int64_t)gridDim.x * RT;
-    for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) {
-        double x = w[i];
-        for (int v = 0; v < nvec; ++v) x -= c[v] * V[(int64_t)v * ldv + i];
-        w[i] = x;
-        acc = fma(x, x, acc);
+    if (vec2) {
+        const int64_t n2 = n / 2;
+        double2* w2 = reinterpret_cast<double2*>(w);
+        for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n2; i += stride) {
+            double2 x = w2[i];
+            int v = 0;
+            for (; v + 4 <= nvec; v += 4) {
+                const double2 a0 = reinterpret_cast<const double2*>(V + (int64_t)v * ldv)[i];
+                const double2 a1 = reinterpret_cast<const double2*>(V + (int64_t)(v + 1) * ldv)[i];
+                const double2 a2 = reinterpret_cast<const double2*>(V + (int64_t)(v + 2) * ldv)[i];
+                const double2 a3 = reinterpret_cast<const double2*>(V + (int64_t)(v + 3) * ldv)[i];
+                x.x -= c[v] * a0.x; x.y -= c[v] * a0.y;
+                x.x -= c[v + 1] * a1.x; x.y -= c[v + 1] * a1.y;
+                x.x -= c[v + 2] * a2.x; x.y -= c[v + 2] * a2.y;
+                x.x -= c[v + 3] * a3.x; x.y -= c[v + 3] * a3.y;
+            }
+            for (; v < nvec; ++v) {
+                const double2 a = reinterpret_cast<const double2*>(V + (int64_t)v * ldv)[i];
+                x.x -= c[v] * a.x;
+                x.y -= c[v] * a.y;
+            }
+            w2[i] = x;
+            nn = fma(x.x, x.x, fma(x.y, x.y, nn));
+        }
+    } else {
+        for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) {
+            double x = w[i];
+            for (int v = 0; v < nvec; ++v) x -= c[v] * V[(int64_t)v * ldv + i];
+            w[i] = x;
+            nn = fma(x, x, nn);
+        }
     }
-    acc = ct_block_sum<RT>(acc, sm);
-    if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+    nn = ct_block_sum<RT>(nn, sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = nn;
+    if (!last_block_arrived(counter)) return;
+    double s = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += RT) s += __ldcg(partials + b);
+    s = ct_block_sum<RT>(s, sm);
+    if (threadIdx.x == 0) {
+        const double b = sqrt(s);
+        if (b < thr) {
+            flags[FL_NUMITER] = j + 1;
+            flags[FL_STOP] = 1;
+        } else {
+            scalars[SC_BETA + j] = b;
+        }
+        *counter = 0u;
+    }
 }
 
 // Ritz vector: out = sum_{i < numiter} c_i V[i]
@@ -610,19 +696,33 @@ int ct_lanczos_update(ct_handle* h, int64_t n, double* w, const double* vj, cons
     return CT_OK;
 }
 
-// Full reorthogonalisation of w against V[0..nvec) followed by the beta
-// decision.  Runs after ct_lanczos_update (whose beta it overwrites).
-int ct_lanczos_reorth_beta(ct_handle* h, int64_t n, double* w, const double* V, int64_t ldv, int nvec, int j,
+// Reorthogonalisation pass of Lanczos step j (passes A and B above), after the
+// reference recurrence has updated w; beta_j (or the breakdown stop) goes to the
+// scalar slots.  The caller then forms v_{j+1} = w / beta_j.
+int ct_lanczos_reorth_pass(ct_handle* h, int64_t n, double* w, const double* V, int64_t ldv, int j,
                            double beta_threshold, const int* skip) {
-    if (nvec > CT_MAX_KRYLOV) return CT_ERR_UNSUPPORTED;
+    const int nvec = j + 1;
+    if (nvec > 64) return CT_ERR_UNSUPPORTED;
     int g = grid_for(h, n);
     if ((int64_t)g * nvec > CT_NPARTIALS) g = CT_NPARTIALS / nvec;
+    const int vec2 = ((n & 1) == 0 && (ldv & 1) == 0 && aligned16(w) && aligned16(V)) ? 1 : 0;
+    unsigned* counter = reinterpret_cast<unsigned*>(h->d_flags + FL_CNT);
     double* coeff = h->d_scalars + SC_MISC;
-    multidot_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, h->d_partials, skip); ct_note_launch();
-    multidot_finish<<<1, RT, 0, h->stream>>>(h->d_partials, g, nvec, coeff, skip); ct_note_launch();
-    multiaxpy_norm_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, coeff, h->d_partials, skip); ct_note_launch();
-    lanczos_beta_finish<<<1, RT, 0, h->stream>>>(h->d_partials, g, h->d_scalars, h->d_flags, j,
-                                                 beta_threshold, skip); ct_note_launch();
+    cgs_dots_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, vec2, h->d_partials, counter, coeff, skip);
+    ct_note_launch();
+    cgs_update_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, vec2, coeff, h->d_partials, counter,
+                                               h->d_scalars, h->d_flags, j, beta_threshold, skip); ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+// w -= alpha_j v_j + beta_{j-1} v_{j-1} without the norm (the reorthogonalisation
+// pass measures it afterwards)
+int ct_lanczos_update_nonorm(ct_handle* h, int64_t n, double* w, const double* vj, const double* vjm1, int j,
+                             const int* skip) {
+    const int g = grid_for(h, n);
+    lanczos_update_kernel<<<g, RT, 0, h->stream>>>(n, w, vj, vjm1, h->d_scalars, j, h->d_partials, skip);
+    ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }

@@ -208,6 +208,33 @@ def test_lanczos_matches_oracle(ctx, dims, max_rot):
     assert abs(abs(vv @ vr) - 1.0) < 1e-8
 
 
+@pytest.mark.parametrize("prec", ["fp64", "tf32x3"])
+@pytest.mark.parametrize("dims", [(12, 2, 9, 5, 5, 5), (6, 4, 5, 4, 4, 4), (40, 2, 33, 5, 5, 5)])
+def test_lanczos_reorth_matches_oracle(ctx, dims, prec):
+    """Reorthogonalised Lanczos (the reference recurrence, then one Gram-Schmidt pass of w
+    against the whole Krylov basis, fused into two kernels with last-block reductions)
+    against the oracle's recurrence followed by Gram-Schmidt.  FP64: alpha, beta and the
+    energy to 1e-9 / 1e-10; TF32x3 (tensor-core H_eff): the energy to 1e-6."""
+    ct = ct_mod()
+    th, L, R, W1, W2 = _lanczos_case(sum(dims) + 7, *dims)
+    tr = od.LanczosTrace()
+    E_ref, v_ref = od.lanczos_two_site_optimize(th, L, R, W1, W2, 20, 1e-10, eig="exact", trace=tr, reorth=True)
+    info = ct.dmrg.LanczosInfo(0, [], [])
+    E, v = ct.lanczos_two_site_optimize(dt(ctx, th), dt(ctx, L), dt(ctx, R), ct.MPOSite(dt(ctx, W1)),
+                                        ct.MPOSite(dt(ctx, W2)), ctx, max_iter=20, tol=1e-10, prec=prec,
+                                        max_rotations=0, reorth=True, info=info)
+    assert info.numiter == tr.numiter
+    if prec == "fp64":
+        scale = np.abs(tr.alpha).max()
+        assert np.allclose(info.alpha, tr.alpha, rtol=1e-9, atol=1e-9 * scale)
+        assert np.allclose(info.beta, tr.beta, rtol=1e-9, atol=1e-9 * scale)
+        assert abs(E - E_ref) <= 1e-10 * max(1.0, abs(E_ref))
+        vv = v.to_numpy().reshape(-1)
+        assert abs(abs(vv @ v_ref.reshape(-1)) - 1.0) < 1e-8
+    else:
+        assert abs(E - E_ref) <= 1e-6 * max(1.0, abs(E_ref))
+
+
 def test_lanczos_breakdown_matches_oracle(ctx):
     """Rank-deficient H_eff: the Krylov space closes early (beta below 100 n eps)."""
     ct = ct_mod()
