@@ -611,20 +611,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // out too small by ~6e-9 per unit of K (-3e-5 relative at K = 5120).  This
 // variant bounds the number of adds into any accumulator: each tile's K range is
 // cut into chunks of `kc` k-blocks (kc * 32 of K); every chunk starts a fresh
-// TMEM accumulator, alternating between two BN-column buffers, and the epilogue
+// TMEM accumulator, cycling through 512 / BN BN-column buffers, and the epilogue
 // warps add the chunks in FP32 registers with round-to-nearest, whose errors
 // have no sign preference.  The bias left is that of one chunk, kc times that of
 // one 32-wide k-block (~1.8e-7).
 //   * one CTA per SM walks tiles c, c + G, ... (no stream-K);
-//   * warps: 0 TMA producer, 1 TMEM allocator + MMA issuer, 2..9 epilogue;
-//     epilogue warp w reads TMEM lane quadrant w % 4 (the quadrant a warp may
-//     access) and column half (w - 2) / 4 of the tile, holding BN / 2 FP32
-//     running sums per thread;
+//   * warps: 0 TMA producer, 1 TMEM allocator + MMA issuer, then 4 EPW epilogue
+//     warps; epilogue warp w reads TMEM lane quadrant w % 4 (the quadrant a warp
+//     may access) and column group (w - 2) / 4 of the tile, holding BN / EPW
+//     FP32 running sums per thread.  EPW = 4 for the 128 x 128 tile (a chunk of
+//     64 of K is ~2000 cycles of MMAs there, so the per-chunk epilogue must be
+//     short), 2 for the 128 x 256 tile (its 128 sums per thread leave no room
+//     for more warps in the register file);
 //   * acc_full[b] is committed by the MMA thread after a chunk's last MMA,
-//     acc_empty[b] released by the eight epilogue warps once the chunk is in
-//     registers, so the MMAs of chunk i + 1 run while chunk i is read; a tile's
-//     stores overlap the next tile's first two chunks.
-constexpr int TC_THREADS_CH = 320;
+//     acc_empty[b] released by the epilogue warps once the chunk is in
+//     registers, so the MMAs of the next chunks run while chunk i is read (with
+//     four buffers the MMA thread is three chunks ahead, which hides the
+//     commit -> epilogue -> release latency of a short chunk); a tile's stores
+//     overlap the next tile's first chunks.
+__host__ __device__ constexpr int tc_chunk_epw(int BN) { return BN >= 256 ? 2 : 4; }
+__host__ __device__ constexpr int tc_chunk_threads(int BN) { return 32 * (2 + 4 * tc_chunk_epw(BN)); }
 
 __device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t (&r)[8]) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -633,24 +639,26 @@ __device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t (&r)[8]
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// Registers: each SM sub-partition holds 16K of them and 10 warps put 3 on some
-// sub-partitions, so a thread gets at most 168; the 128 x 256 tile's 128 running
-// sums per thread fit when TMEM is read 8 columns at a time.
+// Registers: each SM sub-partition holds 16K of them; 10 warps put 3 on some
+// sub-partitions (168 per thread), 18 warps put 5 (96 per thread, enough for 32
+// sums and 32 loaded columns).
 template <int BN, int STAGES>
-__global__ void __launch_bounds__(TC_THREADS_CH, 1)
+__global__ void __launch_bounds__(tc_chunk_threads(BN), 1)
     tc_gemm_chunk_kernel(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                          const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl, int M,
                          int N, int Kpad, int kc, TcEpi epi, const int* skip, int* status) {
     using L = TcSmem<BN, STAGES>;
-    constexpr int HC = BN / 2;   // columns per epilogue warp
+    constexpr int EPW = tc_chunk_epw(BN);
+    constexpr int HC = BN / EPW;   // columns per epilogue warp
+    constexpr int NB = 512 / BN;   // chunk accumulators in TMEM (all 512 columns)
     if (ct_skip(skip)) return;
     extern __shared__ uint8_t tc_smem_raw[];
     uint8_t* smem = tc_smem_raw + ((1024u - (smem_u32(tc_smem_raw) & 1023u)) & 1023u);
     uint64_t* full = (uint64_t*)(smem + L::TILE_BYTES);
     uint64_t* empty = full + STAGES;
     uint64_t* acc_full = empty + STAGES;
-    uint64_t* acc_empty = acc_full + 2;
-    uint32_t* tmem_slot = (uint32_t*)(acc_empty + 2);
+    uint64_t* acc_empty = acc_full + NB;
+    uint32_t* tmem_slot = (uint32_t*)(acc_empty + NB);
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -664,16 +672,16 @@ __global__ void __launch_bounds__(TC_THREADS_CH, 1)
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < NB; ++b) {
             mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], 8);
+            mbar_init(&acc_empty[b], 4 * EPW);
         }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"((uint32_t)(2 * BN))
+                     "r"((uint32_t)(NB * BN))
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -714,7 +722,7 @@ __global__ void __launch_bounds__(TC_THREADS_CH, 1)
             bool ok = true;
             for (int t = c; t < tiles && ok; t += G) {
                 for (int kb0 = 0; kb0 < nkb && ok; kb0 += kc, ++gc) {
-                    const int b = gc & 1, u = gc >> 1;
+                    const int b = gc % NB, u = gc / NB;
                     if (u > 0 && !mbar_wait(&acc_empty[b], (uint32_t)((u - 1) & 1), abort_flag)) {
                         *abort_flag = 1;
                         ct_set_status(status, CT_ERR_CUDA);
@@ -754,7 +762,7 @@ __global__ void __launch_bounds__(TC_THREADS_CH, 1)
         }
     } else {
         const int q = warp & 3;              // TMEM lane quadrant of this warp
-        const int hf = (warp - 2) >> 2;      // column half of the tile
+        const int hf = (warp - 2) >> 2;      // column group of the tile
         const int row = q * 32 + lane;
         float sum[HC];
         int gc = 0;
@@ -763,7 +771,7 @@ __global__ void __launch_bounds__(TC_THREADS_CH, 1)
 #pragma unroll
             for (int j = 0; j < HC; ++j) sum[j] = 0.f;
             for (int kb0 = 0; kb0 < nkb; kb0 += kc, ++gc) {
-                const int b = gc & 1, u = gc >> 1;
+                const int b = gc % NB, u = gc / NB;
                 if (!mbar_wait(&acc_full[b], (uint32_t)(u & 1), abort_flag)) {
                     *abort_flag = 1;
                     ct_set_status(status, CT_ERR_CUDA);
@@ -773,13 +781,19 @@ __global__ void __launch_bounds__(TC_THREADS_CH, 1)
                 __syncwarp();
                 tc_fence_after();
                 const uint32_t tq = tmem + (uint32_t)(b * BN + hf * HC) + ((uint32_t)(q * 32) << 16);
+                // LB columns per wait: several TMEM loads in flight before one
+                // tcgen05.wait::ld (fewer for the wide tile, whose 128 sums leave
+                // room for 32 more registers only)
+                constexpr int LB = HC >= 128 ? 32 : HC;
 #pragma unroll
-                for (int cc = 0; cc < HC; cc += 8) {
-                    uint32_t r[8];
-                    tmem_ld8_nowait(tq + (uint32_t)cc, r);
+                for (int cc = 0; cc < HC; cc += LB) {
+                    uint32_t r[LB];
+#pragma unroll
+                    for (int q8 = 0; q8 < LB; q8 += 8)
+                        tmem_ld8_nowait(tq + (uint32_t)(cc + q8), *reinterpret_cast<uint32_t(*)[8]>(&r[q8]));
                     tmem_wait_ld();
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) sum[cc + j] += __uint_as_float(r[j]);
+                    for (int j = 0; j < LB; ++j) sum[cc + j] += __uint_as_float(r[j]);
                 }
                 tc_fence_before();
                 __syncwarp();
@@ -838,7 +852,7 @@ __global__ void __launch_bounds__(TC_THREADS_CH, 1)
     __syncthreads();
     if (warp == 1) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)(2 * BN))
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)(NB * BN))
                      : "memory");
     }
 }
@@ -1143,7 +1157,7 @@ int tc_gemm_run(ct_handle* h, const SplitOperand& A, const SplitOperand& B, int6
     const int kc = tc_kchunk();
     if (tc_use_persistent() && kc > 0 && !tc_use_stream_k()) {
         const int64_t grid = tiles < h->num_sms ? tiles : h->num_sms;
-        tc_gemm_chunk_kernel<BN, STAGES><<<(unsigned)grid, TC_THREADS_CH, L::TOTAL, h->stream>>>(
+        tc_gemm_chunk_kernel<BN, STAGES><<<(unsigned)grid, tc_chunk_threads(BN), L::TOTAL, h->stream>>>(
             ta_h, ta_l, tb_h, tb_l, (int)M, (int)N, (int)A.ldk, kc, epi, skip, h->d_status);
         ct_note_launch();
     } else if (tc_use_persistent()) {

@@ -233,6 +233,35 @@ __device__ __forceinline__ bool last_block_arrived(unsigned* counter) {
     return last;
 }
 
+// acc[k] += <V[k], w> over this thread's elements, k < NV.  NV is a template
+// parameter so exactly NV multiply-adds issue per element: FP64 issues at 1/64 of
+// the FP32 rate on this part, and a predicated-off FMA of a runtime-bounded loop
+// still occupies the FP64 pipe (measured: a 16-wide group did the same FP64 work
+// for one live vector as for sixteen).
+template <int NV>
+__device__ __forceinline__ void cgs_dots_group(int64_t n, const double* __restrict__ w, const double* __restrict__ x,
+                                               int64_t ldv, int vec2, double (&acc)[CGS_VB]) {
+    const int64_t stride = (int64_t)gridDim.x * RT;
+    if (vec2) {
+        const int64_t n2 = n / 2;
+        const double2* w2 = reinterpret_cast<const double2*>(w);
+        for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n2; i += stride) {
+            const double2 wi = w2[i];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                const double2 a = reinterpret_cast<const double2*>(x + (int64_t)k * ldv)[i];
+                acc[k] = fma(a.x, wi.x, fma(a.y, wi.y, acc[k]));
+            }
+        }
+    } else {
+        for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) {
+            const double wi = w[i];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) acc[k] = fma(x[(int64_t)k * ldv + i], wi, acc[k]);
+        }
+    }
+}
+
 // pass A: coeff[v] = <V[v], w> for v < nvec
 __global__ void __launch_bounds__(RT) cgs_dots_kernel(int64_t n, const double* __restrict__ w,
                                                       const double* __restrict__ V, int64_t ldv, int nvec, int vec2,
@@ -247,32 +276,22 @@ __global__ void __launch_bounds__(RT) cgs_dots_kernel(int64_t n, const double* _
 #pragma unroll
         for (int k = 0; k < CGS_VB; ++k) acc[k] = 0.0;
         const double* x = V + (int64_t)v0 * ldv;
-        if (vec2) {
-            const int64_t n2 = n / 2, stride = (int64_t)gridDim.x * RT;
-            const double2* w2 = reinterpret_cast<const double2*>(w);
-            for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n2; i += stride) {
-                const double2 wi = w2[i];
-#pragma unroll
-                for (int k = 0; k < CGS_VB; ++k)
-                    if (k < nv) {
-                        const double2 a = reinterpret_cast<const double2*>(x + (int64_t)k * ldv)[i];
-                        acc[k] = fma(a.x, wi.x, fma(a.y, wi.y, acc[k]));
-                    }
-            }
-        } else {
-            const int64_t stride = (int64_t)gridDim.x * RT;
-            for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) {
-                const double wi = w[i];
-#pragma unroll
-                for (int k = 0; k < CGS_VB; ++k)
-                    if (k < nv) acc[k] = fma(x[(int64_t)k * ldv + i], wi, acc[k]);
-            }
+        switch (nv) {
+#define CT_CGS_CASE(K) \
+    case K: cgs_dots_group<K>(n, w, x, ldv, vec2, acc); break;
+            CT_CGS_CASE(1) CT_CGS_CASE(2) CT_CGS_CASE(3) CT_CGS_CASE(4) CT_CGS_CASE(5) CT_CGS_CASE(6)
+            CT_CGS_CASE(7) CT_CGS_CASE(8) CT_CGS_CASE(9) CT_CGS_CASE(10) CT_CGS_CASE(11) CT_CGS_CASE(12)
+            CT_CGS_CASE(13) CT_CGS_CASE(14) CT_CGS_CASE(15) CT_CGS_CASE(16)
+#undef CT_CGS_CASE
+            default: break;
         }
 #pragma unroll
-        for (int k = 0; k < CGS_VB; ++k) acc[k] = ct_warp_sum(acc[k]);
+        for (int k = 0; k < CGS_VB; ++k)
+            if (k < nv) acc[k] = ct_warp_sum(acc[k]);
         if (lane == 0) {
 #pragma unroll
-            for (int k = 0; k < CGS_VB; ++k) sm[k][wid] = acc[k];
+            for (int k = 0; k < CGS_VB; ++k)
+                if (k < nv) sm[k][wid] = acc[k];
         }
         __syncthreads();
         if (threadIdx.x < nv) {
