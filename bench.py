@@ -629,8 +629,27 @@ def cpu_threads() -> int:
     return os.cpu_count() or 1
 
 
+def cpu_sweep_seconds(L, chi, seed=3):
+    """One full sweep of the CPU FP64 oracle (converged eigensolve, eps_trunc = 0) on the
+    Heisenberg chain at chi_max = chi, from the seeded random MPS right-normalised with
+    bond dimensions min(2^k, 2^(L-k), chi): every bond runs at its full size."""
+    from oracle import dmrg as od
+    from oracle import hamiltonians as oh
+    from oracle import rng as orng
+    mpo = oh.spin_half_xxz(L, 1.0)
+    sites, _ = orng.create_random_mps_c_compatible(L, D_PHYS, chi, seed)
+    mps = od.right_normalize(sites)
+    t0 = time.perf_counter()
+    od.dmrg_two_site(mpo, mps, od.DMRGParams(1, chi, EPS, LANCZOS, 1e-10, 0.0), eig="exact")
+    return time.perf_counter() - t0
+
+
 def reference_arm(args, rank):
-    """CPU oracle port of the reference path: sampled centre-bond updates, extrapolated."""
+    """CPU oracle port of the reference path: sampled centre-bond updates, extrapolated.
+
+    The extrapolation (centre-bond local update x the sweep's FLOP weight) is checked
+    once per run at chi = 256, where a whole CPU sweep is affordable: the measured
+    sweep and its extrapolation are both reported."""
     if rank != 0:
         return
     chi = args.chi
@@ -639,6 +658,13 @@ def reference_arm(args, rank):
     times = [cpu_local_update_seconds(chi, seed=s) for s in range(args.steps)]
     weight = sweep_flop_weight(args.L, chi)
     per_sweep = float(np.mean(times)) * weight
+    chk = min(chi, 256)
+    t_centre = float(np.mean([cpu_local_update_seconds(chk, seed=s) for s in range(3)]))
+    t_sweep = cpu_sweep_seconds(args.L, chk)
+    extrapolated = t_centre * sweep_flop_weight(args.L, chk)
+    check = {"chi_max": chk, "measured_sweep_s": t_sweep, "extrapolated_sweep_s": extrapolated,
+             "measured_over_extrapolated": t_sweep / extrapolated,
+             "note": "one whole CPU sweep vs 3 centre-bond local updates x the FLOP weight"}
     line = {
         "impl": "reference", "metric": METRIC, "value": per_sweep, "unit": "s/sweep", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_sweep * 1e3, "higher_is_better": False,
@@ -649,6 +675,7 @@ def reference_arm(args, rank):
                          "sample": f"{args.steps} centre-bond local updates at chi={chi}, FLOP-weighted x{weight:.1f}"
                                    " to a sweep (extrapolated)"},
         "e2e": {"value": per_sweep, "unit": "s/sweep", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_extrapolation_check": check,
     }
     print(json.dumps(line), flush=True)
 
