@@ -363,6 +363,7 @@ def schedule_run(ctx, ct, mpo, arrays, schedule, prec):
     energy, seconds (the call's wall clock without the Rayleigh contraction), splits."""
     mps = ct.mps_right_normalize(ctx, ct.mps_from_arrays(ctx, arrays))
     out = []
+    st = None
     for k, c in enumerate(schedule):
         st = ct.DMRGStats()
         E, mps = ct.dmrg_two_site(ctx, mpo, mps, ct.DMRGParams(
@@ -373,7 +374,7 @@ def schedule_run(ctx, ct, mpo, arrays, schedule, prec):
                     "seconds_lanczos": st.seconds_lanczos, "seconds_split": st.seconds_svd,
                     "seconds_env": st.seconds_env, "max_discarded": st.max_discarded,
                     "subspace_splits": st.subspace_splits, "exact_splits": st.exact_splits})
-    return out
+    return out, mps, list(st.discarded)
 
 
 def fp64_ref_mode(args):
@@ -394,7 +395,9 @@ def fp64_ref_mode(args):
     mpo = ct.create_spin_half_xxz_mpo(ctx, L, 1.0)
     arrays, _ = ct.random_mps_c_compatible_arrays(L, D_PHYS, RAMP[0], ACC_SEED)
     schedule = [64, 256] + [args.chi] * max(args.steps, 1)
-    runs = {pr: schedule_run(ctx, ct, mpo, arrays, schedule, pr) for pr in args.forms.split(",")}
+    runs, states, disc = {}, {}, {}
+    for pr in args.forms.split(","):
+        runs[pr], states[pr], disc[pr] = schedule_run(ctx, ct, mpo, arrays, schedule, pr)
     line = {"metric": "FP64 vs mixed two-site sweep at chi_max", "unit": "s/sweep", "data": "synthetic",
             "config": {"workload": f"heisenberg_xxz L={L} d=2 D=5 seed={ACC_SEED} chi schedule "
                                    f"{','.join(map(str, schedule))} lanczos={LANCZOS} eps={EPS}",
@@ -409,6 +412,20 @@ def fp64_ref_mode(args):
                                         for x, y in zip(a, b)]
         line["dE_over_E_at_chi"] = max(line["dE_over_E_each_sweep"][k] for k in at)
         line["speedup_mixed_vs_fp64_at_chi"] = line["fp64_s_per_sweep_at_chi"] / line["tf32x3_s_per_sweep_at_chi"]
+        # Schmidt spectra of every bond of the two final states (FP64 device SVD) and the
+        # discarded weights of the last sweep's 2(L-1) splits
+        sa, sb = ct.mps_schmidt_values(states["tf32x3"], ctx), ct.mps_schmidt_values(states["fp64"], ctx)
+        w_err, top_rel = 0.0, 0.0
+        for x, y in zip(sa, sb):
+            n = min(len(x), len(y))
+            w_err = max(w_err, float(np.max(np.abs(x[:n] ** 2 - y[:n] ** 2))))   # weights of a normalised state
+            top_rel = max(top_rel, float(np.max(np.abs(x[:8] - y[:8]) / y[:8])))
+        da, db = np.array(disc["tf32x3"]), np.array(disc["fp64"])
+        line["spectrum_check"] = {
+            "bonds": len(sa), "max_abs_weight_diff": w_err, "max_rel_diff_top8_schmidt_values": top_rel,
+            "last_sweep_discarded_max_abs_diff": float(np.max(np.abs(da - db))) if len(da) == len(db) else None,
+            "last_sweep_discarded_max": {"tf32x3": float(da.max()), "fp64": float(db.max())},
+            "note": "final MPS of each form; weights s^2 of the normalised state at every bond"}
     print(json.dumps(line), flush=True)
     if args.out:
         with open(args.out, "w") as f:

@@ -24,7 +24,7 @@ from .environments import (apply_mpo, build_right_environments, expectation_valu
                            update_right_environment, variance)
 from . import dmrg_utils  # noqa: F401
 from .results import (DMRGJsonParams, DMRGReference, dmrg_results_to_json_string, load_dmrg_reference,  # noqa
-                      mps_bond_entropies, print_dmrg_reference_info, save_dmrg_results_to_json)
+                      mps_bond_entropies, mps_schmidt_values, print_dmrg_reference_info, save_dmrg_results_to_json)
 from .dmrg import (DMRGParams, DMRGStats, DMRGWorkspace, apply_two_site_heff, build_two_site_theta,  # noqa
                    dmrg_local_update_two_site, dmrg_two_site, lanczos_two_site_optimize, split_two_site_theta_svd)
 

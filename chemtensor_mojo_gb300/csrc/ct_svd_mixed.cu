@@ -13,9 +13,10 @@
 //      Newton-Schulz steps  Q <- Q - 1/2 (Q Q^T - I) Q  with the Gram matrix in
 //      FP64 (the canonical factor must be orthonormal to FP64 accuracy: its
 //      defect enters the next H_eff as a metric error, first order in energy);
-//   3. the centre factor (S Vt or U S) is the projection of theta on that basis
-//      on the tensor cores (TF32x3): an error there only perturbs the next
-//      Lanczos start vector;
+//   3. the centre factor (S Vt or U S) is the projection of theta on that basis,
+//      on the tensor cores (TF32x3) when chi = min(k, chi_max) is fixed -- an
+//      error there only perturbs the next Lanczos start vector -- and in FP64
+//      when eps_trunc can decide chi or the spectrum is returned;
 //   4. singular values = FP64 norms of the projected rows/columns, descending;
 //      chi by the reference rule with the total weight |theta|^2 in FP64.
 #include "ct_ops.cuh"
@@ -240,15 +241,42 @@ int ct_svd_mixed_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_
         ar.off = mark;
         CT_TRY(ct_tc_gemm(h, ar, 0, 0, c, nvec, c, -0.5, G, c, Qt, nvec, 1.0, Qt, nvec));
     }
-    // 3. centre factor on the tensor cores
+    // 3. centre factor: on the tensor cores when only the kept subspace matters
+    // (chi = min(k, chi_max)); in FP64 when eps_trunc can decide chi or the caller
+    // wants the spectrum.  The basis is FP64-orthonormal and within ~1e-6 (angle)
+    // of the singular subspace, so the weights it captures -- and the projected
+    // norms -- are then exact to second order in that angle (~1e-12 of |theta|^2),
+    // which makes the truncation rule's tail sums and the kept singular values
+    // FP64-accurate.
     ar.off = mark;
+    const bool fp64_proj = eps_trunc > 0.0 || Sout != nullptr;
     if (mode == 0) {
         // Pj[c][n] = Qt[c][m] . M[m][n]
-        CT_TRY(ct_tc_gemm(h, ar, 0, 0, c, n, m, 1.0, Qt, nvec, M, n, 0.0, Pj, n));
+        if (fp64_proj) {
+            GemmDesc g{};
+            g.M = c; g.N = n; g.K = m;
+            g.A = Qt; g.sAm = nvec; g.sAk = 1;
+            g.B = M; g.sBk = n; g.sBn = 1;
+            g.C = Pj; g.sCm = n; g.sCn = 1;
+            g.alpha = 1.0; g.beta = 0.0; g.nb1 = 1; g.nb0 = 1;
+            CT_TRY(ct_gemm_f64_launch(h, g));
+        } else {
+            CT_TRY(ct_tc_gemm(h, ar, 0, 0, c, n, m, 1.0, Qt, nvec, M, n, 0.0, Pj, n));
+        }
         proj_norms_kernel<<<(unsigned)ct_cdiv(c * 32, 256), 256, 0, h->stream>>>(Pj, c, n, 1, sig); ct_note_launch();
     } else {
         // Pj[m][c] = M[m][n] . Qt[c][n]^T
-        CT_TRY(ct_tc_gemm(h, ar, 0, 1, m, c, n, 1.0, M, n, Qt, nvec, 0.0, Pj, c));
+        if (fp64_proj) {
+            GemmDesc g{};
+            g.M = m; g.N = c; g.K = n;
+            g.A = M; g.sAm = n; g.sAk = 1;
+            g.B = Qt; g.sBk = 1; g.sBn = nvec;
+            g.C = Pj; g.sCm = c; g.sCn = 1;
+            g.alpha = 1.0; g.beta = 0.0; g.nb1 = 1; g.nb0 = 1;
+            CT_TRY(ct_gemm_f64_launch(h, g));
+        } else {
+            CT_TRY(ct_tc_gemm(h, ar, 0, 1, m, c, n, 1.0, M, n, Qt, nvec, 0.0, Pj, c));
+        }
         proj_norms_kernel<<<(unsigned)ct_cdiv(c * 32, 256), 256, 0, h->stream>>>(Pj, c, m, 0, sig); ct_note_launch();
     }
     rank_desc_kernel<<<(unsigned)ct_cdiv(c, 256), 256, 0, h->stream>>>(sig, c, perm); ct_note_launch();

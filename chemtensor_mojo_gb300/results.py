@@ -138,14 +138,20 @@ def entropy_from_schmidt(s: Sequence[float]) -> float:
 
 
 def mps_bond_entropies(mps: MatrixProductState, ctx: DeviceContext | None = None) -> List[float]:
-    """Entropies of the L-1 inner bonds.  Right-normalise, then sweep left to right:
-    M_i = C_{i-1} A_i = U S V^T (device Jacobi SVD, no truncation), S are the
-    Schmidt values of bond i+1 and C_i = U^T M_i carries S V^T to the next site."""
+    """Entropies of the L-1 inner bonds (from mps_schmidt_values)."""
+    return [entropy_from_schmidt(s.tolist()) for s in mps_schmidt_values(mps, ctx)]
+
+
+def mps_schmidt_values(mps: MatrixProductState, ctx: DeviceContext | None = None) -> List["np.ndarray"]:
+    """Schmidt values of the L-1 inner bonds of the normalised state, descending, as NumPy
+    arrays.  Right-normalise, then sweep left to right: M_i = C_{i-1} A_i = U S V^T
+    (FP64 device Jacobi SVD, no truncation), S are the Schmidt values of bond i+1 and
+    C_i = U^T M_i carries S V^T to the next site."""
     ctx = ctx or get_context()
     psi = mps_right_normalize(ctx, mps)
     N = psi.num_sites()
     d = psi.physical_dim
-    out: List[float] = []
+    out: List = []
     carry: DenseTensor | None = None
     for i in range(N - 1):
         A = psi.sites[i].tensor
@@ -158,7 +164,7 @@ def mps_bond_entropies(mps: MatrixProductState, ctx: DeviceContext | None = None
             dense_tensor_dot(M, carry, A.reshape([Dl, d * Dr]), ctx)
             M = M.reshape([k * d, Dr])
         U, S, Vt, c = dense_tensor_svd_trunc(M, ctx, chi_max=1 << 30, eps_trunc=0.0)
-        out.append(entropy_from_schmidt(S.to_numpy().reshape(-1).tolist()))
+        out.append(S.to_numpy().reshape(-1).copy())
         carry = create_dense_tensor(ctx, [c, Dr])
         dense_tensor_dot(carry, U, M, ctx, ndim_mult=1, axrange_A=True, axrange_B=True)
     return out
