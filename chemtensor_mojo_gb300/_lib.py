@@ -53,7 +53,7 @@ class ct_dmrg_stats(C.Structure):
                 ("energy_rayleigh", C.c_double), ("subspace_splits", C.c_int64), ("exact_splits", C.c_int64),
                 ("seconds_subspace", C.c_double), ("cold_splits", C.c_int64),
                 ("completed_rows", C.c_int64), ("seconds_rayleigh", C.c_double),
-                ("stale_retries", C.c_int64)]
+                ("stale_retries", C.c_int64), ("fp64_handovers", C.c_int64)]
 
 
 P = C.c_void_p

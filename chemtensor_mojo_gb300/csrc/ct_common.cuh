@@ -45,6 +45,7 @@ struct ct_handle {
     // diagnostics: Jacobi sweeps of the last SVD split, and the running total
     int last_svd_sweeps = 0;
     int64_t total_svd_sweeps = 0;
+    int64_t mixed_fp64_splits = 0;   // mixed splits handed to the FP64 Jacobi (ct_svd_mixed.cu)
     // FP64 GEMM split-K partial sums (grown on demand, freed by ct_destroy)
     double* splitk = nullptr;
     size_t splitk_cap = 0;   // doubles

@@ -142,6 +142,7 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
     uint64_t cold_seq = 0;   // seeds of the random start rows of first-visit splits
     ct_dmrg_stats st{};
     std::vector<double> disc_all;
+    const int64_t handovers0 = h->mixed_fp64_splits;
 
     // build_right_environments (environments.mojo:420-472)
     CT_TRY(ct_identity_env(h, Renv[N].p, mpo_dims[N], bd[N]));
@@ -460,6 +461,7 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
     if (discarded_host)
         for (size_t k = 0; k < disc_all.size(); ++k) discarded_host[k] = disc_all[k];
     st.seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    st.fp64_handovers = h->mixed_fp64_splits - handovers0;
     if (stats_host) *stats_host = st;
     return CT_OK;
 }

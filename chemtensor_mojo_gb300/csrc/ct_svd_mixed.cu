@@ -19,6 +19,16 @@
 //      when eps_trunc can decide chi or the spectrum is returned;
 //   4. singular values = FP64 norms of the projected rows/columns, descending;
 //      chi by the reference rule with the total weight |theta|^2 in FP64.
+//
+// The projected weights are exact to second order in the FP32 Jacobi's angles
+// (~1e-12 of |theta|^2 measured), which decides chi exactly only when the cut is
+// far from eps_trunc.  So the split is handed to the FP64 Jacobi of ct_svd.cu
+// (QR-preconditioned, ~11 sweeps) when the caller wants the spectrum, and when
+// eps_trunc > 0 and the projected tail at chi = min(k, chi_max) is below
+// 2 eps_trunc + 1e-9 of |theta|^2: then eps_trunc may decide chi, and the FP64
+// split gives the reference's chi, spectrum and discarded weight.  Otherwise
+// the exact tail exceeds eps_trunc as well, chi = min(k, chi_max) is the
+// reference's, and the reported weights are those of the split returned.
 #include "ct_ops.cuh"
 #include "ct_jacobi_coop.cuh"
 
@@ -186,6 +196,8 @@ int ct_svd_mixed_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_
         out->chi = 0;
         return CT_OK;
     }
+    if (Sout) return ct_svd_run(h, ar, M, m, n, chi_max, eps_trunc, mode, Aout, Bout, Sout, out);
+    const size_t entry = ar.off;
     float* X = ar.take<float>(nvec * len);
     float* Q = ar.take<float>(nvec * nvec);
     double* sig32 = ar.take<double>(nvec);
@@ -242,14 +254,12 @@ int ct_svd_mixed_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_
         CT_TRY(ct_tc_gemm(h, ar, 0, 0, c, nvec, c, -0.5, G, c, Qt, nvec, 1.0, Qt, nvec));
     }
     // 3. centre factor: on the tensor cores when only the kept subspace matters
-    // (chi = min(k, chi_max)); in FP64 when eps_trunc can decide chi or the caller
-    // wants the spectrum.  The basis is FP64-orthonormal and within ~1e-6 (angle)
-    // of the singular subspace, so the weights it captures -- and the projected
-    // norms -- are then exact to second order in that angle (~1e-12 of |theta|^2),
-    // which makes the truncation rule's tail sums and the kept singular values
-    // FP64-accurate.
+    // (eps_trunc = 0: chi = min(k, chi_max)); in FP64 when eps_trunc > 0, where
+    // the tail sums decide whether the FP64 split takes over.  The basis is
+    // FP64-orthonormal and within ~1e-6 (angle) of the singular subspace, so the
+    // weights it captures are exact to second order in that angle.
     ar.off = mark;
-    const bool fp64_proj = eps_trunc > 0.0 || Sout != nullptr;
+    const bool fp64_proj = eps_trunc > 0.0;
     if (mode == 0) {
         // Pj[c][n] = Qt[c][m] . M[m][n]
         if (fp64_proj) {
@@ -287,6 +297,12 @@ int ct_svd_mixed_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_
     CT_CUDA(h, cudaMemcpyAsync(&chi, h->d_flags + FL_CHI, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     CT_CUDA(h, cudaMemcpyAsync(sums, h->d_scalars + SC_TMP0, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CT_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (eps_trunc > 0.0 && sums[0] > 0.0 &&
+        (chi < c || (sums[0] - sums[1]) / sums[0] <= 2.0 * eps_trunc + 1e-9)) {
+        ar.off = entry;
+        h->mixed_fp64_splits++;
+        return ct_svd_run(h, ar, M, m, n, chi_max, eps_trunc, mode, Aout, Bout, Sout, out);
+    }
     out->chi = chi;
     out->sum_s2_all = sums[0];
     out->sum_s2_kept = sums[1];
@@ -299,8 +315,13 @@ int ct_svd_mixed_run(ct_handle* h, Arena& ar, const double* M, int64_t m, int64_
 }
 
 size_t ct_split_ws_bytes(int prec, int64_t m, int64_t n, int64_t chi_max, int mode) {
-    if (prec == CT_PREC_TF32X3 && !ct_svd_is_small(m, n, mode)) return ct_svd_mixed_ws_bytes(m, n, chi_max, mode);
-    return ct_svd_ws_bytes(m, n, mode);
+    const size_t exact = ct_svd_ws_bytes(m, n, mode);
+    if (prec == CT_PREC_TF32X3 && !ct_svd_is_small(m, n, mode)) {
+        // the mixed split may hand over to the FP64 one (same arena, from its start)
+        const size_t mixed = ct_svd_mixed_ws_bytes(m, n, chi_max, mode);
+        return mixed > exact ? mixed : exact;
+    }
+    return exact;
 }
 
 int ct_split_run(ct_handle* h, Arena& ar, int prec, const double* M, int64_t m, int64_t n, int64_t chi_max,

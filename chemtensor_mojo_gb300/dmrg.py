@@ -76,6 +76,7 @@ class DMRGStats:
     completed_rows: int = 0
     seconds_rayleigh: float = 0.0
     stale_retries: int = 0
+    fp64_handovers: int = 0
     sweep_energies: List[float] = field(default_factory=list)
     discarded: List[float] = field(default_factory=list)
 
@@ -267,7 +268,7 @@ def dmrg_two_site(ctx: DeviceContext | None, mpo: MatrixProductOperator, mps: Ma
         for f in ("seconds_total", "seconds_lanczos", "seconds_svd", "seconds_env", "heff_flops", "env_flops",
                   "heff_applies", "local_updates", "max_discarded", "energy_rayleigh", "subspace_splits",
                   "exact_splits", "seconds_subspace", "cold_splits", "completed_rows",
-                  "seconds_rayleigh", "stale_retries"):
+                  "seconds_rayleigh", "stale_retries", "fp64_handovers"):
             setattr(stats, f, getattr(st, f))
         stats.sweep_energies = list(sweeps)[:done.value]
         stats.discarded = list(disc)[:done.value * 2 * (N - 1)]

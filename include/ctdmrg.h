@@ -203,6 +203,8 @@ typedef struct ct_dmrg_stats {
     int64_t completed_rows;    /* rows a first visit's rank completion replaced  */
     double seconds_rayleigh;   /* the final FP64 <H> (final_rayleigh), included in seconds_total */
     int64_t stale_retries;     /* warm splits retried with one more power step   */
+    int64_t fp64_handovers;    /* mixed form: splits handed to the FP64 Jacobi
+                                  because eps_trunc may decide chi               */
 } ct_dmrg_stats;
 
 /* Runs the sweeps in place.  mps_sites[i] are caller-owned device buffers of

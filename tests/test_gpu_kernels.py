@@ -279,6 +279,34 @@ def lcg_data(nelem, seed):
     return np.array(out, dtype=np.float64)
 
 
+@pytest.mark.parametrize("n,rate", [(32, 0.5), (512, 0.04), (512, 0.12)])
+def test_svd_split_decaying_spectrum(ctx, n, rate):
+    """FP64 split of theta whose singular values decay geometrically far below machine
+    precision (exp(-rate k); 512 x 2 = 1024: the cooperative Jacobi, 32 x 2: one CTA), the
+    shape of a converged DMRG bond.  The rotations among the tiny columns sit at the noise
+    floor of the FP64 dot products; the split must converge (no CT_ERR_NOCONV), keep an
+    orthonormal canonical factor and give the spectrum to 1e-13 of s_0."""
+    import ctypes as C
+    import torch
+    ct = ct_mod()
+    m = 2 * n
+    rng = np.random.default_rng(n + int(rate * 100))
+    U, _ = np.linalg.qr(rng.standard_normal((m, m)))
+    V, _ = np.linalg.qr(rng.standard_normal((m, m)))
+    s = np.exp(-rate * np.arange(m))
+    th = ((U * s) @ V.T).reshape(n, 2, 2, n)
+    A, B, disc, S = ct.split_two_site_theta_svd(dt(ctx, th), m, 0.0, ctx, True, return_spectrum=True)
+    chi = A.right_bond_dim()
+    am = A.tensor.to_numpy().reshape(-1, chi)
+    assert np.abs(am.T @ am - np.eye(chi)).max() < 1e-12
+    ref = np.linalg.svd(th.reshape(m, m), compute_uv=False)
+    assert np.allclose(S[:chi], ref[:chi], rtol=0, atol=1e-13 * ref[0])
+    sweeps = C.c_int()
+    total = C.c_int64()
+    ctx.call("ct_svd_sweeps", C.byref(sweeps), C.byref(total))
+    assert 0 < sweeps.value < 48
+
+
 def test_svd_known_singular_values(ctx):
     """test_svd_lapack.mojo:55-91: rank-2 4x3 matrix with singular values [3, 2]."""
     ct = ct_mod()

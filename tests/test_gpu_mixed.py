@@ -205,8 +205,9 @@ def test_dmrg_tf32x3_vs_fp64(ctx):
 @pytest.mark.parametrize("dims,chi_max,eps", [((96, 2, 96), 150, 1e-10), ((96, 2, 80), 64, 0.0),
                                               ((50, 4, 60), 300, 1e-12)])
 def test_svd_split_mixed(ctx, dims, chi_max, eps, l2r):
-    """Mixed SVD: canonical factor orthonormal to FP64 accuracy, chi equal to the FP64 split's,
-    discarded weight and squared singular values to 1e-12."""
+    """Mixed form with the spectrum returned, or with eps_trunc deciding chi: the split is the
+    FP64 Jacobi's, so chi equals the oracle's, the discarded weight and the squared singular
+    values agree to 1e-12, and the canonical factor is orthonormal to FP64 accuracy."""
     ct = ct_mod()
     Dl, d, Dr = dims
     rng = np.random.default_rng(Dl + 3 * Dr)
@@ -221,15 +222,10 @@ def test_svd_split_mixed(ctx, dims, chi_max, eps, l2r):
                                                 prec="tf32x3")
     chi = A.right_bond_dim()
     a, b = A.tensor.to_numpy(), B.tensor.to_numpy()
-    # bookkeeping exact: with eps binding (and whenever the spectrum is returned) theta is
-    # projected on the FP64-orthonormal basis in FP64, so the captured weights are exact to
-    # second order in the FP32 Jacobi's subspace angle
     assert chi == info.chi
     recon = np.tensordot(a, b, axes=([2], [0]))
     committed = np.sum((recon - th) ** 2) / np.sum(th * th)
     assert abs(committed - info.discarded_weight) <= 1e-12
-    # weights s^2 to 1e-12 of s_0^2 (individual weak values near the cut can mix with their
-    # neighbours at first order in the angle; their squares only at second order)
     assert np.allclose(S[:chi] ** 2, info.S[:chi] ** 2, rtol=0, atol=1e-12 * info.S[0] ** 2)
     am, bm = a.reshape(-1, chi), b.reshape(chi, -1)
     if l2r:
@@ -240,6 +236,35 @@ def test_svd_split_mixed(ctx, dims, chi_max, eps, l2r):
         prod = np.tensordot(a, b, axes=([2], [0]))
         prod_ref = np.tensordot(A_ref, B_ref, axes=([2], [0]))
         assert rel(prod, prod_ref) < 1e-5
+
+
+@pytest.mark.parametrize("l2r", [True, False])
+def test_svd_split_mixed_chi_max_binds(ctx, l2r):
+    """eps_trunc > 0 far from the cut (the tail at chi_max = 64 is ~1e-5 of |theta|^2, eps 1e-10):
+    the mixed split keeps its own result.  chi = chi_max as in the oracle; the reported discarded
+    weight is that of the factors returned (FP64 projection) and, the excess over the optimal
+    one being second order in the FP32 Jacobi's angles, within 1e-12 of the oracle's
+    (measured: 6e-14)."""
+    ct = ct_mod()
+    Dl, d, Dr = 96, 2, 96
+    rng = np.random.default_rng(17)
+    m, n = Dl * d, d * Dr
+    U0, _ = np.linalg.qr(rng.standard_normal((m, m)))
+    V0, _ = np.linalg.qr(rng.standard_normal((n, m)))
+    th = ((U0 * np.exp(-0.08 * np.arange(m))) @ V0.T).reshape(Dl, d, d, Dr)
+    _, _, info = od.split_two_site_theta_svd(th, 64, 1e-10, l2r)
+    A, B, disc = ct.split_two_site_theta_svd(dt(ctx, th), 64, 1e-10, ctx, l2r, prec="tf32x3")
+    chi = A.right_bond_dim()
+    assert chi == info.chi == 64
+    a, b = A.tensor.to_numpy(), B.tensor.to_numpy()
+    committed = np.sum((np.tensordot(a, b, axes=([2], [0])) - th) ** 2) / np.sum(th * th)
+    assert abs(committed - disc) <= 1e-13
+    assert abs(disc - info.discarded_weight) <= 1e-12
+    am, bm = a.reshape(-1, chi), b.reshape(chi, -1)
+    if l2r:
+        assert np.abs(am.T @ am - np.eye(chi)).max() < 1e-12
+    else:
+        assert np.abs(bm @ bm.T - np.eye(chi)).max() < 1e-12
 
 
 def test_dmrg_warm_subspace_split(ctx):
