@@ -76,7 +76,7 @@ RAMP = [64, 256, 1024]
 ACC_RAMP = (64, 256, 256, 256, 256)
 # dram__bytes_read.sum + dram__bytes_write.sum of one centre-bond H_eff GEMM launch
 # (5120 x 4096 x 1024 at chi=1024, 128x256 tiles) from an ncu --set full capture
-TC_GEMM_TRAFFIC_BYTES = (79.3 + 46.4) * 1e6
+TC_GEMM_TRAFFIC_BYTES = (80.065 + 46.893) * 1e6
 METRIC = "DMRG sweep s & H_eff TFLOP/s, mixed-prec vs FP64 on GPU at |dE/E|<=1e-9"
 
 
@@ -405,13 +405,16 @@ def fp64_ref_mode(args):
             "schedule": schedule, "runs": runs}
     at = [k for k, c in enumerate(schedule) if c == args.chi]
     for pr, r in runs.items():
+        # the first sweep at chi grows the bonds; the last one is the steady state
         line[f"{pr}_s_per_sweep_at_chi"] = float(np.mean([r[k]["seconds"] for k in at]))
+        line[f"{pr}_s_last_sweep"] = float(r[-1]["seconds"])
     if "fp64" in runs and "tf32x3" in runs:
         a, b = runs["tf32x3"], runs["fp64"]
         line["dE_over_E_each_sweep"] = [abs(x["energy_rayleigh"] - y["energy_rayleigh"]) / abs(y["energy_rayleigh"])
                                         for x, y in zip(a, b)]
         line["dE_over_E_at_chi"] = max(line["dE_over_E_each_sweep"][k] for k in at)
         line["speedup_mixed_vs_fp64_at_chi"] = line["fp64_s_per_sweep_at_chi"] / line["tf32x3_s_per_sweep_at_chi"]
+        line["speedup_mixed_vs_fp64_last_sweep"] = line["fp64_s_last_sweep"] / line["tf32x3_s_last_sweep"]
         # Schmidt spectra of every bond of the two final states (FP64 device SVD) and the
         # discarded weights of the last sweep's 2(L-1) splits
         sa, sb = ct.mps_schmidt_values(states["tf32x3"], ctx), ct.mps_schmidt_values(states["fp64"], ctx)
@@ -433,12 +436,15 @@ def fp64_ref_mode(args):
 
 
 def heff_grid_mode(args):
-    """H_eff kernel grid: chi in {256, 512, 1024, 2048} x D in {5, 16, 32} x d in {2, 4}.
+    """Kernel grid: chi in {256, 512, 1024, 2048} x D in {5, 16, 32} x d in {2, 4}.
 
     Random L, R [D, chi, chi], W [D, d, d, D] symmetrised in (s, t), theta
-    [chi, d, d, chi], all N(0, 1) from a fixed seed.  Each point: one warm-up
-    and ``--steps`` timed applies (CUDA events).  The FP64 form runs where one
-    apply stays under ~2 s (algorithmic FLOPs <= 2.5 TFLOP).  One JSON line.
+    [chi, d, d, chi] and a site A [chi, d, chi], all N(0, 1) from a fixed seed.
+    Each point: one H_eff apply and one left-environment update, each with one
+    warm-up and ``--steps`` timed calls (CUDA events), in the TF32x3 form and,
+    where one apply stays under ~2 s (algorithmic FLOPs <= 2.5 TFLOP), in the
+    FP64 form.  FLOPs: H_eff 4 D d^2 chi^3 + 4 D^2 d^3 chi^2, environment
+    4 D d chi^3 + 2 D^2 d^2 chi^2.  One JSON line.
     """
     import torch
     import chemtensor_mojo_gb300 as ct
@@ -459,26 +465,38 @@ def heff_grid_mode(args):
                                     [D, chi, chi])
                 Re = ct.DenseTensor(torch.randn(D * chi * chi, generator=g, dtype=torch.float64).to(dev),
                                     [D, chi, chi])
-                row = {"chi": chi, "D": D, "d": d, "gflop": F / 1e9}
-                for prec in ("tf32x3", "fp64"):
-                    if prec == "fp64" and F > 2.5e12:
-                        continue
-                    ct.apply_two_site_heff(th, Le, Re, mpo.sites[0], mpo.sites[1], ctx, prec=prec)
+                A = ct.MPSSite(ct.DenseTensor(torch.randn(chi * d * chi, generator=g, dtype=torch.float64).to(dev),
+                                              [chi, d, chi]))
+                Fe = 4.0 * D * d * chi ** 3 + 2.0 * D * D * d * d * chi ** 2
+                row = {"chi": chi, "D": D, "d": d, "heff_gflop": F / 1e9, "env_gflop": Fe / 1e9}
+
+                def timed(fn):
+                    fn()
                     torch.cuda.synchronize()
                     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                     e0.record()
                     for _ in range(max(args.steps, 1)):
-                        ct.apply_two_site_heff(th, Le, Re, mpo.sites[0], mpo.sites[1], ctx, prec=prec)
+                        fn()
                     e1.record()
                     torch.cuda.synchronize()
-                    sec = e0.elapsed_time(e1) * 1e-3 / max(args.steps, 1)
-                    row[prec] = {"s": sec, "tflops": F / sec / 1e12}
+                    return e0.elapsed_time(e1) * 1e-3 / max(args.steps, 1)
+
+                for prec in ("tf32x3", "fp64"):
+                    if prec == "fp64" and F > 2.5e12:
+                        continue
+                    sec = timed(lambda: ct.apply_two_site_heff(th, Le, Re, mpo.sites[0], mpo.sites[1], ctx,
+                                                               prec=prec))
+                    sec_e = timed(lambda: ct.update_left_environment(Le, A, mpo.sites[0], ctx, prec))
+                    row[prec] = {"heff_s": sec, "heff_tflops": F / sec / 1e12, "env_s": sec_e,
+                                 "env_tflops": Fe / sec_e / 1e12}
                 rows.append(row)
-                del th, Le, Re, mpo
+                print(json.dumps(row), file=sys.stderr, flush=True)
+                del th, Le, Re, mpo, A
                 torch.cuda.empty_cache()
-    print(json.dumps({"metric": "H_eff apply TFLOP/s (kernel grid)", "unit": "TFLOP/s", "data": "synthetic",
-                      "config": {"workload": "H_eff grid chi x D x d, random L/R/W/theta"}, "grid": rows}),
-          flush=True)
+    print(json.dumps({"metric": "H_eff apply and left-environment update TFLOP/s (kernel grid)", "unit": "TFLOP/s",
+                      "data": "synthetic", "steps": args.steps,
+                      "config": {"workload": "chi x D x d grid, random L/R/W/theta/A, N(0,1) seed 11"},
+                      "grid": rows}), flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -904,13 +922,15 @@ def main():
         peak = bf16 / 6.0
         line["roofline"] = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                             "traffic": TC_GEMM_TRAFFIC_BYTES,
-                            "kernel": "tc_gemm_persist_kernel<128,3> and <256,2> (TF32x3, tcgen05; tile width chosen per shape)",
+                            "kernel": "tc_gemm_chunk_kernel<128,3> and <256,2> (TF32x3, tcgen05, a fresh TMEM "
+                                      "accumulator every 64 of K summed in FP32 registers; tile width chosen per shape)",
                             "launches": kt["launches"], "avg_launch_ms": kt["ms"] / kt["launches"],
                             "flops_per_launch": kt["flops"] / kt["launches"],
                             "share_of_timed_region": kt["ms"] * 1e-3 / max(dev_s, 1e-12),
                             "peak_note": f"{peak_src} bf16 {bf16} TFLOP/s / 2 (TF32 rate) / 3 (3 MMAs per product)",
-                            "traffic_note": "DRAM read+write bytes of one centre-bond H_eff GEMM "
-                                            "(5120x4096x1024) from an ncu capture, per launch"}
+                            "traffic_note": "DRAM read+write bytes of one centre-bond H_eff GEMM 1 "
+                                            "(5120x4096x1024, tc_gemm_chunk_kernel<256,2>) from an ncu capture, "
+                                            "per launch"}
     if kt_heff and kt_heff["launches"] > 0:
         # CUDA-event breakdown of the timed sweeps (device seconds, summed over both sweeps)
         heff_s = kt_heff["ms"] * 1e-3

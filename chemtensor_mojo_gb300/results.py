@@ -146,7 +146,9 @@ def mps_schmidt_values(mps: MatrixProductState, ctx: DeviceContext | None = None
     """Schmidt values of the L-1 inner bonds of the normalised state, descending, as NumPy
     arrays.  Right-normalise, then sweep left to right: M_i = C_{i-1} A_i = U S V^T
     (FP64 device Jacobi SVD, no truncation), S are the Schmidt values of bond i+1 and
-    C_i = U^T M_i carries S V^T to the next site."""
+    C_i = S V^T goes on to the next site.  (Not U^T M_i: a one-sided Jacobi's columns
+    U = X / sigma for sigma below eps |M|_F are rounding noise, not orthonormal, and
+    U^T M_i would feed that noise into every later bond.)"""
     ctx = ctx or get_context()
     psi = mps_right_normalize(ctx, mps)
     N = psi.num_sites()
@@ -165,6 +167,5 @@ def mps_schmidt_values(mps: MatrixProductState, ctx: DeviceContext | None = None
             M = M.reshape([k * d, Dr])
         U, S, Vt, c = dense_tensor_svd_trunc(M, ctx, chi_max=1 << 30, eps_trunc=0.0)
         out.append(S.to_numpy().reshape(-1).copy())
-        carry = create_dense_tensor(ctx, [c, Dr])
-        dense_tensor_dot(carry, U, M, ctx, ndim_mult=1, axrange_A=True, axrange_B=True)
+        carry = DenseTensor(Vt.storage.view(c, Dr).mul(S.storage.view(c, 1)).reshape(-1), [c, Dr])
     return out

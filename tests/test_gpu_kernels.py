@@ -307,6 +307,48 @@ def test_svd_split_decaying_spectrum(ctx, n, rate):
     assert 0 < sweeps.value < 48
 
 
+@pytest.mark.parametrize("m,n", [(300, 200), (200, 300), (512, 512)])
+def test_svd_trunc_qr_preconditioned_shapes(ctx, m, n):
+    """ct_svd_trunc above the one-CTA size: the Householder-QR-preconditioned Jacobi on the
+    shorter side.  Singular values to 1e-13 of s_0, both factors orthonormal to 1e-12 (no
+    singular value below the noise floor here), reconstruction to 1e-13."""
+    ct = ct_mod()
+    rng = np.random.default_rng(m + 7 * n)
+    M = rng.standard_normal((m, n)) * np.exp(-0.03 * np.arange(n))[None, :]
+    U, S, Vt, c = ct.dense_tensor_svd_trunc(dt(ctx, M), ctx, chi_max=1 << 30, eps_trunc=0.0)
+    u, s, vt = U.to_numpy(), S.to_numpy(), Vt.to_numpy()
+    ref = np.linalg.svd(M, compute_uv=False)
+    assert c == min(m, n)
+    assert np.abs(s - ref).max() <= 1e-13 * ref[0]
+    assert np.abs(u.T @ u - np.eye(c)).max() < 1e-12
+    assert np.abs(vt @ vt.T - np.eye(c)).max() < 1e-12
+    assert np.abs((u * s) @ vt - M).max() <= 1e-13 * np.abs(M).max()
+
+
+def test_mps_schmidt_values_below_noise_floor(ctx):
+    """Schmidt values of a 16-site state whose middle bond carries a spectrum down to 1e-30
+    (below the Jacobi's eps |M|_F floor, so the normalised factor U = X / sigma is noise there):
+    every bond's weights sum to 1 within 1e-12 and match the state vector's SVD to 1e-13."""
+    ct = ct_mod()
+    L = 16
+    arrays, _ = ct.random_mps_c_compatible_arrays(L, 2, 256, 9)
+    sites = od.right_normalize(arrays)
+    mid = sites[7]
+    lam = np.exp(-np.linspace(0.0, 69.0, mid.shape[2]))
+    sites[7] = mid * lam[None, None, :]
+    sites = od.right_normalize(sites)
+    mps = ct.mps_from_arrays(ctx, sites)
+    sv = ct.mps_schmidt_values(mps, ctx)
+    psi = od.mps_to_statevector(sites)
+    psi = psi / np.linalg.norm(psi)
+    assert min(float(x.min()) for x in sv) < 1e-20
+    for b, x in enumerate(sv):
+        assert abs(np.sum(x * x) - 1.0) < 1e-12, b
+        r = np.linalg.svd(psi.reshape(2 ** (b + 1), -1), compute_uv=False)
+        k = min(len(x), len(r))
+        assert np.abs(x[:k] - r[:k]).max() < 1e-13, b
+
+
 def test_svd_known_singular_values(ctx):
     """test_svd_lapack.mojo:55-91: rank-2 4x3 matrix with singular values [3, 2]."""
     ct = ct_mod()
