@@ -93,7 +93,7 @@ def parse():
     ap.add_argument("--verbose", action="store_true", help="log every split of the timed sweeps to stderr")
     ap.add_argument("--mode", default="sweep",
                     choices=["sweep", "heff", "heff-grid", "split", "hubbard", "contractions", "fp64-ref",
-                             "lanczos"],
+                             "lanczos", "fp64tc"],
                     help="heff / split: only centre-bond H_eff applies / warm splits (small, fixed workloads "
                          "for profilers); heff-grid: H_eff over chi x D x d; contractions: the MPS/MPO "
                          "contraction operations of the reference's contraction benchmark")
@@ -137,6 +137,84 @@ def heff_mode(args):
                       "dtype": args.prec, "config": {"workload": f"centre-bond H_eff chi={chi} D=5 d=2"},
                       "steps": args.steps, "warmup": args.warmup,
                       "gpu_launches": _lib.launch_count() - n0}), flush=True)
+
+
+def fp64tc_mode(args):
+    """FP64 GEMM on the BF16 tensor cores (CT_PREC_FP64_TC) against the FP64 SIMT GEMM.
+
+    GEMM shapes of the mixed form's FP64 work: the subspace split's Gram matrix
+    (1024 x 1024 x 2048, Z Z^T) and its triangular product (1024 x 2048 x 1024),
+    and the two products of one FP64 environment step at chi=1024, D=5, d=2
+    (5120 x 2048 x 1024 and 5120 x 1024 x 2048); N(0,1) operands, seed 13.
+    Per shape and form: one warm-up and --steps timed launches (CUDA events),
+    FP64-equivalent TFLOP/s (2 M N K), and the largest |C_tc - C_fp64| over
+    sum_k |A||B|.  Then <psi|H|psi>/<psi|psi> of a random (unnormalised) MPS,
+    L=24 with bonds up to chi=1024 (Heisenberg MPO), in both forms.  One JSON line.
+    """
+    import ctypes as C
+    import torch
+    import chemtensor_mojo_gb300 as ct
+    from chemtensor_mojo_gb300 import _lib
+    ctx = ct.get_context(0)
+    dev = ctx.torch_device
+    g = torch.Generator(device="cpu").manual_seed(13)
+    rows = []
+    for (m, n, k, tb, name) in ((1024, 1024, 2048, 1, "split Gram Z Z^T"), (1024, 2048, 1024, 0, "split L^-1 Z"),
+                                (5120, 2048, 1024, 0, "env step product 1"), (5120, 1024, 2048, 0, "env step product 2")):
+        A = torch.randn(m, k, generator=g, dtype=torch.float64).to(dev)
+        B = (torch.randn(n, k, generator=g, dtype=torch.float64) if tb else
+             torch.randn(k, n, generator=g, dtype=torch.float64)).to(dev)
+        row = {"shape": [m, n, k], "what": name}
+        out = {}
+        for prec in (0, 2):
+            Cm = torch.zeros(m, n, dtype=torch.float64, device=dev)
+
+            def call():
+                ctx.call("ct_gemm", prec, 0, tb, m, n, k, C.c_double(1.0), C.c_void_p(A.data_ptr()), k,
+                         C.c_void_p(B.data_ptr()), B.shape[1], C.c_double(0.0), C.c_void_p(Cm.data_ptr()), n)
+            call()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(max(args.steps, 1)):
+                call()
+            e1.record()
+            torch.cuda.synchronize()
+            sec = e0.elapsed_time(e1) * 1e-3 / max(args.steps, 1)
+            out[prec] = Cm.clone()
+            row["fp64_tc" if prec else "fp64"] = {"ms": sec * 1e3, "tflops": 2.0 * m * n * k / sec / 1e12}
+        scale = A.abs() @ (B.abs().T if tb else B.abs())
+        row["max_err_over_AB"] = float(((out[2] - out[0]).abs() / scale).max())
+        row["speedup"] = row["fp64"]["ms"] / row["fp64_tc"]["ms"]
+        rows.append(row)
+        del A, B, out, scale
+        torch.cuda.empty_cache()
+    # expectation value chain
+    L, chi = 24, 1024
+    dims = [min(chi, 2 ** min(i, L - i)) for i in range(L + 1)]
+    sites = [ct.MPSSite(ct.DenseTensor(torch.randn(dims[i] * 2 * dims[i + 1], generator=g,
+                                                   dtype=torch.float64).to(dev) / math.sqrt(2 * dims[i + 1]),
+                                       [dims[i], 2, dims[i + 1]])) for i in range(L)]
+    mps = ct.MatrixProductState(sites)
+    mpo = ct.create_spin_half_xxz_mpo(ctx, L, 1.0)
+    ev = {}
+    for prec in ("fp64", "fp64_tc"):
+        ct.expectation_value_normalized(mps, mpo, ctx, prec=prec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ev[prec] = (ct.expectation_value_normalized(mps, mpo, ctx, prec=prec), None)
+        torch.cuda.synchronize()
+        ev[prec] = (ev[prec][0], time.perf_counter() - t0)
+    print(json.dumps({"metric": "FP64 GEMM on BF16 tensor cores vs FP64 SIMT", "unit": "TFLOP/s (FP64-equivalent)",
+                      "data": "synthetic", "steps": args.steps,
+                      "config": {"workload": "GEMM shapes of the mixed form's FP64 work, N(0,1) seed 13; "
+                                             f"<H> of a random MPS L={L} chi<={chi}"},
+                      "gemm": rows,
+                      "expectation": {"L": L, "chi": chi,
+                                      "fp64": {"value": ev["fp64"][0], "s": ev["fp64"][1]},
+                                      "fp64_tc": {"value": ev["fp64_tc"][0], "s": ev["fp64_tc"][1]},
+                                      "rel_diff": abs(ev["fp64_tc"][0] - ev["fp64"][0]) / abs(ev["fp64"][0])}}),
+          flush=True)
 
 
 def lanczos_mode(args):
@@ -272,9 +350,9 @@ def hubbard_mode(args):
     power steps); then one adjoint-gradient pass at the final state in the
     mixed form (environment checkpoints every 7 sites).  Reports sweep seconds per chi,
     the FP64 Rayleigh energy, the gradient residual |grad E| (zero at a
-    stationary state), |dE/E| of the mixed form against the FP64 form at
-    chi=256 (two sweeps each from the same start, Jacobi first visits in both)
-    and peak device memory.  One JSON line.
+    stationary state), |dE/E| of the mixed form against the FP64 form after two
+    sweeps at chi=256 and two more at 512 (same start, Jacobi first visits in
+    both) and peak device memory.  One JSON line.
     """
     import ctypes as C
     import torch
@@ -318,21 +396,28 @@ def hubbard_mode(args):
                     "max_discarded": st.max_discarded})
     accuracy, gradient = None, None
     if not args.no_extras:
-        # mixed vs FP64 form at chi=256, two sweeps each from the same start with
-        # Jacobi first visits in both (so the difference is precision, not the start)
+        # mixed vs FP64 form on the same start: two sweeps at chi=256, then two at 512
+        # (Jacobi first visits in both forms, so the difference is precision, not the start);
+        # FP64 Rayleigh energy after each call in both forms
+        stages = [c for c in (256, 512) if c <= max(ramp)]
         acc_e = {}
         acc_t = {}
         for pr in ("fp64", "tf32x3"):
             mps_c = ct.mps_right_normalize(ctx, ct.mps_from_arrays(ctx, arrays))
-            st_c = ct.DMRGStats()
-            E_c, _ = ct.dmrg_two_site(ctx, mpo, mps_c, ct.DMRGParams(
-                num_sweeps=2, chi_max=ramp[0], eps_trunc=0.0, max_krylov_iter=LANCZOS, krylov_tol=1e-10,
-                energy_tol=0.0, max_rotations=0, prec=pr, final_rayleigh=(pr == "tf32x3")), st_c)
-            acc_e[pr] = st_c.energy_rayleigh if pr == "tf32x3" else E_c
-            acc_t[pr] = st_c.seconds_total / 2
-        accuracy = {"chi_max": ramp[0], "sweeps": 2, "E_fp64": acc_e["fp64"], "E_mixed_rayleigh_fp64": acc_e["tf32x3"],
-                    "dE_over_E": abs(acc_e["tf32x3"] - acc_e["fp64"]) / abs(acc_e["fp64"]),
-                    "seconds_per_sweep": acc_t}
+            acc_e[pr], acc_t[pr] = [], []
+            for k, c in enumerate(stages):
+                st_c = ct.DMRGStats()
+                _, mps_c = ct.dmrg_two_site(ctx, mpo, mps_c, ct.DMRGParams(
+                    num_sweeps=2, chi_max=c, eps_trunc=0.0, max_krylov_iter=LANCZOS, krylov_tol=1e-10,
+                    energy_tol=0.0, max_rotations=0, prec=pr, final_rayleigh=True,
+                    keep_bases=(pr == "tf32x3" and k > 0)), st_c)
+                acc_e[pr].append(st_c.energy_rayleigh)
+                acc_t[pr].append((st_c.seconds_total - st_c.seconds_rayleigh) / 2)
+        accuracy = {"chi_max_stages": stages, "sweeps_per_stage": 2, "E_fp64": acc_e["fp64"],
+                    "E_mixed_rayleigh_fp64": acc_e["tf32x3"],
+                    "dE_over_E": [abs(a - b) / abs(b) for a, b in zip(acc_e["tf32x3"], acc_e["fp64"])],
+                    "seconds_per_sweep": acc_t,
+                    "note": "FP64 Rayleigh energies of both forms after each stage, same start"}
         sites = [s.tensor.storage[: int(np.prod(s.tensor.shape))].view(*s.tensor.shape) for s in mps.sites]
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -751,6 +836,9 @@ def main():
         return
     if args.mode == "lanczos":
         lanczos_mode(args)
+        return
+    if args.mode == "fp64tc":
+        fp64tc_mode(args)
         return
     if args.mode == "heff":
         heff_mode(args)

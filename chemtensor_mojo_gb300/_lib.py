@@ -29,7 +29,8 @@ NOALLOC_SCRATCH_DOUBLES = 1 << 21
 
 CT_PREC_FP64 = 0
 CT_PREC_TF32X3 = 1
-PRECISIONS = {"fp64": CT_PREC_FP64, "tf32x3": CT_PREC_TF32X3}
+CT_PREC_FP64_TC = 2
+PRECISIONS = {"fp64": CT_PREC_FP64, "tf32x3": CT_PREC_TF32X3, "fp64_tc": CT_PREC_FP64_TC}
 
 
 class CTDMRGError(RuntimeError):

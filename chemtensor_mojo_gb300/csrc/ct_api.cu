@@ -161,6 +161,7 @@ int ct_destroy(ct_handle* h) {
     for (auto& b : h->basis_cache) cudaFree(b.p);
     for (auto e : h->ktime_ev) cudaEventDestroy(e);
     cudaFree(h->splitk);
+    cudaFree(h->oz_ws);
     cudaFree(h->tc_sk_part);
     cudaFree(h->tc_sk_flag);
     cudaFree(h->d_status);
@@ -239,7 +240,14 @@ int ct_set_svd_max_sweeps(ct_handle* h, int max_sweeps) {
 int ct_gemm(ct_handle* h, int prec, int trans_a, int trans_b, int64_t m, int64_t n, int64_t k, double alpha,
             const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc) {
     CT_NULLCHK(h, h);
-    CT_TRY(check_prec(h, prec));
+    if (prec == CT_PREC_FP64_TC) {
+        if (!ct_tc_available(h)) {
+            ct_seterr(h, "FP64 tensor-core GEMM needs an sm_103 device");
+            return CT_ERR_UNSUPPORTED;
+        }
+    } else {
+        CT_TRY(check_prec(h, prec));
+    }
     if (m < 0 || n < 0 || k < 0) return CT_ERR_SHAPE;
     if (m == 0 || n == 0) return CT_OK;
     CT_NULLCHK(h, C);
@@ -256,6 +264,12 @@ int ct_gemm(ct_handle* h, int prec, int trans_a, int trans_b, int64_t m, int64_t
         CT_TRY(ct_reserve(h, ct_tc_gemm_ws_bytes(m, n, k)));
         Arena ar(h);
         CT_TRY(ct_tc_gemm(h, ar, trans_a, trans_b, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc));
+        return CT_OK;
+    }
+    if (prec == CT_PREC_FP64_TC && k > 0) {
+        // op(A)(i,p) = trans_a ? A[p*lda + i] : A[i*lda + p]; B(j,p) = op(B)[p][j]
+        CT_TRY(ct_oz_gemm(h, m, n, k, A, trans_a ? 1 : lda, trans_a ? lda : 1, B, trans_b ? ldb : 1,
+                          trans_b ? 1 : ldb, alpha, beta, C, ldc));
         return CT_OK;
     }
     GemmDesc g{};

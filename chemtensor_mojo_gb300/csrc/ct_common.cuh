@@ -49,6 +49,8 @@ struct ct_handle {
     // FP64 GEMM split-K partial sums (grown on demand, freed by ct_destroy)
     double* splitk = nullptr;
     size_t splitk_cap = 0;   // doubles
+    void* oz_ws = nullptr;   // slices of the FP64 tensor-core GEMM (ct_ozaki.cu)
+    size_t oz_ws_bytes = 0;
     // allocation-free mode (the stack handle of ct_heff2_apply_noalloc): the
     // launchers never call cudaMalloc; split-K partials come from the fixed
     // region below, and K is split only as far as that region holds
@@ -71,15 +73,16 @@ struct ct_handle {
     int ktime_pending = 0;
     int ktime_open = 0;              // regions begun and not yet ended
     int64_t ktime_dropped = 0;       // regions not timed: pool full while a region was open
-    int64_t ktime_count[4] = {0, 0, 0, 0};
-    double ktime_ms[4] = {0, 0, 0, 0}, ktime_flops[4] = {0, 0, 0, 0};
+    int64_t ktime_count[5] = {0, 0, 0, 0, 0};
+    double ktime_ms[5] = {0, 0, 0, 0, 0}, ktime_flops[5] = {0, 0, 0, 0, 0};
 };
 
 // live timing classes; KT_HEFF_LARGEST is derived: the H_eff applies with the
 // largest FLOP count seen (the centre bond at chi_max).  KT_LANCZOS_VEC: the
 // Krylov vector work of each reorthogonalised Lanczos step (alpha, recurrence,
 // Gram-Schmidt pass, next vector), its "flops" field holding algorithmic bytes.
-enum { KT_TC_GEMM = 0, KT_HEFF_APPLY = 1, KT_HEFF_LARGEST = 2, KT_LANCZOS_VEC = 3, KT_NCLASSES = 4 };
+// KT_OZ_GEMM: the FP64 GEMM on the BF16 tensor cores (2 M N K per launch).
+enum { KT_TC_GEMM = 0, KT_HEFF_APPLY = 1, KT_HEFF_LARGEST = 2, KT_LANCZOS_VEC = 3, KT_OZ_GEMM = 4, KT_NCLASSES = 5 };
 // start a timed region of class cls (slot = -1 when timing is off); end it after the launches
 int ct_ktime_begin(ct_handle* h, int cls, double flops, int* slot);
 int ct_ktime_end(ct_handle* h, int slot);
@@ -272,6 +275,12 @@ int ct_lanczos_reorth_pass(ct_handle* h, int64_t n, double* w, const double* V, 
                            double beta_threshold, const int* skip);
 int ct_lanczos_update_nonorm(ct_handle* h, int64_t n, double* w, const double* vj, const double* vjm1, int j,
                              const int* skip);
+// the same pass against an FP32 copy of the basis; v_{j+1} with its FP32 copy
+int ct_lanczos_reorth_pass32(ct_handle* h, int64_t n, double* w, const float* V32, int64_t ldv, int j,
+                             double beta_threshold, const int* skip);
+int ct_lanczos_next32(ct_handle* h, int64_t n, const double* w, double* vnext, float* vnext32, int j,
+                      const int* skip);
+int ct_f64_to_f32(ct_handle* h, int64_t n, const double* x, float* y, const int* skip);
 int ct_tridiag_eig(ct_handle* h, int max_iter, double tol, int max_rotations);
 int ct_ritz(ct_handle* h, int64_t n, const double* V, int64_t ldv, double* out);
 

@@ -452,7 +452,10 @@ int ct_dmrg_two_site(ct_handle* h, const ct_dmrg_params* P, int N, int d, const 
     if (P->final_rayleigh) {
         const auto t_rq = std::chrono::steady_clock::now();
         double e = 0.0, nsq = 0.0;
-        CT_TRY(ct_mps_expectation(h, CT_PREC_FP64, N, d, mpo_dims, mpo_sites, bd, (const double* const*)mps_sites,
+        // the mixed form's FP64 energy with its products on the BF16 tensor cores (FP64-accurate
+        // slicing); the FP64 form keeps its SIMT GEMMs
+        const int rprec = (prec == CT_PREC_TF32X3) ? CT_PREC_FP64_TC : CT_PREC_FP64;
+        CT_TRY(ct_mps_expectation(h, rprec, N, d, mpo_dims, mpo_sites, bd, (const double* const*)mps_sites,
                                   &e, &nsq));
         st.energy_rayleigh = e / nsq;
         st.seconds_rayleigh = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_rq).count();
@@ -520,7 +523,10 @@ int ct_mps_right_normalize(ct_handle* h, int N, int d, int64_t* bd, double* cons
 int ct_mps_expectation(ct_handle* h, int prec, int N, int d, const int64_t* mpo_dims, const double* const* mpo_sites,
                        const int64_t* bd, const double* const* sites, double* energy_host, double* norm_sq_host) {
     if (!h || !mpo_dims || !mpo_sites || !bd || !sites || N < 1 || d < 1) return CT_ERR_INVALID;
-    if (prec != CT_PREC_FP64 && !(prec == CT_PREC_TF32X3 && ct_tc_available(h))) return CT_ERR_UNSUPPORTED;
+    if (prec != CT_PREC_FP64 && !((prec == CT_PREC_TF32X3 || prec == CT_PREC_FP64_TC) && ct_tc_available(h)))
+        return CT_ERR_UNSUPPORTED;
+    // CT_PREC_FP64_TC: FP64-accurate products on the BF16 tensor cores; TF32X3 as FP64
+    const int eprec = (prec == CT_PREC_FP64_TC) ? CT_PREC_FP64_TC : CT_PREC_FP64;
     int64_t cap = 1;
     for (int k = 0; k <= N; ++k) cap = std::max<int64_t>(cap, std::max<int64_t>(mpo_dims[k], 1) * bd[k] * bd[k]);
     DevBuf e0, e1, Wid;
@@ -542,7 +548,7 @@ int ct_mps_expectation(ct_handle* h, int prec, int N, int d, const int64_t* mpo_
             const int64_t wl = (pass == 0) ? mpo_dims[i] : 1, wr = (pass == 0) ? mpo_dims[i + 1] : 1;
             CT_TRY(ct_reserve(h, ct_env_ws_bytes(CT_PREC_FP64, bd[i], d, bd[i + 1], wl, wr)));
             Arena ar(h);
-            CT_TRY(ct_env_left_run(h, ar, CT_PREC_FP64, a, sites[i], pass == 0 ? mpo_sites[i] : Wid.p, b, bd[i], d,
+            CT_TRY(ct_env_left_run(h, ar, eprec, a, sites[i], pass == 0 ? mpo_sites[i] : Wid.p, b, bd[i], d,
                                    bd[i + 1], wl, wr));
             std::swap(a, b);
         }

@@ -15,6 +15,8 @@
 //     T1[Dr', wR, s, Dl] = sum_Dr R[wR,Dr,Dr'] A[Dl,s,Dr]                  GEMM, batch (wR,s)
 //     T2[wL, Dl, s', Dr'] = sum_(wR s) W[wL,s,s',wR] T1                    MPO apply
 //     Rp[wL, Dl, Dl'] = sum_(s' Dr') T2[wL,Dl,(s' Dr')] A[Dl',(s' Dr')]    GEMM, batch wL
+#include <stdlib.h>
+
 #include "ct_ops.cuh"
 
 size_t ct_heff_ws_bytes(int prec, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wM, int64_t wR) {
@@ -95,14 +97,29 @@ size_t ct_env2_ws_bytes(int64_t Dlk, int64_t Dlb, int64_t d, int64_t Drk, int64_
 //   Ln[wR, Drk, Drb] = sum L[wL, Dlk, Dlb] Ak[Dlk, s, Drk] W[wL, s, s', wR] Ab[Dlb, s', Drb]
 // With W == null (wL = wR = 1) the MPO step drops out and this is the overlap
 // transfer step L[Dlk, Dlb] -> L[Drk, Drb] of environments.mojo:767-862.
+bool ct_fp64_tc_enabled(ct_handle* h, int64_t M, int64_t N, int64_t K) {
+    static const int mode = [] {
+        const char* e = getenv("CTDMRG_FP64_TC");
+        return e ? atoi(e) : 1;
+    }();
+    return mode != 0 && !h->no_alloc && M * N * K >= ((int64_t)1 << 21) && ct_tc_available(h);
+}
+
 int ct_env_left2_run(ct_handle* h, Arena& ar, const double* Lp, const double* Ak, const double* Ab,
                      const double* W, double* Ln, int64_t Dlk, int64_t Dlb, int64_t d, int64_t Drk, int64_t Drb,
-                     int64_t wL, int64_t wR) {
+                     int64_t wL, int64_t wR, bool fp64_tc) {
     if (!W && (wL != 1 || wR != 1)) return CT_ERR_SHAPE;
     const int64_t n1 = d * Drk;
     double* T1 = ar.take<double>(Dlb * wL * n1);
     if (!T1) return CT_ERR_OOM;
-    {   // T1[Dlb, wL, (s Drk)] = sum_Dlk L[wL, Dlk, Dlb] Ak[Dlk, (s Drk)]; batch wL
+    if (fp64_tc && ct_fp64_tc_enabled(h, wL * Dlb, n1, Dlk)) {
+        // the same product as one GEMM over rows (wL, Dlb): A(r, k) = L[wL][k][Dlb],
+        // B(n, k) = Ak[k][n], C row (wL, Dlb) at T1[Dlb][wL][.]
+        const OzMat a{Lp, Dlb, Dlk * Dlb, 1, Dlb};
+        const OzMat b{Ak, n1, 0, 1, n1};
+        const OzOut c{T1, Dlb, n1, wL * n1};
+        CT_TRY(ct_oz_gemm_ex(h, wL * Dlb, n1, Dlk, a, b, 1.0, 0.0, c));
+    } else {   // T1[Dlb, wL, (s Drk)] = sum_Dlk L[wL, Dlk, Dlb] Ak[Dlk, (s Drk)]; batch wL
         GemmDesc g{};
         g.M = Dlb; g.N = n1; g.K = Dlk;
         g.A = Lp; g.sAm = 1; g.sAk = Dlb;
@@ -126,7 +143,13 @@ int ct_env_left2_run(ct_handle* h, Arena& ar, const double* Lp, const double* Ak
         CT_TRY(ct_mpo_apply_f64_launch(h, m));
         T2 = T2w;
     }
-    {   // Ln[(wR Drk), Drb] = sum_(Dlb s') T2[(Dlb s'), (wR Drk)] Ab[(Dlb s'), Drb]
+    if (fp64_tc && ct_fp64_tc_enabled(h, wR * Drk, Drb, Dlb * d)) {
+        const int64_t M2 = wR * Drk;
+        const OzMat a{T2, M2, 0, 1, M2};      // A(m, k) = T2[k][m]
+        const OzMat b{Ab, Drb, 0, 1, Drb};    // B(n, k) = Ab[k][n]
+        const OzOut c{Ln, M2, 0, Drb};
+        CT_TRY(ct_oz_gemm_ex(h, M2, Drb, Dlb * d, a, b, 1.0, 0.0, c));
+    } else {   // Ln[(wR Drk), Drb] = sum_(Dlb s') T2[(Dlb s'), (wR Drk)] Ab[(Dlb s'), Drb]
         GemmDesc g{};
         g.M = wR * Drk; g.N = Drb; g.K = Dlb * d;
         g.A = T2; g.sAm = 1; g.sAk = wR * Drk;
@@ -141,7 +164,7 @@ int ct_env_left2_run(ct_handle* h, Arena& ar, const double* Lp, const double* Ak
 int ct_env_left_run(ct_handle* h, Arena& ar, int prec, const double* Lp, const double* A, const double* W,
                     double* Ln, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR) {
     if (prec == CT_PREC_TF32X3) return ct_tc_env_left_run(h, ar, Lp, A, W, Ln, Dl, d, Dr, wL, wR);
-    return ct_env_left2_run(h, ar, Lp, A, A, W, Ln, Dl, Dl, d, Dr, Dr, wL, wR);
+    return ct_env_left2_run(h, ar, Lp, A, A, W, Ln, Dl, Dl, d, Dr, Dr, wL, wR, prec == CT_PREC_FP64_TC);
 }
 
 int ct_env_right_run(ct_handle* h, Arena& ar, int prec, const double* Rn, const double* A, const double* W,
@@ -215,7 +238,9 @@ int ct_theta_run(ct_handle* h, int prec, const double* Ai, const double* Aj, dou
 size_t ct_lanczos_ws_bytes(int prec, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wM, int64_t wR,
                            int max_iter) {
     const int64_t N = Dl * d * d * Dr;
-    return ct_bytes(N * (int64_t)max_iter, 8) + ct_bytes(N, 8) + ct_heff_ws_bytes(prec, Dl, d, Dr, wL, wM, wR);
+    // (the mixed form also keeps an FP32 copy of the basis for the reorthogonalisation)
+    return ct_bytes(N * (int64_t)max_iter, 8) + ct_bytes(N, 8) + ct_heff_ws_bytes(prec, Dl, d, Dr, wL, wM, wR) +
+           (prec == CT_PREC_TF32X3 ? ct_bytes(N * (int64_t)max_iter, 4) : 0);
 }
 
 int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, double* theta_out, const double* L,
@@ -230,6 +255,12 @@ int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, do
     double* V = ar.take<double>(N * (int64_t)max_iter);
     double* w = ar.take<double>(N);
     if (!V || !w) return CT_ERR_OOM;
+    // mixed form: FP32 copy of the basis for the reorthogonalisation pass
+    float* V32 = nullptr;
+    if (reorth && prec == CT_PREC_TF32X3) {
+        V32 = ar.take<float>(N * (int64_t)max_iter);
+        if (!V32) return CT_ERR_OOM;
+    }
     HeffPlan plan;
     CT_TRY(ct_heff_prepare(h, ar, plan, prec, L, R, W1, W2, Dl, d, Dr, wL, wM, wR));
     const int* stop = h->d_flags + FL_STOP;
@@ -239,6 +270,7 @@ int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, do
     CT_TRY(ct_reduce_nrm2sq(h, N, theta_in, h->d_scalars + SC_NORM, nullptr));
     CT_TRY(ct_check_finite(h, h->d_scalars + SC_NORM, nullptr));
     CT_TRY(ct_scale_by_inv_sqrt(h, N, theta_in, V, h->d_scalars + SC_NORM, nullptr, CT_ERR_ZERO_NORM));
+    if (V32) CT_TRY(ct_f64_to_f32(h, N, V, V32, nullptr));
     const double thr = 100.0 * (double)N * 2.2204460492503131e-16;
     // algorithmic FLOPs of one apply (the reference's four contractions)
     const double heff_flops = 2.0 * (double)Dl * wL * d * d * Dr * Dl + 2.0 * (double)Dl * d * Dr * wL * d * d * wM +
@@ -256,13 +288,23 @@ int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, do
             // Algorithmic bytes of the vector work: alpha reads v_j and w, the
             // recurrence reads w, v_j, v_{j-1} and writes w, the pass reads w and j + 1
             // vectors twice and writes w, the next vector reads w and writes v_{j+1}.
-            const double bytes = 8.0 * (double)N * (double)(2 + (j > 0 ? 4 : 3) + (j + 2) + (j + 3) + 2);
+            // With the FP32 copy (mixed form) the pass reads 4-byte basis vectors and the
+            // next-vector kernel also writes the copy.
+            const double nb = (double)(j + 1);
+            const double bytes = V32 ? (double)N * (8.0 * (2 + (j > 0 ? 4 : 3)) + (8.0 + 4.0 * nb) +
+                                                    (16.0 + 4.0 * nb) + 20.0)
+                                     : 8.0 * (double)N * (double)(2 + (j > 0 ? 4 : 3) + (j + 2) + (j + 3) + 2);
             int kv = -1;
             CT_TRY(ct_ktime_begin(h, KT_LANCZOS_VEC, bytes, &kv));
             CT_TRY(ct_lanczos_alpha(h, N, vj, w, j, stop));
             CT_TRY(ct_lanczos_update_nonorm(h, N, w, vj, vjm1, j, stop));
-            CT_TRY(ct_lanczos_reorth_pass(h, N, w, V, N, j, thr, stop));
-            CT_TRY(ct_lanczos_next(h, N, w, V + (int64_t)(j + 1) * N, j, stop));
+            if (V32) {
+                CT_TRY(ct_lanczos_reorth_pass32(h, N, w, V32, N, j, thr, stop));
+                CT_TRY(ct_lanczos_next32(h, N, w, V + (int64_t)(j + 1) * N, V32 + (int64_t)(j + 1) * N, j, stop));
+            } else {
+                CT_TRY(ct_lanczos_reorth_pass(h, N, w, V, N, j, thr, stop));
+                CT_TRY(ct_lanczos_next(h, N, w, V + (int64_t)(j + 1) * N, j, stop));
+            }
             CT_TRY(ct_ktime_end(h, kv));
             continue;
         }

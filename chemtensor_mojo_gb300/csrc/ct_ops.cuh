@@ -33,9 +33,12 @@ int ct_env_left_run(ct_handle* h, Arena& ar, int prec, const double* Lp, const d
 int ct_env_right_run(ct_handle* h, Arena& ar, int prec, const double* Rn, const double* A, const double* W,
                      double* Rp, int64_t Dl, int64_t d, int64_t Dr, int64_t wL, int64_t wR);
 size_t ct_env2_ws_bytes(int64_t Dlk, int64_t Dlb, int64_t d, int64_t Drk, int64_t Drb, int64_t wL, int64_t wR);
+// fp64_tc: the two large products on the BF16 tensor cores (ct_oz_gemm_ex, FP64-accurate)
 int ct_env_left2_run(ct_handle* h, Arena& ar, const double* Lp, const double* Ak, const double* Ab,
                      const double* W, double* Ln, int64_t Dlk, int64_t Dlb, int64_t d, int64_t Drk, int64_t Drb,
-                     int64_t wL, int64_t wR);
+                     int64_t wL, int64_t wR, bool fp64_tc = false);
+// FP64 products on the BF16 tensor cores for this size (CTDMRG_FP64_TC=0 disables them)
+bool ct_fp64_tc_enabled(ct_handle* h, int64_t M, int64_t N, int64_t K);
 size_t ct_theta_ws_bytes(int prec, int64_t Dl, int64_t d, int64_t Dm, int64_t Dr);
 int ct_theta_run(ct_handle* h, int prec, const double* Ai, const double* Aj, double* theta, int64_t Dl,
                  int64_t d, int64_t Dm, int64_t Dr);
@@ -74,6 +77,26 @@ size_t ct_split_ws_bytes(int prec, int64_t m, int64_t n, int64_t chi_max, int mo
 int ct_split_run(ct_handle* h, Arena& ar, int prec, const double* M, int64_t m, int64_t n, int64_t chi_max,
                  double eps_trunc, int mode, double* A, double* B, double* S, const double* d_total, SvdOut* out,
                  float* qcache = nullptr, int warm = 0);
+
+// FP64 GEMM on the BF16 tensor cores (ct_ozaki.cu): C[m*ldc + n] = alpha * sum_k
+// A(m,k) B(n,k) + beta * C, A(m,k) = A[m*a_sr + k*a_sk], B(n,k) = B[n*b_sr + k*b_sk]
+// (slices in a handle-owned buffer that grows on demand; a Gram product A A^T slices once)
+// Two-level rows: element (r, k) of an operand at p[(r / R0) * s1 + (r % R0) * s0 + k * sk]
+// (R0 = 0: one level), row m of C at p[(m / M0) * s1 + (m % M0) * s0] with contiguous columns.
+struct OzMat {
+    const double* p;
+    int64_t R0, s1, s0, sk;
+};
+struct OzOut {
+    double* p;
+    int64_t M0, s1, s0;
+};
+int ct_oz_gemm_ex(ct_handle* h, int64_t M, int64_t N, int64_t K, const OzMat& A, const OzMat& B, double alpha,
+                  double beta, const OzOut& C, int lower = 0);
+size_t ct_oz_gemm_ws_bytes(int64_t M, int64_t N, int64_t K);
+int ct_oz_gemm(ct_handle* h, int64_t M, int64_t N, int64_t K, const double* A, int64_t a_sr, int64_t a_sk,
+               const double* B, int64_t b_sr, int64_t b_sk, double alpha, double beta, double* C, int64_t ldc,
+               int lower = 0);
 
 // warm-started subspace split (ct_svd_subspace.cu)
 size_t ct_split_subspace_ws_bytes(int64_t m, int64_t n, int64_t c);

@@ -57,6 +57,8 @@
 // exceeds stale_mult x that of the previous visit of the bond plus stale_abs
 // (the cached basis no longer tracks the dominant subspace), or when it is
 // <= eps_trunc (then the rule may keep fewer states and needs the spectrum).
+#include <stdlib.h>
+
 #include "ct_ops.cuh"
 
 namespace {
@@ -232,9 +234,14 @@ GemmDesc gemm2d(int64_t M, int64_t N, int64_t K, const double* A, int64_t sAm, i
     return g;
 }
 
-// C = alpha A op(B) + beta C in FP64 for the factorisation (tri as in GemmDesc).
+// C = alpha A op(B) + beta C in FP64 for the factorisation (tri as in GemmDesc).  On the
+// tensor cores, tri == 1 skips the tiles above the diagonal block and tri == 2 (lower-
+// triangular A) runs over the whole K: the zeros of A's upper triangle add nothing.
 int fac_gemm(ct_handle* h, int64_t M, int64_t N, int64_t K, const double* A, int64_t lda, const double* B,
              int64_t ldb, int trans_b, double* C, int64_t ldc, double alpha, double beta, int tri) {
+    if (ct_fp64_tc_enabled(h, M, N, K))
+        return ct_oz_gemm(h, M, N, K, A, lda, 1, B, trans_b ? ldb : 1, trans_b ? 1 : ldb, alpha, beta, C, ldc,
+                          tri == 1);
     GemmDesc g = trans_b ? gemm2d(M, N, K, A, lda, 1, B, 1, ldb, C, ldc, alpha, beta)
                          : gemm2d(M, N, K, A, lda, 1, B, ldb, 1, C, ldc, alpha, beta);
     g.tri = tri;

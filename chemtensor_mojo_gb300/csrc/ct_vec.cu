@@ -376,6 +376,168 @@ __global__ void __launch_bounds__(RT) cgs_update_kernel(int64_t n, double* __res
     }
 }
 
+// ---- the same pass against an FP32 copy of the basis (mixed form) --------------------
+// After the FP64 recurrence the coefficients c_k = <V_k, w> are small (the components
+// that the TF32-level H_eff and rounding leave along the older vectors), so the pass
+// needs them only to a small relative accuracy: the dots run on FP32 copies of the
+// basis and of w (FP32 products, per-thread FP32 sums of a few dozen terms, FP64
+// across threads and blocks), and the update forms the correction sum_k c_k V32_k in
+// FP32 and subtracts it from w in FP64.  Errors: ~1e-7 relative on c_k and on the
+// correction, i.e. residual components ~1e-7 |c| along the basis, against the 1e-8
+// that semi-orthogonality asks for.  The basis is read at 4 bytes per element instead
+// of 8, with FP32 multiply-adds instead of FP64 ones (1/64 of the FP32 rate here).
+template <int NV>
+__device__ __forceinline__ void cgs32_dots_group(int64_t n, const double* __restrict__ w, const float* __restrict__ x,
+                                                 int64_t ldv, int vec4, float (&acc)[CGS_VB]) {
+    const int64_t stride = (int64_t)gridDim.x * RT;
+    if (vec4) {
+        const int64_t n4 = n / 4;
+        const double2* w2 = reinterpret_cast<const double2*>(w);
+        for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n4; i += stride) {
+            const double2 wa = w2[2 * i], wb = w2[2 * i + 1];
+            const float w0 = (float)wa.x, w1 = (float)wa.y, w2f = (float)wb.x, w3 = (float)wb.y;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                const float4 a = reinterpret_cast<const float4*>(x + (int64_t)k * ldv)[i];
+                acc[k] = fmaf(a.x, w0, fmaf(a.y, w1, fmaf(a.z, w2f, fmaf(a.w, w3, acc[k]))));
+            }
+        }
+    } else {
+        for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) {
+            const float wi = (float)w[i];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) acc[k] = fmaf(x[(int64_t)k * ldv + i], wi, acc[k]);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(RT) cgs32_dots_kernel(int64_t n, const double* __restrict__ w,
+                                                        const float* __restrict__ V, int64_t ldv, int nvec, int vec4,
+                                                        double* partials, unsigned* counter, double* coeff,
+                                                        const int* skip) {
+    if (ct_skip(skip)) return;
+    __shared__ double sm[CGS_VB][RT / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int v0 = 0; v0 < nvec; v0 += CGS_VB) {
+        const int nv = min(CGS_VB, nvec - v0);
+        float acc[CGS_VB];
+#pragma unroll
+        for (int k = 0; k < CGS_VB; ++k) acc[k] = 0.0f;
+        const float* x = V + (int64_t)v0 * ldv;
+        switch (nv) {
+#define CT_CGS_CASE(K) \
+    case K: cgs32_dots_group<K>(n, w, x, ldv, vec4, acc); break;
+            CT_CGS_CASE(1) CT_CGS_CASE(2) CT_CGS_CASE(3) CT_CGS_CASE(4) CT_CGS_CASE(5) CT_CGS_CASE(6)
+            CT_CGS_CASE(7) CT_CGS_CASE(8) CT_CGS_CASE(9) CT_CGS_CASE(10) CT_CGS_CASE(11) CT_CGS_CASE(12)
+            CT_CGS_CASE(13) CT_CGS_CASE(14) CT_CGS_CASE(15) CT_CGS_CASE(16)
+#undef CT_CGS_CASE
+            default: break;
+        }
+        double accd[CGS_VB];
+#pragma unroll
+        for (int k = 0; k < CGS_VB; ++k) accd[k] = (k < nv) ? ct_warp_sum((double)acc[k]) : 0.0;
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < CGS_VB; ++k)
+                if (k < nv) sm[k][wid] = accd[k];
+        }
+        __syncthreads();
+        if (threadIdx.x < nv) {
+            double r = 0.0;
+            for (int q = 0; q < RT / 32; ++q) r += sm[threadIdx.x][q];
+            partials[(int64_t)blockIdx.x * nvec + v0 + threadIdx.x] = r;
+        }
+        __syncthreads();
+    }
+    if (!last_block_arrived(counter)) return;
+    for (int v = wid; v < nvec; v += RT / 32) {
+        double r = 0.0;
+        for (int b = lane; b < (int)gridDim.x; b += 32) r += __ldcg(partials + (int64_t)b * nvec + v);
+        r = ct_warp_sum(r);
+        if (lane == 0) coeff[v] = r;
+    }
+    if (threadIdx.x == 0) *counter = 0u;
+}
+
+__global__ void __launch_bounds__(RT) cgs32_update_kernel(int64_t n, double* __restrict__ w,
+                                                          const float* __restrict__ V, int64_t ldv, int nvec, int vec4,
+                                                          const double* coeff, double* partials, unsigned* counter,
+                                                          double* scalars, int* flags, int j, double thr,
+                                                          const int* skip) {
+    if (ct_skip(skip)) return;
+    __shared__ double sm[32];
+    __shared__ float c[CT_MAX_KRYLOV];
+    for (int v = threadIdx.x; v < nvec; v += RT) c[v] = (float)coeff[v];
+    __syncthreads();
+    double nn = 0.0;
+    const int64_t stride = (int64_t)gridDim.x * RT;
+    if (vec4) {
+        const int64_t n4 = n / 4;
+        double2* w2 = reinterpret_cast<double2*>(w);
+        for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n4; i += stride) {
+            float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int v = 0; v < nvec; ++v) {
+                const float4 a = reinterpret_cast<const float4*>(V + (int64_t)v * ldv)[i];
+                const float cv = c[v];
+                s.x = fmaf(cv, a.x, s.x);
+                s.y = fmaf(cv, a.y, s.y);
+                s.z = fmaf(cv, a.z, s.z);
+                s.w = fmaf(cv, a.w, s.w);
+            }
+            double2 xa = w2[2 * i], xb = w2[2 * i + 1];
+            xa.x -= (double)s.x;
+            xa.y -= (double)s.y;
+            xb.x -= (double)s.z;
+            xb.y -= (double)s.w;
+            w2[2 * i] = xa;
+            w2[2 * i + 1] = xb;
+            nn = fma(xa.x, xa.x, fma(xa.y, xa.y, fma(xb.x, xb.x, fma(xb.y, xb.y, nn))));
+        }
+    } else {
+        for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) {
+            float s = 0.f;
+            for (int v = 0; v < nvec; ++v) s = fmaf(c[v], V[(int64_t)v * ldv + i], s);
+            const double x = w[i] - (double)s;
+            w[i] = x;
+            nn = fma(x, x, nn);
+        }
+    }
+    nn = ct_block_sum<RT>(nn, sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = nn;
+    if (!last_block_arrived(counter)) return;
+    double s = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += RT) s += __ldcg(partials + b);
+    s = ct_block_sum<RT>(s, sm);
+    if (threadIdx.x == 0) {
+        const double b = sqrt(s);
+        if (b < thr) {
+            flags[FL_NUMITER] = j + 1;
+            flags[FL_STOP] = 1;
+        } else {
+            scalars[SC_BETA + j] = b;
+        }
+        *counter = 0u;
+    }
+}
+
+// v_{j+1} = w / beta_j in FP64 and its FP32 copy
+__global__ void lanczos_next32_kernel(int64_t n, const double* w, double* vnext, float* vnext32,
+                                      const double* scalars, int j, const int* skip) {
+    if (ct_skip(skip)) return;
+    const double inv = 1.0 / scalars[SC_BETA + j];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = w[i] * inv;
+        vnext[i] = v;
+        vnext32[i] = (float)v;
+    }
+}
+
+__global__ void f64_to_f32_copy_kernel(int64_t n, const double* x, float* y, const int* skip) {
+    if (ct_skip(skip)) return;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = (float)x[i];
+}
+
 // Ritz vector: out = sum_{i < numiter} c_i V[i]
 __global__ void ritz_kernel(int64_t n, const double* V, int64_t ldv, const double* scalars, const int* flags,
                             double* out) {
@@ -731,6 +893,38 @@ int ct_lanczos_reorth_pass(ct_handle* h, int64_t n, double* w, const double* V, 
     ct_note_launch();
     cgs_update_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, vec2, coeff, h->d_partials, counter,
                                                h->d_scalars, h->d_flags, j, beta_threshold, skip); ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+// Reorthogonalisation pass against the FP32 copy V32 of the basis (mixed form).
+int ct_lanczos_reorth_pass32(ct_handle* h, int64_t n, double* w, const float* V32, int64_t ldv, int j,
+                             double beta_threshold, const int* skip) {
+    const int nvec = j + 1;
+    if (nvec > 64) return CT_ERR_UNSUPPORTED;
+    int g = grid_for(h, n);
+    if ((int64_t)g * nvec > CT_NPARTIALS) g = CT_NPARTIALS / nvec;
+    const int vec4 = ((n & 3) == 0 && (ldv & 3) == 0 && aligned16(w) && aligned16(V32)) ? 1 : 0;
+    unsigned* counter = reinterpret_cast<unsigned*>(h->d_flags + FL_CNT);
+    double* coeff = h->d_scalars + SC_MISC;
+    cgs32_dots_kernel<<<g, RT, 0, h->stream>>>(n, w, V32, ldv, nvec, vec4, h->d_partials, counter, coeff, skip);
+    ct_note_launch();
+    cgs32_update_kernel<<<g, RT, 0, h->stream>>>(n, w, V32, ldv, nvec, vec4, coeff, h->d_partials, counter,
+                                                 h->d_scalars, h->d_flags, j, beta_threshold, skip); ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_lanczos_next32(ct_handle* h, int64_t n, const double* w, double* vnext, float* vnext32, int j,
+                      const int* skip) {
+    lanczos_next32_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, w, vnext, vnext32, h->d_scalars, j, skip);
+    ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+int ct_f64_to_f32(ct_handle* h, int64_t n, const double* x, float* y, const int* skip) {
+    f64_to_f32_copy_kernel<<<elem_grid(h, n), 256, 0, h->stream>>>(n, x, y, skip); ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }

@@ -84,24 +84,26 @@ def _mps_mpo_pointers(mps: MatrixProductState, mpo: MatrixProductOperator):
     return mpo_pp, mps_pp, (k1, k2)
 
 
-def expectation_value(mps: MatrixProductState, mpo: MatrixProductOperator, ctx: DeviceContext | None = None):
-    """<psi|H|psi> (not normalised), environments.mojo:475-500."""
+def expectation_value(mps: MatrixProductState, mpo: MatrixProductOperator, ctx: DeviceContext | None = None,
+                      prec: str = "fp64"):
+    """<psi|H|psi> (not normalised), environments.mojo:475-500.  prec "fp64_tc": the
+    environment GEMMs on the BF16 tensor cores with FP64-accurate slicing."""
     ctx = ctx or get_context()
     e = C.c_double()
     mpo_pp, mps_pp, keep = _mps_mpo_pointers(mps, mpo)
-    ctx.call("ct_mps_expectation", _lib.CT_PREC_FP64, mps.num_sites(), mps.physical_dim,
+    ctx.call("ct_mps_expectation", _lib.PRECISIONS[prec], mps.num_sites(), mps.physical_dim,
              _lib.i64_array(mpo.bond_dims), mpo_pp, _lib.i64_array(mps.bond_dims), mps_pp, C.byref(e), None)
     return e.value
 
 
 def expectation_value_normalized(mps: MatrixProductState, mpo: MatrixProductOperator,
-                                 ctx: DeviceContext | None = None) -> float:
-    """<psi|H|psi> / <psi|psi>, environments.mojo:503-532."""
+                                 ctx: DeviceContext | None = None, prec: str = "fp64") -> float:
+    """<psi|H|psi> / <psi|psi>, environments.mojo:503-532 (prec as in expectation_value)."""
     ctx = ctx or get_context()
     e = C.c_double()
     n = C.c_double()
     mpo_pp, mps_pp, keep = _mps_mpo_pointers(mps, mpo)
-    ctx.call("ct_mps_expectation", _lib.CT_PREC_FP64, mps.num_sites(), mps.physical_dim,
+    ctx.call("ct_mps_expectation", _lib.PRECISIONS[prec], mps.num_sites(), mps.physical_dim,
              _lib.i64_array(mpo.bond_dims), mpo_pp, _lib.i64_array(mps.bond_dims), mps_pp, C.byref(e), C.byref(n))
     return e.value / n.value
 

@@ -20,6 +20,11 @@
  *   CT_PREC_TF32X3  contractions on tcgen05 tensor cores in TF32 with
  *                   3xTF32 split compensation and FP32 accumulation; all
  *                   storage, Lanczos, eigensolve, SVD and reductions FP64.
+ *   CT_PREC_FP64_TC (ct_gemm only) FP64 products emulated on the BF16
+ *                   tensor cores: each operand row cut into 7 exact 8-bit
+ *                   slices, 28 slice products per FP64 product accumulated
+ *                   exactly in FP32 per 128 of K, combined in FP64; about as
+ *                   accurate as an FP64 GEMM (3e-15 of |A||B|).
  */
 #ifndef CTDMRG_H
 #define CTDMRG_H
@@ -52,7 +57,7 @@ enum ct_status {
     CT_ERR_TOO_LARGE = -10   /* problem exceeds the static scratch of a no-alloc entry */
 };
 
-enum ct_prec { CT_PREC_FP64 = 0, CT_PREC_TF32X3 = 1 };
+enum ct_prec { CT_PREC_FP64 = 0, CT_PREC_TF32X3 = 1, CT_PREC_FP64_TC = 2 };
 
 typedef struct ct_handle ct_handle;
 
@@ -228,7 +233,10 @@ CT_API int ct_mps_right_normalize(ct_handle* h, int nsites, int d, int64_t* bond
                            double* const* mps_sites);
 
 /* <psi|H|psi> and <psi|psi> through left environments on the device
- * (expectation_value, environments.mojo:475-532).                           */
+ * (expectation_value, environments.mojo:475-532).  prec CT_PREC_FP64: SIMT
+ * FP64 GEMMs; CT_PREC_FP64_TC: the environment GEMMs on the BF16 tensor
+ * cores with FP64-accurate slicing (the mixed form's final Rayleigh
+ * quotient); CT_PREC_TF32X3 is taken as CT_PREC_FP64.                       */
 CT_API int ct_mps_expectation(ct_handle* h, int prec, int nsites, int d, const int64_t* mpo_dims,
                        const double* const* mpo_sites, const int64_t* bond_dims,
                        const double* const* mps_sites, double* energy_host, double* norm_sq_host);
@@ -341,7 +349,9 @@ CT_API int ct_kernel_timing_read(ct_handle* h, int64_t* launches, double* ms, do
 /* Same per class: 0 = TF32x3 GEMM launches (as above), 1 = whole H_eff applies
  * inside Lanczos (FLOPs = 4 D d^2 chi^3 + 4 D^2 d^3 chi^2 per apply, as in
  * ct_dmrg_stats.heff_flops), 2 = the applies of class 1 with the largest FLOP
- * count seen (the centre bond at chi_max).                                   */
+ * count seen (the centre bond at chi_max), 3 = the Krylov vector work of each
+ * reorthogonalised Lanczos step (algorithmic bytes in place of FLOPs), 4 = the
+ * FP64 GEMM launches on the BF16 tensor cores (2 M N K).                     */
 CT_API int ct_kernel_timing_read_class(ct_handle* h, int cls, int64_t* count, double* ms, double* flops);
 
 #ifdef __cplusplus
