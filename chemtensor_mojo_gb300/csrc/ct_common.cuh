@@ -112,7 +112,7 @@ static_assert(SC_MISC + CT_MAX_KRYLOV_SLOTS <= SC_SVD_FROB2 && SC_SPLIT_PIV + 2 
                   SC_ORTH_EMAX < SC_SVD_MINKEPT && SC_SVD_MINKEPT + 1 <= CT_NSCALARS,
               "scalar slots overlap or overflow d_scalars");
 // int slots inside d_flags
-enum { FL_STOP = 0, FL_NUMITER = 1, FL_ROT = 2, FL_CHI = 3, FL_TMP = 4, FL_CNT = 8 };
+enum { FL_STOP = 0, FL_NUMITER = 1, FL_ROT = 2, FL_CHI = 3, FL_TMP = 4, FL_CNT = 8, FL_REDO = 9 };
 
 #define CT_MAX_KRYLOV 128
 
@@ -271,8 +271,9 @@ int ct_lanczos_update(ct_handle* h, int64_t n, double* w, const double* vj, cons
 int ct_lanczos_next(ct_handle* h, int64_t n, const double* w, double* vnext, int j, const int* skip);
 int ct_lanczos_alpha(ct_handle* h, int64_t n, const double* vj, const double* w, int j,
                      const int* skip);
+// (gate != null: the kernels run only when *gate != 0, set by the FP32 pass)
 int ct_lanczos_reorth_pass(ct_handle* h, int64_t n, double* w, const double* V, int64_t ldv, int j,
-                           double beta_threshold, const int* skip);
+                           double beta_threshold, const int* skip, const int* gate = nullptr);
 int ct_lanczos_update_nonorm(ct_handle* h, int64_t n, double* w, const double* vj, const double* vjm1, int j,
                              const int* skip);
 // the same pass against an FP32 copy of the basis; v_{j+1} with its FP32 copy

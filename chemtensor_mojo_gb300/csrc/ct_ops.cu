@@ -255,9 +255,13 @@ int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, do
     double* V = ar.take<double>(N * (int64_t)max_iter);
     double* w = ar.take<double>(N);
     if (!V || !w) return CT_ERR_OOM;
-    // mixed form: FP32 copy of the basis for the reorthogonalisation pass
+    // mixed form: FP32 copy of the basis for the reorthogonalisation pass (CTDMRG_LANCZOS_FP32=0: FP64 basis)
+    static const bool fp32_basis = [] {
+        const char* e = getenv("CTDMRG_LANCZOS_FP32");
+        return !(e && e[0] == '0');
+    }();
     float* V32 = nullptr;
-    if (reorth && prec == CT_PREC_TF32X3) {
+    if (reorth && prec == CT_PREC_TF32X3 && fp32_basis) {
         V32 = ar.take<float>(N * (int64_t)max_iter);
         if (!V32) return CT_ERR_OOM;
     }
@@ -300,6 +304,8 @@ int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, do
             CT_TRY(ct_lanczos_update_nonorm(h, N, w, vj, vjm1, j, stop));
             if (V32) {
                 CT_TRY(ct_lanczos_reorth_pass32(h, N, w, V32, N, j, thr, stop));
+                // the FP64 pass again when the FP32 one removed much of w (gated on the device)
+                CT_TRY(ct_lanczos_reorth_pass(h, N, w, V, N, j, thr, stop, h->d_flags + FL_REDO));
                 CT_TRY(ct_lanczos_next32(h, N, w, V + (int64_t)(j + 1) * N, V32 + (int64_t)(j + 1) * N, j, stop));
             } else {
                 CT_TRY(ct_lanczos_reorth_pass(h, N, w, V, N, j, thr, stop));

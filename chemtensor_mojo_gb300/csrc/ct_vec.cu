@@ -266,8 +266,8 @@ __device__ __forceinline__ void cgs_dots_group(int64_t n, const double* __restri
 __global__ void __launch_bounds__(RT) cgs_dots_kernel(int64_t n, const double* __restrict__ w,
                                                       const double* __restrict__ V, int64_t ldv, int nvec, int vec2,
                                                       double* partials, unsigned* counter, double* coeff,
-                                                      const int* skip) {
-    if (ct_skip(skip)) return;
+                                                      const int* skip, const int* gate) {
+    if (ct_skip(skip) || (gate && *(volatile const int*)gate == 0)) return;
     __shared__ double sm[CGS_VB][RT / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int v0 = 0; v0 < nvec; v0 += CGS_VB) {
@@ -318,8 +318,8 @@ __global__ void __launch_bounds__(RT) cgs_update_kernel(int64_t n, double* __res
                                                         const double* __restrict__ V, int64_t ldv, int nvec, int vec2,
                                                         const double* coeff, double* partials, unsigned* counter,
                                                         double* scalars, int* flags, int j, double thr,
-                                                        const int* skip) {
-    if (ct_skip(skip)) return;
+                                                        const int* skip, const int* gate) {
+    if (ct_skip(skip) || (gate && *(volatile const int*)gate == 0)) return;
     __shared__ double sm[32];
     __shared__ double c[CT_MAX_KRYLOV];
     for (int v = threadIdx.x; v < nvec; v += RT) c[v] = coeff[v];
@@ -508,7 +508,17 @@ __global__ void __launch_bounds__(RT) cgs32_update_kernel(int64_t n, double* __r
     double s = 0.0;
     for (int b = threadIdx.x; b < (int)gridDim.x; b += RT) s += __ldcg(partials + b);
     s = ct_block_sum<RT>(s, sm);
+    double cc = 0.0;   // |sum_k c_k V_k|^2 = sum_k c_k^2 (orthonormal basis)
+    for (int v = threadIdx.x; v < nvec; v += RT) cc += coeff[v] * coeff[v];
+    cc = ct_block_sum<RT>(cc, sm);
     if (threadIdx.x == 0) {
+        // The FP32 correction leaves ~3e-7 |c| of the removed part in the new residual,
+        // i.e. ~3e-7 |c| / beta of orthogonality loss for v_{j+1}.  Up to |c| = 0.1 beta
+        // that stays near 3e-8, about the semi-orthogonality Lanczos needs; beyond it
+        // (a Krylov space close to exhausted, where w lies mostly inside the basis and
+        // |c| / beta reaches 1e5) the FP64 pass runs on the FP64 basis and decides
+        // beta and breakdown itself.
+        flags[FL_REDO] = (cc > 1e-2 * s) ? 1 : 0;
         const double b = sqrt(s);
         if (b < thr) {
             flags[FL_NUMITER] = j + 1;
@@ -881,7 +891,7 @@ int ct_lanczos_update(ct_handle* h, int64_t n, double* w, const double* vj, cons
 // reference recurrence has updated w; beta_j (or the breakdown stop) goes to the
 // scalar slots.  The caller then forms v_{j+1} = w / beta_j.
 int ct_lanczos_reorth_pass(ct_handle* h, int64_t n, double* w, const double* V, int64_t ldv, int j,
-                           double beta_threshold, const int* skip) {
+                           double beta_threshold, const int* skip, const int* gate) {
     const int nvec = j + 1;
     if (nvec > 64) return CT_ERR_UNSUPPORTED;
     int g = grid_for(h, n);
@@ -889,10 +899,11 @@ int ct_lanczos_reorth_pass(ct_handle* h, int64_t n, double* w, const double* V, 
     const int vec2 = ((n & 1) == 0 && (ldv & 1) == 0 && aligned16(w) && aligned16(V)) ? 1 : 0;
     unsigned* counter = reinterpret_cast<unsigned*>(h->d_flags + FL_CNT);
     double* coeff = h->d_scalars + SC_MISC;
-    cgs_dots_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, vec2, h->d_partials, counter, coeff, skip);
+    cgs_dots_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, vec2, h->d_partials, counter, coeff, skip, gate);
     ct_note_launch();
     cgs_update_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, vec2, coeff, h->d_partials, counter,
-                                               h->d_scalars, h->d_flags, j, beta_threshold, skip); ct_note_launch();
+                                               h->d_scalars, h->d_flags, j, beta_threshold, skip, gate);
+    ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }

@@ -235,6 +235,31 @@ def test_lanczos_reorth_matches_oracle(ctx, dims, prec):
         assert abs(E - E_ref) <= 1e-6 * max(1.0, abs(E_ref))
 
 
+@pytest.mark.parametrize("dims", [(1, 2, 4, 1, 3, 3), (2, 2, 3, 3, 3, 3), (3, 2, 2, 3, 3, 1), (2, 4, 2, 3, 3, 3)])
+def test_lanczos_mixed_exhausted_krylov(ctx, dims):
+    """Mixed form, reorthogonalised, on bonds whose whole space (N = Dl d^2 Dr <= 32) is smaller
+    than or equal to 24 Lanczos steps, as at the ends of a chain: the Krylov space closes, w after
+    the recurrence lies almost entirely inside the basis, and the FP32 pass alone would leave a
+    1e-7 residual along it that is not small against beta (ghost eigenvalues far below the
+    spectrum were measured).  The gated FP64 pass must take over: the energy equals the lowest
+    eigenvalue of the dense H_eff to 1e-6 and never lies below it by more."""
+    ct = ct_mod()
+    th, L, R, W1, W2 = _lanczos_case(101 + sum(dims), *dims)
+    Dl, d, Dr = dims[0], dims[1], dims[2]
+    n = Dl * d * d * Dr
+    H = np.zeros((n, n))
+    for i in range(n):
+        e = np.zeros(n)
+        e[i] = 1.0
+        H[:, i] = od.apply_two_site_heff(e.reshape(Dl, d, d, Dr), L, R, W1, W2).reshape(-1)
+    e0 = np.linalg.eigvalsh(0.5 * (H + H.T))[0]
+    E, _ = ct.lanczos_two_site_optimize(dt(ctx, th), dt(ctx, L), dt(ctx, R), ct.MPOSite(dt(ctx, W1)),
+                                        ct.MPOSite(dt(ctx, W2)), ctx, max_iter=24, tol=1e-10, prec="tf32x3",
+                                        max_rotations=0, reorth=True)
+    scale = max(1.0, np.abs(np.linalg.eigvalsh(0.5 * (H + H.T))).max())
+    assert abs(E - e0) <= 1e-6 * scale
+
+
 def test_lanczos_breakdown_matches_oracle(ctx):
     """Rank-deficient H_eff: the Krylov space closes early (beta below 100 n eps)."""
     ct = ct_mod()
