@@ -7,32 +7,40 @@
 // kind::f16 with BF16 operands and FP32 accumulation in TMEM:
 //
 //   * every row of A and of B is scaled by a power of two 2^e so that its
-//     entries satisfy |x| < 1, and cut into S = 7 slices of 8 bits with
-//     round-to-nearest digits:  x = sum_s a_s 2^{-8s} + r,  a_1 in [-256, 256],
-//     a_s in [-128, 128] for s > 1,  |r| <= 2^{-57}.  a_s 2^{-8s} is exact in
+//     entries satisfy |x| < 1, and cut into S = 8 slices of 7 bits with
+//     round-to-nearest digits:  x = sum_s a_s 2^{-7s} + r,  a_1 in [-128, 128],
+//     a_s in [-64, 64] for s > 1,  |r| <= 2^{-57}.  a_s 2^{-7s} is exact in
 //     BF16 (8 significant bits, FP32's exponent range);
-//   * a product of slices s and t is an integer times 2^{-8(s+t)}.  Summed over
-//     128 of K, the products of one level l = s + t stay below 2^24 (level 2:
-//     2^16 per term; level 5: four pairs of at most 2^15), so an FP32 accumulator
-//     holds them exactly and the tensor core's truncating adds lose nothing;
-//   * levels 2, 3, 4 and 5 get one exact accumulator each; levels 6..8, at
-//     2^{-32} and below relative to level 2, share a fifth whose rounding stays
-//     below 2^{-51} of the result; pairs with s + t > 8 (below 2^{-56}) are not
-//     formed.  28 BF16 products per FP64 product;
-//   * per 128 of K the epilogue combines the five accumulators with error-free
+//   * a product of slices s and t is an integer times 2^{-7(s+t)}.  Summed over
+//     512 of K, the products of one level l = s + t stay below 2^24 for l <= 6
+//     (level 2: 2^14 per term; level 6: five pairs, at most 7 * 2^12 per term),
+//     so an FP32 accumulator holds them exactly and the tensor core's truncating
+//     adds lose nothing;
+//   * levels 2..6 get one exact accumulator each; levels 7..9, at 2^{-35} and
+//     below relative to level 2, share a sixth whose rounding stays below 2^{-53}
+//     of the result; pairs with s + t > 9 (below 2^{-56}) are not formed.  36
+//     BF16 products per FP64 product;
+//   * per 512 of K the epilogue combines the six accumulators with error-free
 //     FP32 two-sums into hi + lo and adds both to FP64 registers; the result is
-//     scaled back by 2^{e_m + e_n} once per tile.
+//     scaled back by 2^{e_m + e_n} once per tile.  (7-bit slices and 512-wide
+//     chunks, not 8-bit and 128: the epilogue's FP64 adds and conversions, at
+//     1/64 of the FP32 rate, bound an 8-bit version -- FP64 pipe 59%, tensor pipe
+//     22% in an ncu capture of a 1024 x 2048 x 1024 product.)
 //
-// Accuracy (NumPy model of exactly this arithmetic, graded data with entries
-// spanning 1e-9 of the row maximum): |C - AB| <= 3e-15 |A||B| elementwise,
-// against 2.5e-15 for a plain FP64 GEMM of the same data.
+// Accuracy (NumPy model of exactly this arithmetic): |C - AB| <= 2.6e-15 |A||B|
+// elementwise on graded data with entries spanning 1e-18 of the row maximum
+// (2.5e-15 for a plain FP64 GEMM of the same data), 1.7e-16 on Gaussian data
+// (1.1e-16); the largest level sum met was 8.1e5 against the 2^24 limit.
 //
-// Kernel: one CTA per SM walks 128 x 32 tiles (consecutive CTAs share the A
+// Kernel: one CTA per SM walks 128 x 64 tiles (consecutive CTAs share the A
 // rows, which stay in L2); warp 0 issues TMA loads (64-byte swizzle, 32 BF16
-// of K per row, all 7 slices of A and of B per stage, 3 stages), one thread of
-// warp 1 issues the 56 MMAs (M128 N32 K16) of a K-block, and 8 epilogue warps
-// (two per TMEM lane quadrant, 16 columns each) drain the five accumulators of
-// a 128-wide chunk while the MMAs fill the other of two TMEM buffers.  Every
+// of K per row, all 8 slices of A and of B per stage, 2 stages), one thread of
+// warp 1 issues the 72 MMAs (M128 N64 K16) of a K-block, and 8 epilogue warps
+// (two per TMEM lane quadrant, 32 columns each) read the six accumulators of a
+// 512-wide chunk (384 TMEM columns, one buffer: the MMAs of the next chunk wait
+// only for the reads, ~1 us against ~20 us of MMAs) and add them in FP64.
+// (128 x 32 tiles with two TMEM buffers kept the tensor pipe at 24%: an N = 32
+// MMA is too short to fill it, ncu showing its issue pipe 87% busy.)  Every
 // wait is bounded (2 s), after which the kernel sets the status word, releases
 // TMEM and returns.
 #include <cuda.h>
@@ -48,27 +56,31 @@ PFN_cuTensorMapEncodeTiled_v12000 ct_tma_encoder();
 
 namespace {
 
-constexpr int OZ_S = 7;                                  // slices per operand
+constexpr int OZ_S = 8;                                  // slices per operand
+constexpr int OZ_BITS = 7;                               // bits per slice
+constexpr int OZ_MAXLEV = OZ_S + 1;                      // pairs s + t <= OZ_MAXLEV are formed
+constexpr int OZ_EXACT = 6;                              // levels 2..OZ_EXACT accumulate exactly
 constexpr int OZ_BM = 128;
-constexpr int OZ_BN = 32;
+constexpr int OZ_BN = 64;
 constexpr int OZ_BK = 32;                                // BF16 of K per 64-byte row
-constexpr int OZ_STAGES = 3;
-constexpr int OZ_KCH = 4;                                // k-blocks per exact chunk (128 of K)
-constexpr int OZ_G = 5;                                  // accumulator groups
+constexpr int OZ_STAGES = 2;
+constexpr int OZ_KCH = 16;                               // k-blocks per exact chunk (512 of K)
+constexpr int OZ_G = OZ_EXACT;                           // groups: levels 2..6 and one for 7..9
 constexpr int OZ_EPW = 2;                                // epilogue warps per lane quadrant
 constexpr int OZ_HC = OZ_BN / OZ_EPW;                    // columns per epilogue thread
+constexpr int OZ_HH = OZ_HC / 2;                         // ... handled in two halves
 constexpr int OZ_THREADS = 32 * (2 + 4 * OZ_EPW);
 constexpr int OZ_A_SLICE = OZ_BM * OZ_BK * 2;            // 8 KB
-constexpr int OZ_B_SLICE = OZ_BN * OZ_BK * 2;            // 2 KB
+constexpr int OZ_B_SLICE = OZ_BN * OZ_BK * 2;            // 4 KB
 constexpr int OZ_STAGE = OZ_S * (OZ_A_SLICE + OZ_B_SLICE);
 constexpr int OZ_TILE_BYTES = OZ_STAGES * OZ_STAGE;
 constexpr int OZ_SMEM = OZ_TILE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr int OZ_ACC_COLS = OZ_G * OZ_BN;                // TMEM columns per buffer
-constexpr int OZ_NBUF = 2;
+constexpr int OZ_NBUF = 1;                               // 6 groups x 64 columns fill 384 of 512
 constexpr int OZ_TMEM_COLS = 512;                        // power of two >= OZ_NBUF * OZ_ACC_COLS
 static_assert(OZ_NBUF * OZ_ACC_COLS <= OZ_TMEM_COLS, "TMEM budget");
 static_assert(OZ_SMEM <= 227 * 1024, "shared memory budget");
-static_assert(OZ_HC % 8 == 0, "epilogue loads 8 columns at a time");
+static_assert(OZ_HH % 8 == 0, "epilogue loads 8 columns at a time");
 
 // K-major operand, 64-byte swizzle: rows of 64 B, 8-row groups 512 B apart.
 __device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
@@ -196,7 +208,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                     tc_fence_after();
                     const uint32_t dt = tmem + (uint32_t)(b * OZ_ACC_COLS);
                     const int kb1 = kb0 + OZ_KCH < nkb ? kb0 + OZ_KCH : nkb;
-                    uint32_t started = 0;   // groups written in this chunk
                     for (int kb = kb0; kb < kb1; ++kb, ++g) {
                         const int s = g % OZ_STAGES;
                         const uint32_t ph = (uint32_t)(g / OZ_STAGES) & 1u;
@@ -207,22 +218,28 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                             break;
                         }
                         tc_fence_after();
+                        // descriptors built once per stage; every MMA adds a compile-time
+                        // offset (in 16-byte units) to the start-address field
                         const uint32_t a0 = smem_u32(smem + s * OZ_STAGE);
-                        const uint32_t b0 = a0 + OZ_S * OZ_A_SLICE;
+                        const uint64_t da = sw64_desc(a0), db = sw64_desc(a0 + OZ_S * OZ_A_SLICE);
+                        const uint32_t first = (kb == kb0) ? 1u : 0u;
 #pragma unroll
-                        for (int l = 2; l <= OZ_S + 1; ++l) {
-                            const int grp = l < 6 ? l - 2 : 4;
+                        for (int l = 2; l <= OZ_MAXLEV; ++l) {
+                            const int grp = l <= OZ_EXACT ? l - 2 : OZ_G - 1;
                             const uint32_t d = dt + (uint32_t)(grp * OZ_BN);
+                            // the group's first product in a chunk overwrites the accumulator
+                            const int l0 = l <= OZ_EXACT ? l : OZ_EXACT + 1;
+                            const int s_first = l0 - OZ_S > 1 ? l0 - OZ_S : 1;
 #pragma unroll
                             for (int sa = 1; sa <= OZ_S; ++sa) {
                                 const int tb = l - sa;
                                 if (tb < 1 || tb > OZ_S) continue;
 #pragma unroll
                                 for (int kk = 0; kk < 2; ++kk) {
-                                    const uint32_t acc = (started >> grp) & 1u;
-                                    mma_bf16(d, sw64_desc(a0 + (uint32_t)((sa - 1) * OZ_A_SLICE + kk * 32)),
-                                             sw64_desc(b0 + (uint32_t)((tb - 1) * OZ_B_SLICE + kk * 32)), idesc, acc);
-                                    started |= 1u << grp;
+                                    const bool fresh = (l == l0 && sa == s_first && kk == 0);
+                                    const uint32_t acc = fresh ? (first ^ 1u) : 1u;
+                                    mma_bf16(d, da + (uint64_t)((((sa - 1) * OZ_A_SLICE) + kk * 32) >> 4),
+                                             db + (uint64_t)((((tb - 1) * OZ_B_SLICE) + kk * 32) >> 4), idesc, acc);
                                 }
                             }
                         }
@@ -254,29 +271,43 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 __syncwarp();
                 tc_fence_after();
                 const uint32_t tq = tmem + (uint32_t)(b * OZ_ACC_COLS + hf * OZ_HC) + ((uint32_t)(q * 32) << 16);
-                uint32_t v[OZ_G][OZ_HC];
+                // this thread's OZ_HC columns in two halves; per half the six groups are
+                // folded into hi + lo by two-sums, largest level first
 #pragma unroll
-                for (int grp = 0; grp < OZ_G; ++grp)
+                for (int half = 0; half < 2; ++half) {
+                    float hi[OZ_HH], lo[OZ_HH];
 #pragma unroll
-                    for (int q8 = 0; q8 < OZ_HC; q8 += 8)
-                        tmem_ld8_nowait(tq + (uint32_t)(grp * OZ_BN + q8),
-                                        *reinterpret_cast<uint32_t(*)[8]>(&v[grp][q8]));
-                tmem_wait_ld();
-                tc_fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&acc_empty[b]);
+                    for (int grp = 0; grp < OZ_G; ++grp) {
+                        uint32_t v[OZ_HH];
 #pragma unroll
-                for (int j = 0; j < OZ_HC; ++j) {
-                    float hi = __uint_as_float(v[0][j]), lo = 0.f;
+                        for (int q8 = 0; q8 < OZ_HH; q8 += 8)
+                            tmem_ld8_nowait(tq + (uint32_t)(grp * OZ_BN + half * OZ_HH + q8),
+                                            *reinterpret_cast<uint32_t(*)[8]>(&v[q8]));
+                        tmem_wait_ld();
 #pragma unroll
-                    for (int grp = 1; grp < OZ_G; ++grp) {
-                        float s, e;
-                        two_sum(hi, __uint_as_float(v[grp][j]), s, e);
-                        hi = s;
-                        lo = __fadd_rn(lo, e);
+                        for (int j = 0; j < OZ_HH; ++j) {
+                            const float x = __uint_as_float(v[j]);
+                            if (grp == 0) {
+                                hi[j] = x;
+                                lo[j] = 0.f;
+                            } else {
+                                float sm, e;
+                                two_sum(hi[j], x, sm, e);
+                                hi[j] = sm;
+                                lo[j] = __fadd_rn(lo[j], e);
+                            }
+                        }
                     }
-                    acc[j] += (double)hi;
-                    acc[j] += (double)lo;
+                    if (half == 1) {   // every column read: the MMAs may overwrite the buffer
+                        tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(&acc_empty[b]);
+                    }
+#pragma unroll
+                    for (int j = 0; j < OZ_HH; ++j) {
+                        acc[half * OZ_HH + j] += (double)hi[j];
+                        acc[half * OZ_HH + j] += (double)lo[j];
+                    }
                 }
             }
             if (!ok) break;
@@ -353,15 +384,42 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(OzSrc a, int64_t Rp, int6
         }
     }
     __syncthreads();
+    // Digits from the bit pattern with integer arithmetic (FP64 issues at 1/64 of the
+    // FP32 rate here): X = round(x * 2^56) with x = v 2^-e, |X| < 2^56, then balanced
+    // base-2^7 digits, most significant first, d = round(Y / 2^k), Y -= d 2^k:
+    // X = sum_s d_s 2^(56 - 7s) exactly, |d_1| <= 128, |d_s| <= 64 for s > 1.
+    constexpr int FRAC = OZ_S * OZ_BITS;   // 56 fractional bits
     for (int dy = ty; dy < 32; dy += 8) {
         const int64_t r = r0 + dy, k = k0 + tx;
         if (r >= Rp || k >= ldk) continue;
-        double x = (r < a.R) ? ldexp(tile[dy][tx], -ex[r]) : 0.0;   // |x| < 1, exact
+        long long X = 0;
+        const double v = (r < a.R) ? tile[dy][tx] : 0.0;
+        if (v != 0.0) {
+            const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+            int ev = (int)((bits >> 52) & 0x7FF);
+            unsigned long long m = bits & ((1ull << 52) - 1);
+            if (ev == 0) ev = 1;           // subnormal
+            else m |= 1ull << 52;
+            // v = m 2^(ev - 1075), so x 2^56 = m 2^sh with sh <= 3 (|x| < 1)
+            const int sh = ev - 1075 - ex[r] + FRAC;
+            unsigned long long u = 0;
+            if (sh >= 0) u = m << sh;
+            else if (sh > -63) u = (m + (1ull << (-sh - 1))) >> (-sh);
+            X = (bits >> 63) ? -(long long)u : (long long)u;
+        }
 #pragma unroll
         for (int s = 0; s < OZ_S; ++s) {
-            const double d = rint(x * 256.0);                     // x * 256 exact
-            out[((int64_t)s * Rp + r) * ldk + k] = __float2bfloat16_rn((float)ldexp(d, -8 * (s + 1)));
-            x = x * 256.0 - d;                                     // exact, |x| <= 1/2
+            const int sh = FRAC - OZ_BITS * (s + 1);
+            long long d;
+            if (sh > 0) {
+                d = (X + (1ll << (sh - 1))) >> sh;
+                X -= d << sh;
+            } else {
+                d = X;
+            }
+            // d 2^(-7(s+1)) is exact in FP32 and in BF16
+            out[((int64_t)s * Rp + r) * ldk + k] = __float2bfloat16_rn(__int2float_rn((int)d) *
+                                                                       __int_as_float((127 - OZ_BITS * (s + 1)) << 23));
         }
     }
 }

@@ -20,11 +20,11 @@
  *   CT_PREC_TF32X3  contractions on tcgen05 tensor cores in TF32 with
  *                   3xTF32 split compensation and FP32 accumulation; all
  *                   storage, Lanczos, eigensolve, SVD and reductions FP64.
- *   CT_PREC_FP64_TC (ct_gemm only) FP64 products emulated on the BF16
- *                   tensor cores: each operand row cut into 7 exact 8-bit
- *                   slices, 28 slice products per FP64 product accumulated
- *                   exactly in FP32 per 128 of K, combined in FP64; about as
- *                   accurate as an FP64 GEMM (3e-15 of |A||B|).
+ *   CT_PREC_FP64_TC (ct_gemm, ct_mps_expectation) FP64 products emulated on
+ *                   the BF16 tensor cores: each operand row cut into 8 exact
+ *                   7-bit slices, 36 slice products per FP64 product summed
+ *                   exactly in FP32 per 512 of K, combined in FP64; about as
+ *                   accurate as an FP64 GEMM (~3e-15 of |A||B|).
  */
 #ifndef CTDMRG_H
 #define CTDMRG_H

@@ -1,7 +1,7 @@
 """FP64 GEMM emulated on the BF16 tensor cores (ct_gemm with CT_PREC_FP64_TC).
 
-Each operand row is cut into 7 exact 8-bit slices after a power-of-two row
-scaling; 28 slice products per FP64 product are summed exactly in FP32 per 128
+Each operand row is cut into 8 exact 7-bit slices after a power-of-two row
+scaling; 36 slice products per FP64 product are summed exactly in FP32 per 512
 of K and combined in FP64.  The error bound checked is elementwise against
 sum_k |A_ik||B_kj| (the scale of an FP64 GEMM's own rounding): 2e-14, with the
 plain FP64 GEMM of the same data held to the same bound for comparison.  The
