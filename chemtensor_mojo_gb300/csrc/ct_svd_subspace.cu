@@ -63,7 +63,12 @@
 
 namespace {
 
-constexpr int CH_NB = 64;            // Cholesky block
+// Cholesky block.  A leaf factors and inverts one CH_NB x CH_NB block in one CTA
+// (~145 us for 64 x 64, latency-bound: a serial FP64 square root and reciprocal
+// and three barriers per column).  32 x 32 leaves were measured slower overall
+// (7.4 vs 6.4 ms per chi=1024 warm split): the extra recursion level's small
+// products cost more than the leaves saved.
+constexpr int CH_NB = 64;
 constexpr int FL_CHOL_FAIL = 100;    // d_flags slot: non-positive pivot seen
 constexpr int FL_DEF_COUNT = 101;    // d_flags slot: rows marked for replacement in a first pass
 // smallest accepted Cholesky pivot of a first pass (the squared share of a
@@ -187,13 +192,14 @@ __global__ void __launch_bounds__(256) chol_diag_kernel(double* G, double* Linv,
         // the row loop is uniform across the warp (its 8 columns start at 8w);
         // a column takes part once i reaches it
         const int col = t >> 2, q = t & 3, first = (t >> 5) * 8;
+        const bool live = col < CH_NB;   // 256 threads cover 64 columns; a 32-wide block uses half
         for (int i = first; i < CH_NB; ++i) {
             T s = (T)0;
-            if (i >= col)
+            if (live && i >= col)
                 for (int l = col + q; l < i; l += 4) s += A[i][l] * X[l][col];
             s += __shfl_xor_sync(0xffffffffu, s, 1);
             s += __shfl_xor_sync(0xffffffffu, s, 2);
-            if (q == 0 && i >= col) X[i][col] = (((i == col) ? (T)1 : (T)0) - s) * dinv[i];
+            if (live && q == 0 && i >= col) X[i][col] = (((i == col) ? (T)1 : (T)0) - s) * dinv[i];
             __syncwarp();
         }
     }
