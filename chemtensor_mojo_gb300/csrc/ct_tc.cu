@@ -534,7 +534,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 //     four buffers the MMA thread is three chunks ahead, which hides the
 //     commit -> epilogue -> release latency of a short chunk); a tile's stores
 //     overlap the next tile's first chunks.
-__host__ __device__ constexpr int tc_chunk_epw(int BN) { return BN >= 256 ? 2 : 4; }
+__host__ __device__ constexpr int tc_chunk_epw(int BN) { return BN >= 192 ? 2 : 4; }
+// tcgen05.alloc takes a power of two (>= 32) of columns
+__host__ __device__ constexpr uint32_t tc_pow2_cols(int n) { return n <= 32 ? 32u : 2u * tc_pow2_cols((n + 1) / 2); }
 __host__ __device__ constexpr int tc_chunk_threads(int BN) { return 32 * (2 + 4 * tc_chunk_epw(BN)); }
 
 
@@ -550,6 +552,7 @@ __global__ void __launch_bounds__(tc_chunk_threads(BN), 1)
     constexpr int EPW = tc_chunk_epw(BN);
     constexpr int HC = BN / EPW;   // columns per epilogue warp
     constexpr int NB = 512 / BN;   // chunk accumulators in TMEM (all 512 columns)
+    constexpr uint32_t TMEM_COLS = tc_pow2_cols(NB * BN);
     if (ct_skip(skip)) return;
     extern __shared__ uint8_t tc_smem_raw[];
     uint8_t* smem = tc_smem_raw + ((1024u - (smem_u32(tc_smem_raw) & 1023u)) & 1023u);
@@ -580,7 +583,7 @@ __global__ void __launch_bounds__(tc_chunk_threads(BN), 1)
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"((uint32_t)(NB * BN))
+                     "r"(TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -683,7 +686,7 @@ __global__ void __launch_bounds__(tc_chunk_threads(BN), 1)
                 // LB columns per wait: several TMEM loads in flight before one
                 // tcgen05.wait::ld (fewer for the wide tile, whose 128 sums leave
                 // room for 32 more registers only)
-                constexpr int LB = HC >= 128 ? 32 : HC;
+                constexpr int LB = HC >= 96 ? 32 : HC;
 #pragma unroll
                 for (int cc = 0; cc < HC; cc += LB) {
                     uint32_t r[LB];
@@ -751,7 +754,7 @@ __global__ void __launch_bounds__(tc_chunk_threads(BN), 1)
     __syncthreads();
     if (warp == 1) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)(NB * BN))
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS)
                      : "memory");
     }
 }
@@ -1023,15 +1026,29 @@ int tc_kchunk() {
 // wide tile's fixed per-tile cost (pipeline fill, epilogue) is spread over twice the MMAs, measured
 // as 1.12x the narrow tile's rate per flop (5120x4096x1024: 0.164 vs 0.166 ms; 2048x2048x1024:
 // 0.037 vs 0.041 ms); at K = 5120 both run at the same rate per flop.
-int tc_pick_bn(int64_t M, int64_t N, int64_t K, int num_sms) {
+int tc_pick_bn(int64_t M, int64_t N, int64_t K, int num_sms, bool chunked) {
     const int mode = tc_bn_mode();
     if (mode) return mode;
     if (N <= 128) return 128;
     const int64_t tm = ct_cdiv(M, TC_BM);
-    const int64_t w128 = ct_cdiv(tm * ct_cdiv(N, 128), num_sms);
-    const int64_t w256 = ct_cdiv(tm * ct_cdiv(N, 256), num_sms);
     const double wide_speed = K <= 2048 ? 1.12 : 1.0;
-    return (double)w256 * 256.0 / wide_speed < (double)w128 * 128.0 ? 256 : 128;
+    auto cost = [&](int bn) {
+        const int64_t waves = ct_cdiv(tm * ct_cdiv(N, bn), num_sms);
+        return (double)waves * (double)bn / (bn > 128 ? wide_speed : 1.0);
+    };
+    int best = 128;
+    double c = cost(128);
+    // 128 x 192 tiles (chunked kernel only): a GEMM of 640 wide tiles (4.2 waves on 152 SMs)
+    // becomes 880 three-quarter tiles (5.8 waves)
+    for (int bn : {256, 192}) {
+        if (bn == 192 && !chunked) continue;
+        const double cb = cost(bn);
+        if (cb < c) {
+            c = cb;
+            best = bn;
+        }
+    }
+    return best;
 }
 
 struct SplitOperand {
@@ -1061,6 +1078,10 @@ int tc_gemm_run(ct_handle* h, const SplitOperand& A, const SplitOperand& B, int6
     }
     const int64_t tiles = ct_cdiv(N, BN) * ct_cdiv(M, TC_BM);
     const int kc = tc_kchunk();
+    if (BN == 192 && !(tc_use_persistent() && kc > 0 && !tc_use_stream_k())) {
+        ct_seterr(h, "128 x 192 tiles exist only in the chunked kernel");
+        return CT_ERR_UNSUPPORTED;
+    }
     if (tc_use_persistent() && kc > 0 && !tc_use_stream_k()) {
         const int64_t grid = tiles < h->num_sms ? tiles : h->num_sms;
         tc_gemm_chunk_kernel<BN, STAGES><<<(unsigned)grid, tc_chunk_threads(BN), L::TOTAL, h->stream>>>(
@@ -1115,8 +1136,10 @@ int tc_gemm_launch(ct_handle* h, const SplitOperand& A, const SplitOperand& B, i
     }
     int slot = -1;
     CT_TRY(ct_ktime_begin(h, KT_TC_GEMM, 2.0 * (double)M * (double)N * (double)A.ldk, &slot));
-    const int bn = tc_pick_bn(M, N, A.ldk, h->num_sms);
+    const bool chunked = tc_use_persistent() && tc_kchunk() > 0 && !tc_use_stream_k();
+    const int bn = tc_pick_bn(M, N, A.ldk, h->num_sms, chunked);
     const int rc = bn == 256 ? tc_gemm_run<256, GEMM_STAGES_W>(h, A, B, M, N, e, skip)
+                 : bn == 192 ? tc_gemm_run<192, GEMM_STAGES_W>(h, A, B, M, N, e, skip)
                              : tc_gemm_run<128, GEMM_STAGES_N>(h, A, B, M, N, e, skip);
     CT_TRY(rc);
     CT_TRY(ct_ktime_end(h, slot));
