@@ -164,6 +164,8 @@ int ct_destroy(ct_handle* h) {
     cudaFree(h->oz_ws);
     cudaFree(h->tc_sk_part);
     cudaFree(h->tc_sk_flag);
+    cudaFree(h->tc_hy_part);
+    cudaFree(h->tc_hy_cnt);
     cudaFree(h->d_status);
     cudaFree(h->d_scalars);
     cudaFree(h->d_partials);

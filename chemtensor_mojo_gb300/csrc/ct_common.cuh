@@ -61,6 +61,13 @@ struct ct_handle {
     float* tc_sk_part = nullptr;
     int* tc_sk_flag = nullptr;
     int64_t tc_sk_floats = 0;       // floats held by tc_sk_part
+    // stream-K partials and arrival counters of the chunked tensor-core GEMM's hybrid
+    // schedule (grown on demand after a stream synchronisation, freed by ct_destroy)
+    float* tc_hy_part = nullptr;
+    int64_t tc_hy_part_floats = 0;
+    unsigned long long* tc_hy_cnt = nullptr;
+    int64_t tc_hy_cnt_n = 0;
+    unsigned tc_hy_epoch = 0;       // tag of the last launch (never 0 once used)
     // tensor-core path state
     bool tc_checked = false;
     bool tc_ok = false;

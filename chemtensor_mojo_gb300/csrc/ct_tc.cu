@@ -520,7 +520,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // warps add the chunks in FP32 registers with round-to-nearest, whose errors
 // have no sign preference.  The bias left is that of one chunk, kc times that of
 // one 32-wide k-block (~1.8e-7).
-//   * one CTA per SM walks tiles c, c + G, ... (no stream-K);
+//   * one CTA per SM; the schedule is hybrid (TcHybrid below): whole tiles
+//     c, c + G, ... for the full waves, then the last partial wave's k-blocks
+//     shared out evenly over the CTAs (stream-K);
 //   * warps: 0 TMA producer, 1 TMEM allocator + MMA issuer, then 4 EPW epilogue
 //     warps; epilogue warp w reads TMEM lane quadrant w % 4 (the quadrant a warp
 //     may access) and column group (w - 2) / 4 of the tile, holding BN / EPW
@@ -539,6 +541,92 @@ __host__ __device__ constexpr int tc_chunk_epw(int BN) { return BN >= 192 ? 2 : 
 __host__ __device__ constexpr uint32_t tc_pow2_cols(int n) { return n <= 32 ? 32u : 2u * tc_pow2_cols((n + 1) / 2); }
 __host__ __device__ constexpr int tc_chunk_threads(int BN) { return 32 * (2 + 4 * tc_chunk_epw(BN)); }
 
+// Hybrid schedule.  Tiles [0, tiles_dp) (whole waves, tiles_dp a multiple of G)
+// go round-robin, one whole tile per turn, so that the CTAs of a wave read the
+// same operand rows at the same time (L2 reuse).  The k-blocks of the remaining
+// tiles, units = (tiles - tiles_dp) * nkb of them in tile-major order, are cut
+// into gsk equal contiguous ranges, CTA c < gsk taking [c*units/gsk,
+// (c+1)*units/gsk); a tile whose k-blocks span several ranges is a set of
+// pieces, numbered in k order.  Each piece's epilogue warp (region = lane
+// quadrant x column group) stores its FP32 sums to its own partial slot, then
+// counts itself in the tile-region's arrival counter; the warp that arrives
+// last adds all pieces' partials in piece order and stores the result.  No CTA
+// waits for another, and the sum is the same FP32 expression whichever piece
+// arrives last (deterministic).  Counters carry the launch's epoch in their high
+// half, so a counter left by an earlier (even an aborted) launch reads as zero
+// and no reset is needed between launches.
+struct TcHybrid {
+    int tiles_dp;               // whole-tile part; == tiles when there is no stream-K part
+    int gsk;                    // CTAs sharing the stream-K units (0: none)
+    int64_t units;              // (tiles - tiles_dp) * nkb
+    int maxp;                   // partial slots per stream-K tile (most pieces of any tile)
+    unsigned epoch;             // nonzero tag of this launch
+    float* part;                // [(tiles - tiles_dp) * maxp][regions][HC / 4][32] float4
+    unsigned long long* cnt;    // [(tiles - tiles_dp) * regions]: epoch << 32 | arrivals
+};
+
+struct TcPiece {
+    int t, kb0, kb1;   // tile, k-block range
+    int p, n;          // piece index, pieces of the tile (n = 1: the whole tile)
+    int st;            // stream-K tile index (t - tiles_dp), -1 for a whole tile
+};
+
+// Walks CTA c's work in processing order: its whole tiles, then its stream-K range.
+struct TcCursor {
+    int t;
+    int64_t u, ue;
+    __device__ TcCursor(const TcHybrid& hy, int c) : t(c), u(0), ue(0) {
+        if (c < hy.gsk) {
+            u = (int64_t)c * hy.units / hy.gsk;
+            ue = (int64_t)(c + 1) * hy.units / hy.gsk;
+        }
+    }
+    __device__ bool next(const TcHybrid& hy, int nkb, int G, int c, TcPiece& w) {
+        if (t < hy.tiles_dp) {
+            w.t = t;
+            w.kb0 = 0;
+            w.kb1 = nkb;
+            w.p = 0;
+            w.n = 1;
+            w.st = -1;
+            t += G;
+            return true;
+        }
+        if (u >= ue) return false;
+        const int st = (int)(u / nkb);
+        const int k0 = (int)(u - (int64_t)st * nkb);
+        const int64_t left = ue - u;
+        const int k1 = left < nkb - k0 ? k0 + (int)left : nkb;
+        // owner of unit x: the largest c with c*units/gsk <= x, i.e. ((x+1)*gsk - 1) / units
+        const int64_t base = (int64_t)st * nkb;
+        const int cf = (int)(((base + 1) * hy.gsk - 1) / hy.units);
+        const int cl = (int)(((base + nkb) * hy.gsk - 1) / hy.units);
+        w.t = hy.tiles_dp + st;
+        w.kb0 = k0;
+        w.kb1 = k1;
+        w.p = c - cf;
+        w.n = cl - cf + 1;
+        w.st = st;
+        u += k1 - k0;
+        return true;
+    }
+};
+
+// Count one arrival of this launch (epoch) at *p; returns the arrivals so far
+// including this one, 0 if the CAS loop did not settle (it needs at most one
+// retry per other piece of the tile).
+__device__ __forceinline__ unsigned tc_arrive(unsigned long long* p, unsigned epoch) {
+    unsigned long long old = *(volatile unsigned long long*)p;
+    for (int i = 0; i < 1024; ++i) {
+        const unsigned cnt = (unsigned)(old >> 32) == epoch ? (unsigned)old : 0u;
+        const unsigned long long nw = ((unsigned long long)epoch << 32) | (unsigned long long)(cnt + 1u);
+        const unsigned long long prev = atomicCAS(p, old, nw);
+        if (prev == old) return cnt + 1u;
+        old = prev;
+    }
+    return 0u;
+}
+
 
 // Registers: each SM sub-partition holds 16K of them; 10 warps put 3 on some
 // sub-partitions (168 per thread), 18 warps put 5 (96 per thread, enough for 32
@@ -547,7 +635,7 @@ template <int BN, int STAGES>
 __global__ void __launch_bounds__(tc_chunk_threads(BN), 1)
     tc_gemm_chunk_kernel(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
                          const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl, int M,
-                         int N, int Kpad, int kc, TcEpi epi, const int* skip, int* status) {
+                         int N, int Kpad, int kc, TcEpi epi, TcHybrid hy, const int* skip, int* status) {
     using L = TcSmem<BN, STAGES>;
     constexpr int EPW = tc_chunk_epw(BN);
     constexpr int HC = BN / EPW;   // columns per epilogue warp
@@ -565,7 +653,6 @@ __global__ void __launch_bounds__(tc_chunk_threads(BN), 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tiles_n = (N + BN - 1) / BN;
-    const int tiles = tiles_n * ((M + TC_BM - 1) / TC_BM);
     const int nkb = Kpad / TC_BK;
     const int c = blockIdx.x, G = gridDim.x;
 
@@ -596,9 +683,11 @@ __global__ void __launch_bounds__(tc_chunk_threads(BN), 1)
         if (lane == 0) {
             int g = 0;
             bool ok = true;
-            for (int t = c; t < tiles && ok; t += G) {
-                const int m0 = (t / tiles_n) * TC_BM, n0 = (t % tiles_n) * BN;
-                for (int kb = 0; kb < nkb; ++kb, ++g) {
+            TcCursor cur(hy, c);
+            TcPiece w;
+            while (ok && cur.next(hy, nkb, G, c, w)) {
+                const int m0 = (w.t / tiles_n) * TC_BM, n0 = (w.t % tiles_n) * BN;
+                for (int kb = w.kb0; kb < w.kb1; ++kb, ++g) {
                     const int s = g % STAGES;
                     const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
                     if (g >= STAGES && !mbar_wait(&empty[s], ph ^ 1u, abort_flag)) {
@@ -622,8 +711,10 @@ __global__ void __launch_bounds__(tc_chunk_threads(BN), 1)
             constexpr uint32_t idesc = idesc_tf32(TC_BM, BN);
             int g = 0, gc = 0;
             bool ok = true;
-            for (int t = c; t < tiles && ok; t += G) {
-                for (int kb0 = 0; kb0 < nkb && ok; kb0 += kc, ++gc) {
+            TcCursor cur(hy, c);
+            TcPiece w;
+            while (ok && cur.next(hy, nkb, G, c, w)) {
+                for (int kb0 = w.kb0; kb0 < w.kb1 && ok; kb0 += kc, ++gc) {
                     const int b = gc % NB, u = gc / NB;
                     if (u > 0 && !mbar_wait(&acc_empty[b], (uint32_t)((u - 1) & 1), abort_flag)) {
                         *abort_flag = 1;
@@ -633,7 +724,7 @@ __global__ void __launch_bounds__(tc_chunk_threads(BN), 1)
                     }
                     tc_fence_after();
                     const uint32_t dt = tmem + (uint32_t)(b * BN);
-                    const int kb1 = kb0 + kc < nkb ? kb0 + kc : nkb;
+                    const int kb1 = kb0 + kc < w.kb1 ? kb0 + kc : w.kb1;
                     for (int kb = kb0; kb < kb1; ++kb, ++g) {
                         const int s = g % STAGES;
                         const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
@@ -669,10 +760,12 @@ __global__ void __launch_bounds__(tc_chunk_threads(BN), 1)
         float sum[HC];
         int gc = 0;
         bool ok = true;
-        for (int t = c; t < tiles && ok; t += G) {
+        TcCursor cur(hy, c);
+        TcPiece w;
+        while (ok && cur.next(hy, nkb, G, c, w)) {
 #pragma unroll
             for (int j = 0; j < HC; ++j) sum[j] = 0.f;
-            for (int kb0 = 0; kb0 < nkb; kb0 += kc, ++gc) {
+            for (int kb0 = w.kb0; kb0 < w.kb1; kb0 += kc, ++gc) {
                 const int b = gc % NB, u = gc / NB;
                 if (!mbar_wait(&acc_full[b], (uint32_t)(u & 1), abort_flag)) {
                     *abort_flag = 1;
@@ -686,7 +779,7 @@ __global__ void __launch_bounds__(tc_chunk_threads(BN), 1)
                 // LB columns per wait: several TMEM loads in flight before one
                 // tcgen05.wait::ld (fewer for the wide tile, whose 128 sums leave
                 // room for 32 more registers only)
-                constexpr int LB = HC >= 96 ? 32 : HC;
+                constexpr int LB = HC >= 96 ? (HC % 32 == 0 ? 32 : 16) : HC;
 #pragma unroll
                 for (int cc = 0; cc < HC; cc += LB) {
                     uint32_t r[LB];
@@ -702,8 +795,66 @@ __global__ void __launch_bounds__(tc_chunk_threads(BN), 1)
                 if (lane == 0) mbar_arrive(&acc_empty[b]);
             }
             if (!ok) break;
-            const int m0 = (t / tiles_n) * TC_BM;
-            const int n0 = (t % tiles_n) * BN + hf * HC;
+            if (w.n > 1) {
+                // a piece of a stream-K tile: FP32 sums to this piece's slot (lane-interleaved
+                // float4, so a warp's store covers 512 contiguous bytes), then the arrival count
+                constexpr int NREG = 4 * EPW;
+                constexpr int64_t REG4 = (int64_t)(HC / 4) * 32;       // float4 per region
+                const int region = warp - 2;
+                if (w.n > hy.maxp) {
+                    *abort_flag = 1;
+                    ct_set_status(status, CT_ERR_CUDA);
+                    ok = false;
+                    break;
+                }
+                float4* slot0 = (float4*)hy.part + ((int64_t)w.st * hy.maxp * NREG + region) * REG4 + lane;
+                float4* mine = slot0 + (int64_t)w.p * NREG * REG4;
+#pragma unroll
+                for (int j4 = 0; j4 < HC / 4; ++j4)
+                    __stcg(mine + j4 * 32, make_float4(sum[4 * j4], sum[4 * j4 + 1], sum[4 * j4 + 2], sum[4 * j4 + 3]));
+                __threadfence();
+                __syncwarp();
+                unsigned arrived = 0;
+                if (lane == 0) {
+                    arrived = tc_arrive(hy.cnt + (int64_t)w.st * NREG + region, hy.epoch);
+                    __threadfence();
+                }
+                arrived = __shfl_sync(0xffffffffu, arrived, 0);
+                if (arrived == 0) {
+                    *abort_flag = 1;
+                    ct_set_status(status, CT_ERR_CUDA);
+                    ok = false;
+                    break;
+                }
+                if ((int)arrived < w.n) continue;   // a later piece stores the tile
+                __threadfence();
+                // the last piece: sum the n partials in piece order, LG columns at a time
+                constexpr int LG = HC >= 128 ? 32 : 16;
+#pragma unroll
+                for (int cg = 0; cg < HC; cg += LG) {
+#pragma unroll
+                    for (int j4 = 0; j4 < LG / 4; ++j4) {
+                        const float4 v = __ldcg(slot0 + (cg / 4 + j4) * 32);
+                        sum[cg + 4 * j4] = v.x;
+                        sum[cg + 4 * j4 + 1] = v.y;
+                        sum[cg + 4 * j4 + 2] = v.z;
+                        sum[cg + 4 * j4 + 3] = v.w;
+                    }
+                    for (int q = 1; q < w.n; ++q) {
+                        const float4* sq = slot0 + (int64_t)q * NREG * REG4;
+#pragma unroll
+                        for (int j4 = 0; j4 < LG / 4; ++j4) {
+                            const float4 v = __ldcg(sq + (cg / 4 + j4) * 32);
+                            sum[cg + 4 * j4] += v.x;
+                            sum[cg + 4 * j4 + 1] += v.y;
+                            sum[cg + 4 * j4 + 2] += v.z;
+                            sum[cg + 4 * j4 + 3] += v.w;
+                        }
+                    }
+                }
+            }
+            const int m0 = (w.t / tiles_n) * TC_BM;
+            const int n0 = (w.t % tiles_n) * BN + hf * HC;
             const int64_t m = (int64_t)m0 + row;
             if (m >= M) continue;
             const int64_t rbase = (m / epi.M0) * epi.sCm1 + (m % epi.M0) * epi.sCm0;
@@ -977,10 +1128,10 @@ int make_map(ct_handle* h, CUtensorMap* m, const float* base, int64_t rows, int6
     return CT_OK;
 }
 
-// Tile shapes of the GEMM: 128 x 128 with a 3-stage ring (64 KB stages), or 128 x 256 with a
-// 2-stage ring (96 KB stages).  The wide tile reads 25% fewer operand bytes from shared memory
-// and L2 per MMA flop; the narrow one leaves smaller partial waves.  CTDMRG_TC_BN=128 or 256
-// forces one; otherwise tc_pick_bn chooses per shape.
+// Tile shapes of the GEMM: 128 x 128 with a 3-stage ring (64 KB stages), or 128 x 192 / 128 x 256
+// with a 2-stage ring (80 / 96 KB stages; 192 in the chunked kernel only).  The wide tile reads
+// 25% fewer operand bytes from shared memory and L2 per MMA flop; the narrow one leaves smaller
+// partial waves.  CTDMRG_TC_BN=128, 192 or 256 forces one; otherwise tc_pick_bn chooses per shape.
 constexpr int GEMM_STAGES_N = 3;
 constexpr int GEMM_STAGES_W = 2;
 
@@ -990,7 +1141,7 @@ int tc_bn_mode() {
     const char* e = getenv("CTDMRG_TC_BN");
     if (!e) return 0;
     const int b = atoi(e);
-    return (b == 128 || b == 256) ? b : 0;
+    return (b == 128 || b == 192 || b == 224 || b == 256) ? b : 0;
 }
 
 // persistent kernel by default; CTDMRG_TC_TILE_PER_CTA=1 selects the one-tile-per-CTA kernel
@@ -1022,26 +1173,110 @@ int tc_kchunk() {
     return k < 0 ? 0 : (k > 1024 ? 1024 : k);
 }
 
-// Wide tiles when their whole waves cost less.  Time per tile ~ BN at equal K; at K <= 2048 the
-// wide tile's fixed per-tile cost (pipeline fill, epilogue) is spread over twice the MMAs, measured
-// as 1.12x the narrow tile's rate per flop (5120x4096x1024: 0.164 vs 0.166 ms; 2048x2048x1024:
-// 0.037 vs 0.041 ms); at K = 5120 both run at the same rate per flop.
-int tc_pick_bn(int64_t M, int64_t N, int64_t K, int num_sms, bool chunked) {
+// The chunked kernel's hybrid schedule (TcHybrid): on unless CTDMRG_TC_HYBRID=0, read on every
+// launch like CTDMRG_TC_BN.
+bool tc_hybrid_on() {
+    const char* e = getenv("CTDMRG_TC_HYBRID");
+    return !(e && e[0] == '0');
+}
+
+// Plans the stream-K part for `tiles` tiles of nkb k-blocks on G SMs.  False (hy: whole tiles
+// only) when the last wave is full, when ranges of at least max(8, 2 kc) k-blocks would still be
+// whole tiles, or when the shared-out last wave would not be clearly shorter than one tile
+// (its longest range above 0.85 nkb).
+bool tc_plan_hybrid(int64_t tiles, int G, int64_t nkb, int kc, TcHybrid& hy) {
+    hy = TcHybrid{};
+    hy.tiles_dp = (int)tiles;
+    hy.maxp = 1;
+    if (!tc_hybrid_on() || G <= 0 || nkb <= 0) return false;
+    const int64_t r = tiles % G;
+    // not without whole waves: a schedule of pieces only (tiles < G) made the CTAs sharing an
+    // operand row read it at different k (4096x1024x5120 in 128 x 256 tiles: 205 against 238
+    // TFLOP/s for one partial wave of whole tiles)
+    if (r == 0 || tiles < G) return false;
+    const int64_t units = r * nkb;
+    const int64_t minu = 2 * kc > 8 ? 2 * kc : 8;
+    const int64_t gsk = units / minu < G ? units / minu : G;
+    if (gsk <= r) return false;
+    if (ct_cdiv(units, gsk) * 20 > nkb * 17) return false;
+    int64_t maxp = 1;
+    for (int64_t st = 0; st < r; ++st) {
+        const int64_t base = st * nkb;
+        const int64_t cf = ((base + 1) * gsk - 1) / units, cl = ((base + nkb) * gsk - 1) / units;
+        if (cl - cf + 1 > maxp) maxp = cl - cf + 1;
+    }
+    hy.tiles_dp = (int)(tiles - r);
+    hy.gsk = (int)gsk;
+    hy.units = units;
+    hy.maxp = (int)maxp;
+    return true;
+}
+
+// Grows the handle's stream-K partials / counters (after a synchronisation of the handle's
+// stream, so no running launch uses the old ones); new counters start at zero (epoch 0, stale).
+int tc_hybrid_scratch(ct_handle* h, int64_t part_floats, int64_t cnt_n) {
+    if (h->tc_hy_part_floats >= part_floats && h->tc_hy_cnt_n >= cnt_n) return CT_OK;
+    CT_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (h->tc_hy_part_floats < part_floats) {
+        cudaFree(h->tc_hy_part);
+        h->tc_hy_part = nullptr;
+        h->tc_hy_part_floats = 0;
+        CT_CUDA(h, cudaMalloc((void**)&h->tc_hy_part, (size_t)part_floats * sizeof(float)));
+        h->tc_hy_part_floats = part_floats;
+    }
+    if (h->tc_hy_cnt_n < cnt_n) {
+        cudaFree(h->tc_hy_cnt);
+        h->tc_hy_cnt = nullptr;
+        h->tc_hy_cnt_n = 0;
+        CT_CUDA(h, cudaMalloc((void**)&h->tc_hy_cnt, (size_t)cnt_n * sizeof(unsigned long long)));
+        CT_CUDA(h, cudaMemsetAsync(h->tc_hy_cnt, 0, (size_t)cnt_n * sizeof(unsigned long long), h->stream));
+        h->tc_hy_cnt_n = cnt_n;
+    }
+    return CT_OK;
+}
+
+// Tile width per shape: the least (waves x BN / speed(BN)), waves counted whole.  Speed is a
+// width's rate per flop relative to 128.  Single-accumulator kernels: at K <= 2048 the wide
+// tile's fixed per-tile cost (pipeline fill, epilogue) is spread over twice the MMAs, measured as
+// 1.12x (5120x4096x1024: 0.164 vs 0.166 ms; 2048x2048x1024: 0.037 vs 0.041 ms); at K = 5120 both
+// run at the same rate.  Chunked kernel: each chunk boundary costs a fixed ~0.2 us of tensor time
+// whatever the width, so wide tiles gain at every K; measured on 5120x4096x1024, 4096x1024x5120,
+// 2048x2048x1024 and 8192x2048x8192 with whole waves counted, 192 runs at 1.13-1.30x and 256 at
+// 1.24-1.33x the 128-wide rate (used: 1.2, 1.25 for 224, 1.28).
+// With the hybrid schedule (hybrid_kc > 0: the chunk width) a partial last wave costs its
+// longest shared-out range plus the partial sums' store and reload, ~15 us measured, in units
+// of one tile's time (~36 us for a 128 x 256 x 1024 tile at 1.28).
+double tc_width_speed(int bn, int64_t K, bool chunked) {
+    if (bn <= 128) return 1.0;
+    if (!chunked) return K <= 2048 ? 1.12 : 1.0;
+    return bn >= 256 ? 1.28 : bn >= 224 ? 1.25 : 1.2;
+}
+
+int tc_pick_bn(int64_t M, int64_t N, int64_t K, int num_sms, bool chunked, int hybrid_kc) {
     const int mode = tc_bn_mode();
     if (mode) return mode;
     if (N <= 128) return 128;
     const int64_t tm = ct_cdiv(M, TC_BM);
-    const double wide_speed = K <= 2048 ? 1.12 : 1.0;
+    const int64_t nkb = ct_cdiv(K, TC_BK);
     auto cost = [&](int bn) {
-        const int64_t waves = ct_cdiv(tm * ct_cdiv(N, bn), num_sms);
-        return (double)waves * (double)bn / (bn > 128 ? wide_speed : 1.0);
+        const double speed = tc_width_speed(bn, K, chunked);
+        const int64_t tiles = tm * ct_cdiv(N, bn);
+        double waves = (double)ct_cdiv(tiles, num_sms);
+        TcHybrid hy;
+        if (hybrid_kc > 0 && tc_plan_hybrid(tiles, num_sms, nkb, hybrid_kc, hy)) {
+            const double tile_us = 36.0 * ((double)nkb / 32.0) * ((double)bn / 256.0) * (1.28 / speed);
+            const double sk = (double)(hy.tiles_dp / num_sms) + (double)ct_cdiv(hy.units, hy.gsk) / (double)nkb +
+                              15.0 / tile_us;
+            if (sk < waves) waves = sk;
+        }
+        return waves * (double)bn / speed;
     };
     int best = 128;
     double c = cost(128);
-    // 128 x 192 tiles (chunked kernel only): a GEMM of 640 wide tiles (4.2 waves on 152 SMs)
-    // becomes 880 three-quarter tiles (5.8 waves)
-    for (int bn : {256, 192}) {
-        if (bn == 192 && !chunked) continue;
+    // 192 / 224 (chunked kernel only) fill waves that 256 leaves partial: 5120 x 4096 takes 640
+    // tiles of 256 (4.2 waves on 152 SMs), 880 of 192 (5.8), 760 of 224 (5.0)
+    for (int bn : {256, 224, 192}) {
+        if (bn < 256 && !chunked) continue;
         const double cb = cost(bn);
         if (cb < c) {
             c = cb;
@@ -1078,14 +1313,28 @@ int tc_gemm_run(ct_handle* h, const SplitOperand& A, const SplitOperand& B, int6
     }
     const int64_t tiles = ct_cdiv(N, BN) * ct_cdiv(M, TC_BM);
     const int kc = tc_kchunk();
-    if (BN == 192 && !(tc_use_persistent() && kc > 0 && !tc_use_stream_k())) {
-        ct_seterr(h, "128 x 192 tiles exist only in the chunked kernel");
+    if ((BN == 192 || BN == 224) && !(tc_use_persistent() && kc > 0 && !tc_use_stream_k())) {
+        ct_seterr(h, "128 x 192 and 128 x 224 tiles exist only in the chunked kernel");
         return CT_ERR_UNSUPPORTED;
     }
     if (tc_use_persistent() && kc > 0 && !tc_use_stream_k()) {
-        const int64_t grid = tiles < h->num_sms ? tiles : h->num_sms;
+        int64_t grid = tiles < h->num_sms ? tiles : h->num_sms;
+        TcHybrid hy;
+        if (!tc_plan_hybrid(tiles, h->num_sms, A.ldk / TC_BK, kc, hy) || h->no_alloc) {
+            hy = TcHybrid{};
+            hy.tiles_dp = (int)tiles;
+            hy.maxp = 1;
+        } else {
+            const int64_t r = tiles - hy.tiles_dp;
+            CT_TRY(tc_hybrid_scratch(h, r * hy.maxp * TC_BM * BN, r * 4 * tc_chunk_epw(BN)));
+            if (++h->tc_hy_epoch == 0) h->tc_hy_epoch = 1;
+            hy.epoch = h->tc_hy_epoch;
+            hy.part = h->tc_hy_part;
+            hy.cnt = h->tc_hy_cnt;
+            grid = hy.tiles_dp > 0 ? h->num_sms : hy.gsk;
+        }
         tc_gemm_chunk_kernel<BN, STAGES><<<(unsigned)grid, tc_chunk_threads(BN), L::TOTAL, h->stream>>>(
-            ta_h, ta_l, tb_h, tb_l, (int)M, (int)N, (int)A.ldk, kc, epi, skip, h->d_status);
+            ta_h, ta_l, tb_h, tb_l, (int)M, (int)N, (int)A.ldk, kc, epi, hy, skip, h->d_status);
         ct_note_launch();
     } else if (tc_use_persistent()) {
         const int64_t grid = tiles < h->num_sms ? tiles : h->num_sms;
@@ -1137,8 +1386,9 @@ int tc_gemm_launch(ct_handle* h, const SplitOperand& A, const SplitOperand& B, i
     int slot = -1;
     CT_TRY(ct_ktime_begin(h, KT_TC_GEMM, 2.0 * (double)M * (double)N * (double)A.ldk, &slot));
     const bool chunked = tc_use_persistent() && tc_kchunk() > 0 && !tc_use_stream_k();
-    const int bn = tc_pick_bn(M, N, A.ldk, h->num_sms, chunked);
+    const int bn = tc_pick_bn(M, N, A.ldk, h->num_sms, chunked, chunked && !h->no_alloc ? tc_kchunk() : 0);
     const int rc = bn == 256 ? tc_gemm_run<256, GEMM_STAGES_W>(h, A, B, M, N, e, skip)
+                 : bn == 224 ? tc_gemm_run<224, GEMM_STAGES_W>(h, A, B, M, N, e, skip)
                  : bn == 192 ? tc_gemm_run<192, GEMM_STAGES_W>(h, A, B, M, N, e, skip)
                              : tc_gemm_run<128, GEMM_STAGES_N>(h, A, B, M, N, e, skip);
     CT_TRY(rc);

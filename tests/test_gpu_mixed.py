@@ -86,19 +86,46 @@ def _tc_gemm(ctx, A, B):
     return tC.to_numpy()
 
 
-@pytest.mark.parametrize("bn", ["128", "256"])
+@pytest.mark.parametrize("bn", ["128", "192", "224", "256"])
 @pytest.mark.parametrize("kc", ["1", "2", "3", "64"])
 @pytest.mark.parametrize("m,n,k", [(128, 256, 32), (300, 520, 200), (257, 1000, 1000)])
 def test_tc_gemm_chunked(ctx, monkeypatch, bn, kc, m, n, k):
     """The chunked-accumulation kernel (CTDMRG_TC_KCHUNK k-blocks per TMEM
     accumulator) on ragged shapes, chunk counts that do and do not divide K, and
-    both tile widths."""
+    every tile width (192 and 224 exist only in this kernel)."""
     monkeypatch.setenv("CTDMRG_TC_BN", bn)
     monkeypatch.setenv("CTDMRG_TC_KCHUNK", kc)
     rng = np.random.default_rng(m + 3 * n + k)
     A = rng.standard_normal((m, k))
     B = rng.standard_normal((k, n))
     assert rel(_tc_gemm(ctx, A, B), A @ B) < TOL
+
+
+@pytest.mark.parametrize("bn,m,n,k", [("128", 2560, 1024, 2048), ("128", 2500, 1000, 2000), ("128", 2560, 1024, 9000),
+                                      ("192", 2560, 1600, 2048), ("192", 2500, 1700, 1500),
+                                      ("224", 2560, 1800, 2048), ("224", 2500, 1700, 999),
+                                      ("256", 2560, 2100, 2048), ("256", 2400, 2300, 1200)])
+def test_tc_gemm_hybrid_schedule(ctx, monkeypatch, bn, m, n, k):
+    """The chunked kernel's hybrid schedule: whole waves of tiles, then the last partial wave's
+    k-blocks shared out over all SMs, each split tile summed by the piece that arrives last
+    (shapes of 160-180 tiles on 152 SMs; K = 9000 cuts a tile into up to 19 pieces).
+    Against FP64 and against the whole-tile schedule (CTDMRG_TC_HYBRID=0), whose summation
+    order differs; two runs of the same product are bit-identical (the pieces' partials are
+    added in piece order whichever arrives last)."""
+    monkeypatch.setenv("CTDMRG_TC_BN", bn)
+    rng = np.random.default_rng(m + 5 * n + k)
+    A = rng.standard_normal((m, k))
+    B = rng.standard_normal((k, n))
+    ref = A @ B
+    first = _tc_gemm(ctx, A, B)
+    second = _tc_gemm(ctx, A, B)
+    monkeypatch.setenv("CTDMRG_TC_HYBRID", "0")
+    whole = _tc_gemm(ctx, A, B)
+    assert rel(first, ref) < TOL
+    assert rel(whole, ref) < TOL
+    assert np.array_equal(first, second)
+    assert rel(first, whole) < 2e-6
+    assert not np.array_equal(first, whole)
 
 
 def test_tc_gemm_accumulation_bias(ctx, monkeypatch):
