@@ -61,6 +61,10 @@ struct TcEpi {
     int64_t sCm1, sCm0;
     double alpha, beta;  // C = alpha * acc + beta * C
     int vec;             // set by the launcher: C and both row strides 16-byte aligned
+    // set by the launcher (chunked kernel only): the kernel computes the transposed
+    // product, its element (i, j) is the caller's C(j, i), stored at j * sCm0 + i
+    // (single-level rows: M0 >= the caller's M)
+    int trans;
 };
 
 template <int BN, int STAGES>
@@ -857,6 +861,24 @@ __global__ void __launch_bounds__(tc_chunk_threads(BN), 1)
             const int n0 = (w.t % tiles_n) * BN + hf * HC;
             const int64_t m = (int64_t)m0 + row;
             if (m >= M) continue;
+            if (epi.trans) {
+                // element (m, n) to C[n][m]: for each n the warp's 32 rows are 32 consecutive words
+#pragma unroll
+                for (int j = 0; j < HC; ++j) {
+                    const int64_t n = (int64_t)n0 + j;
+                    if (n >= N) break;
+                    const int64_t a = n * epi.sCm0 + m;
+                    if (epi.out_fp64) {
+                        double* Cd = (double*)epi.C;
+                        double v = epi.alpha * (double)sum[j];
+                        if (epi.beta != 0.0) v = fma(epi.beta, Cd[a], v);
+                        Cd[a] = v;
+                    } else {
+                        ((float*)epi.C)[a] = (float)epi.alpha * sum[j];
+                    }
+                }
+                continue;
+            }
             const int64_t rbase = (m / epi.M0) * epi.sCm1 + (m % epi.M0) * epi.sCm0;
 #pragma unroll
             for (int cc = 0; cc < HC; cc += 16) {
@@ -1252,10 +1274,9 @@ double tc_width_speed(int bn, int64_t K, bool chunked) {
     return bn >= 256 ? 1.28 : bn >= 224 ? 1.25 : 1.2;
 }
 
-int tc_pick_bn(int64_t M, int64_t N, int64_t K, int num_sms, bool chunked, int hybrid_kc) {
+int tc_pick_bn(int64_t M, int64_t N, int64_t K, int num_sms, bool chunked, int hybrid_kc, double* cost_out) {
     const int mode = tc_bn_mode();
     if (mode) return mode;
-    if (N <= 128) return 128;
     const int64_t tm = ct_cdiv(M, TC_BM);
     const int64_t nkb = ct_cdiv(K, TC_BK);
     auto cost = [&](int bn) {
@@ -1276,14 +1297,23 @@ int tc_pick_bn(int64_t M, int64_t N, int64_t K, int num_sms, bool chunked, int h
     // 192 / 224 (chunked kernel only) fill waves that 256 leaves partial: 5120 x 4096 takes 640
     // tiles of 256 (4.2 waves on 152 SMs), 880 of 192 (5.8), 760 of 224 (5.0)
     for (int bn : {256, 224, 192}) {
-        if (bn < 256 && !chunked) continue;
+        if (N <= 128 || (bn < 256 && !chunked)) continue;
         const double cb = cost(bn);
         if (cb < c) {
             c = cb;
             best = bn;
         }
     }
+    if (cost_out) *cost_out = c;
     return best;
+}
+
+// CTDMRG_TC_TRANS: 0 never computes the transposed product, 1 always where it may (chunked
+// kernel, single-level rows), unset chooses by the tile cost; read on every launch.
+int tc_trans_mode() {
+    const char* e = getenv("CTDMRG_TC_TRANS");
+    if (!e) return -1;
+    return e[0] == '1' ? 1 : 0;
 }
 
 struct SplitOperand {
@@ -1386,11 +1416,33 @@ int tc_gemm_launch(ct_handle* h, const SplitOperand& A, const SplitOperand& B, i
     int slot = -1;
     CT_TRY(ct_ktime_begin(h, KT_TC_GEMM, 2.0 * (double)M * (double)N * (double)A.ldk, &slot));
     const bool chunked = tc_use_persistent() && tc_kchunk() > 0 && !tc_use_stream_k();
-    const int bn = tc_pick_bn(M, N, A.ldk, h->num_sms, chunked, chunked && !h->no_alloc ? tc_kchunk() : 0);
-    const int rc = bn == 256 ? tc_gemm_run<256, GEMM_STAGES_W>(h, A, B, M, N, e, skip)
-                 : bn == 224 ? tc_gemm_run<224, GEMM_STAGES_W>(h, A, B, M, N, e, skip)
-                 : bn == 192 ? tc_gemm_run<192, GEMM_STAGES_W>(h, A, B, M, N, e, skip)
-                             : tc_gemm_run<128, GEMM_STAGES_N>(h, A, B, M, N, e, skip);
+    const int hkc = chunked && !h->no_alloc ? tc_kchunk() : 0;
+    double cost = 0.0;
+    int bn = tc_pick_bn(M, N, A.ldk, h->num_sms, chunked, hkc, &cost);
+    // The transposed product C^T = B A^T (B's rows as the tile rows) when its tiles fill the
+    // waves better: 4096 x 1024 x 5120 takes 128 tiles of 128 x 256 on 152 SMs, its transpose
+    // 1024 x 4096 takes 152 tiles of 128 x 224.  The epilogue stores C^T's rows as C's columns.
+    const SplitOperand* opA = &A;
+    const SplitOperand* opB = &B;
+    int64_t Mr = M, Nr = N;
+    const int tmode = tc_trans_mode();
+    if (chunked && e.M0 >= M && (tmode == 1 || (tmode < 0 && !tc_bn_mode()))) {
+        double cost_t = 0.0;
+        const int bt = tc_pick_bn(N, M, A.ldk, h->num_sms, chunked, hkc, &cost_t);
+        if (tmode == 1 || cost_t < 0.97 * cost) {
+            bn = bt;
+            e.trans = 1;
+            e.vec = 0;
+            opA = &B;
+            opB = &A;
+            Mr = N;
+            Nr = M;
+        }
+    }
+    const int rc = bn == 256 ? tc_gemm_run<256, GEMM_STAGES_W>(h, *opA, *opB, Mr, Nr, e, skip)
+                 : bn == 224 ? tc_gemm_run<224, GEMM_STAGES_W>(h, *opA, *opB, Mr, Nr, e, skip)
+                 : bn == 192 ? tc_gemm_run<192, GEMM_STAGES_W>(h, *opA, *opB, Mr, Nr, e, skip)
+                             : tc_gemm_run<128, GEMM_STAGES_N>(h, *opA, *opB, Mr, Nr, e, skip);
     CT_TRY(rc);
     CT_TRY(ct_ktime_end(h, slot));
     return CT_OK;

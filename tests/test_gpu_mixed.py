@@ -128,6 +128,29 @@ def test_tc_gemm_hybrid_schedule(ctx, monkeypatch, bn, m, n, k):
     assert not np.array_equal(first, whole)
 
 
+@pytest.mark.parametrize("bn", ["128", "192", "224", "256"])
+@pytest.mark.parametrize("m,n,k", [(300, 520, 200), (1024, 4096, 640), (4100, 1000, 700)])
+def test_tc_gemm_transposed_product(ctx, monkeypatch, bn, m, n, k):
+    """The launcher's transposed form (CTDMRG_TC_TRANS=1 forces it): the kernel computes
+    C^T = B A^T with B's rows as tile rows and stores its rows as C's columns, with alpha and
+    beta; ragged shapes, every tile width, and (1024 x 4096 at 224) the stream-K last wave."""
+    import ctypes as C
+    import torch
+    monkeypatch.setenv("CTDMRG_TC_TRANS", "1")
+    monkeypatch.setenv("CTDMRG_TC_BN", bn)
+    rng = np.random.default_rng(m + 7 * n + k)
+    A = rng.standard_normal((m, k))
+    B = rng.standard_normal((k, n))
+    Cin = rng.standard_normal((m, n))
+    ref = -0.75 * (A @ B) + 0.5 * Cin
+    tA, tB, tC = dt(ctx, A), dt(ctx, B), dt(ctx, Cin)
+    ctx.call("ct_gemm", 1, 0, 0, C.c_int64(m), C.c_int64(n), C.c_int64(k), C.c_double(-0.75),
+             C.c_void_p(tA.storage.data_ptr()), C.c_int64(k), C.c_void_p(tB.storage.data_ptr()), C.c_int64(n),
+             C.c_double(0.5), C.c_void_p(tC.storage.data_ptr()), C.c_int64(n))
+    torch.cuda.synchronize()
+    assert rel(tC.to_numpy(), ref) < TOL
+
+
 def test_tc_gemm_accumulation_bias(ctx, monkeypatch):
     """All-positive operands, K = 5120: every partial sum has the same sign, so the
     truncating FP32 accumulation of the tensor cores shrinks the product coherently.
