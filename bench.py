@@ -75,8 +75,8 @@ RAMP = [64, 256, 1024]
 # the difference measures precision rather than early-trajectory noise
 ACC_RAMP = (64, 256, 256, 256, 256)
 # dram__bytes_read.sum + dram__bytes_write.sum of one centre-bond H_eff GEMM launch
-# (5120 x 4096 x 1024 at chi=1024, 128x256 tiles) from an ncu --set full capture
-TC_GEMM_TRAFFIC_BYTES = (80.065 + 46.893) * 1e6
+# (5120 x 4096 x 1024 at chi=1024, 128x224 tiles) from an ncu --set full capture
+TC_GEMM_TRAFFIC_BYTES = (80.092 + 47.428) * 1e6
 METRIC = "DMRG sweep s & H_eff TFLOP/s, mixed-prec vs FP64 on GPU at |dE/E|<=1e-9"
 
 
@@ -1010,14 +1010,15 @@ def main():
         peak = bf16 / 6.0
         line["roofline"] = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                             "traffic": TC_GEMM_TRAFFIC_BYTES,
-                            "kernel": "tc_gemm_chunk_kernel<128,3> and <256,2> (TF32x3, tcgen05, a fresh TMEM "
-                                      "accumulator every 64 of K summed in FP32 registers; tile width chosen per shape)",
+                            "kernel": "tc_gemm_chunk_kernel<BN,STAGES> (TF32x3, tcgen05, a fresh TMEM accumulator "
+                                      "every 64 of K summed in FP32 registers; tile width 128/192/224/256 and the "
+                                      "transposed product chosen per shape, stream-K last wave)",
                             "launches": kt["launches"], "avg_launch_ms": kt["ms"] / kt["launches"],
                             "flops_per_launch": kt["flops"] / kt["launches"],
                             "share_of_timed_region": kt["ms"] * 1e-3 / max(dev_s, 1e-12),
                             "peak_note": f"{peak_src} bf16 {bf16} TFLOP/s / 2 (TF32 rate) / 3 (3 MMAs per product)",
                             "traffic_note": "DRAM read+write bytes of one centre-bond H_eff GEMM 1 "
-                                            "(5120x4096x1024, tc_gemm_chunk_kernel<256,2>) from an ncu capture, "
+                                            "(5120x4096x1024, tc_gemm_chunk_kernel<224,2>) from an ncu capture, "
                                             "per launch"}
     if kt_heff and kt_heff["launches"] > 0:
         # CUDA-event breakdown of the timed sweeps (device seconds, summed over both sweeps)
