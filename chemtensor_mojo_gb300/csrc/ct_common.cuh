@@ -119,7 +119,7 @@ static_assert(SC_MISC + CT_MAX_KRYLOV_SLOTS <= SC_SVD_FROB2 && SC_SPLIT_PIV + 2 
                   SC_ORTH_EMAX < SC_SVD_MINKEPT && SC_SVD_MINKEPT + 1 <= CT_NSCALARS,
               "scalar slots overlap or overflow d_scalars");
 // int slots inside d_flags
-enum { FL_STOP = 0, FL_NUMITER = 1, FL_ROT = 2, FL_CHI = 3, FL_TMP = 4, FL_CNT = 8, FL_REDO = 9 };
+enum { FL_STOP = 0, FL_NUMITER = 1, FL_ROT = 2, FL_CHI = 3, FL_TMP = 4, FL_CNT = 8, FL_REDO = 9, FL_REDO64 = 10 };
 
 #define CT_MAX_KRYLOV 128
 
@@ -280,12 +280,14 @@ int ct_lanczos_alpha(ct_handle* h, int64_t n, const double* vj, const double* w,
                      const int* skip);
 // (gate != null: the kernels run only when *gate != 0, set by the FP32 pass)
 int ct_lanczos_reorth_pass(ct_handle* h, int64_t n, double* w, const double* V, int64_t ldv, int j,
-                           double beta_threshold, const int* skip, const int* gate = nullptr);
+                           double beta_threshold, const int* skip);
 int ct_lanczos_update_nonorm(ct_handle* h, int64_t n, double* w, const double* vj, const double* vjm1, int j,
                              const int* skip);
 // the same pass against an FP32 copy of the basis; v_{j+1} with its FP32 copy
 int ct_lanczos_reorth_pass32(ct_handle* h, int64_t n, double* w, const float* V32, int64_t ldv, int j,
-                             double beta_threshold, const int* skip);
+                             double beta_threshold, const int* skip, double ratio64);
+int ct_lanczos_reorth_redo(ct_handle* h, int64_t n, double* w, const double* V, const float* V32, int64_t ldv, int j,
+                           double beta_threshold, const int* skip);
 int ct_lanczos_next32(ct_handle* h, int64_t n, const double* w, double* vnext, float* vnext32, int j,
                       const int* skip);
 int ct_f64_to_f32(ct_handle* h, int64_t n, const double* x, float* y, const int* skip);

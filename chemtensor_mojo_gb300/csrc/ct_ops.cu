@@ -243,6 +243,14 @@ size_t ct_lanczos_ws_bytes(int prec, int64_t Dl, int64_t d, int64_t Dr, int64_t 
            (prec == CT_PREC_TF32X3 ? ct_bytes(N * (int64_t)max_iter, 4) : 0);
 }
 
+// Second FP32 reorthogonalisation pass in place of most FP64 passes (CTDMRG_LANCZOS_REDO32=0
+// restores the FP64 pass after every FP32 pass that removed more than 0.1 beta); read on
+// every Lanczos run so that a test can compare both in one process.
+static bool ct_lanczos_redo32() {
+    const char* e = getenv("CTDMRG_LANCZOS_REDO32");
+    return !(e && e[0] == '0');
+}
+
 int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, double* theta_out, const double* L,
                    const double* R, const double* W1, const double* W2, int64_t Dl, int64_t d, int64_t Dr,
                    int64_t wL, int64_t wM, int64_t wR, int max_iter, double tol, int max_rotations, int reorth,
@@ -303,9 +311,11 @@ int ct_lanczos_run(ct_handle* h, Arena& ar, int prec, const double* theta_in, do
             CT_TRY(ct_lanczos_alpha(h, N, vj, w, j, stop));
             CT_TRY(ct_lanczos_update_nonorm(h, N, w, vj, vjm1, j, stop));
             if (V32) {
-                CT_TRY(ct_lanczos_reorth_pass32(h, N, w, V32, N, j, thr, stop));
-                // the FP64 pass again when the FP32 one removed much of w (gated on the device)
-                CT_TRY(ct_lanczos_reorth_pass(h, N, w, V, N, j, thr, stop, h->d_flags + FL_REDO));
+                // the FP32 pass, then a second pass gated on the device: against the FP32 copy
+                // when the first removed more than 0.1 beta, against the FP64 basis above 1e4 beta
+                // (CTDMRG_LANCZOS_REDO32=0: the FP64 basis whenever above 0.1 beta)
+                CT_TRY(ct_lanczos_reorth_pass32(h, N, w, V32, N, j, thr, stop, ct_lanczos_redo32() ? 1e4 : 0.1));
+                CT_TRY(ct_lanczos_reorth_redo(h, N, w, V, V32, N, j, thr, stop));
                 CT_TRY(ct_lanczos_next32(h, N, w, V + (int64_t)(j + 1) * N, V32 + (int64_t)(j + 1) * N, j, stop));
             } else {
                 CT_TRY(ct_lanczos_reorth_pass(h, N, w, V, N, j, thr, stop));

@@ -64,10 +64,9 @@
 namespace {
 
 // Cholesky block.  A leaf factors and inverts one CH_NB x CH_NB block in one CTA
-// (~145 us for 64 x 64, latency-bound: a serial FP64 square root and reciprocal
-// and three barriers per column).  32 x 32 leaves were measured slower overall
-// (7.4 vs 6.4 ms per chi=1024 warm split): the extra recursion level's small
-// products cost more than the leaves saved.
+// (chol_diag_kernel).  32 x 32 leaves were measured slower overall (7.4 vs 6.4 ms
+// per chi=1024 warm split, with the earlier three-barrier leaf): the extra
+// recursion level's small products cost more than the leaves saved.
 constexpr int CH_NB = 64;
 constexpr int FL_CHOL_FAIL = 100;    // d_flags slot: non-positive pivot seen
 constexpr int FL_DEF_COUNT = 101;    // d_flags slot: rows marked for replacement in a first pass
@@ -131,83 +130,175 @@ __global__ void chol_prepare_kernel(double* G, double* Linv, int64_t c, int64_t 
     }
 }
 
+// 2^e as a double for e in [-1022, 1023] (exact: the exponent field alone)
+__device__ __forceinline__ double chol_pow2(int e) { return __longlong_as_double((long long)(e + 1023) << 52); }
+
+// 1/sqrt(p) in FP64 for finite p > 0, by Newton-Raphson on the reciprocal square root:
+// p = m 2^(2k) with m in [1, 4) (exact power-of-two scaling), an FP32 estimate r of
+// m^(-1/2) (~23 correct bits), then twice r <- r + r (1 - m r^2) / 2, each step doubling
+// the correct bits (~46, then FP64 rounding), and the result r 2^(-k).  On this part
+// FP64 issues at ~1/64 of the FP32 rate, and an IEEE FP64 square root and division in
+// one lane cost the whole warp tens of FP64 issue slots per pivot.
+__device__ __forceinline__ double chol_rsqrt(double p) {
+    int adj = 0;
+    if (p < 2.2250738585072014e-308) {   // subnormal: into the normal range, exactly
+        p *= 18446744073709551616.0;     // 2^64
+        adj = 32;
+    }
+    const int e = (int)((__double_as_longlong(p) >> 52) & 0x7ff) - 1023;
+    const int k = e >> 1;   // floor(e / 2)
+    const double m = p * chol_pow2(-2 * k);
+    double r = (double)rsqrtf((float)m);
+    r = fma(0.5 * r, fma(-(m * r), r, 1.0), r);
+    r = fma(0.5 * r, fma(-(m * r), r, 1.0), r);
+    return r * chol_pow2(adj - k);
+}
+
+// Pivot j of the leaf (by one lane): the replacement rules, the running minimum (as
+// the bit pattern: pivots are >= 0 when recorded, so the integer order is the order),
+// then 1/p, sqrt(p) and 1/sqrt(p) for the step into pv[0..2].  The tests run on the
+// bit pattern too (integer instructions instead of FP64 ones).
+__device__ __forceinline__ void chol_pivot(double p, int j, double* pv, long long* mp, int* fail, int* defrows,
+                                           int* defcount, int64_t row0, long long floor_bits) {
+    const long long pb = __double_as_longlong(p);
+    const bool finite = (pb & 0x7fffffffffffffffll) < 0x7ff0000000000000ll;
+    // with floor > 0, a finite p is below it exactly when its bit pattern is (a negative
+    // p or -0 reads as a negative integer)
+    if (floor_bits > 0 && finite && pb < floor_bits) {
+        // no direction left outside the rows before: mark the row for replacement
+        const int k = atomicAdd(defcount, 1);
+        defrows[k] = (int)(row0 + j);
+        p = 1.0;
+    } else if (!(finite && pb > 0)) {
+        *fail = 1;
+        p = 1.0;
+        *mp = min(*mp, __double_as_longlong(1.0));
+    } else {
+        *mp = min(*mp, pb);
+    }
+    const double r = chol_rsqrt(p);
+    pv[0] = r * r;
+    pv[1] = p * r;
+    pv[2] = r;
+}
+
 // Cholesky of the CH_NB x CH_NB block at G (lower triangle, trailing updates
-// already applied) and the inverse of that factor, in FP64.  L
-// goes back into G's block (zeros above the diagonal), L^{-1} into Linv's
-// block.  A pivot that is not positive and finite is replaced by 1 and
-// flagged; the smallest pivot goes to *minpiv (bit pattern, atomicMin; pivots
-// are >= 0 when recorded).  256 threads: 8 warps own the rows of the update.
+// already applied) and the inverse of that factor, in FP64.  L goes back into
+// G's block (zeros above the diagonal), L^{-1} into Linv's block.  A pivot that
+// is not positive and finite is replaced by 1 and flagged; the smallest pivot
+// goes to *minpiv (bit pattern, atomicMin; pivots are >= 0 when recorded).
+//
+// One elimination sweep builds both factors, one barrier per column.  Working
+// row i holds, at step j, the inverse's row (unscaled: X = I eliminated) at
+// positions k <= j and the trailing matrix's row at positions j < l <= i, so its
+// update at step j is exactly i + 1 multiply-adds with f = a_ij / p_j:
+//     R[i][k] -= f R[j][k]   (k < j)        R[i][j] = -f
+//     R[i][l] -= f a_lj      (j < l <= i)
+// where a_lj is column j of the trailing matrix, snapshotted when the step before
+// finished it (col[], double-buffered).  Column j of L is a_ij / sqrt(p_j) (stored
+// unscaled during the sweep, scaled once at the end), row j of L^{-1} is
+// R[j][k] / sqrt(p_j) (R[j][j] = 1).  The lane that finishes the next diagonal
+// element computes the next pivot's 1/p, sqrt(p), 1/sqrt(p) at once (double-
+// buffered too), so no warp waits on a serial pivot.  256 threads: warp w owns the
+// rows i = w (mod 8), up to 8 per step, lane l the positions l and l + 32 of each;
+// a warp loads all its rows before its multiply-adds, so their latencies overlap.
+// On this part FP64 issues at ~1/64 of the FP32 rate: the sweep's cost is its FP64
+// instruction count (about 2.8k warp-instructions of multiply-adds) and one barrier
+// per column.
 __global__ void __launch_bounds__(256) chol_diag_kernel(double* G, double* Linv, int64_t ld,
                                                         unsigned long long* minpiv, int* fail, int* defrows,
                                                         int* defcount, int64_t row0, double floor) {
-    using T = double;
-    extern __shared__ __align__(16) unsigned char chol_smem_raw[];   // two CH_NB x (CH_NB + 1) tiles
-    T(*A)[CH_NB + 1] = reinterpret_cast<T(*)[CH_NB + 1]>(chol_smem_raw);
-    T(*X)[CH_NB + 1] = reinterpret_cast<T(*)[CH_NB + 1]>(chol_smem_raw + sizeof(T) * CH_NB * (CH_NB + 1));
-    __shared__ T rinv;
-    __shared__ T dinv[CH_NB];
+    extern __shared__ __align__(16) unsigned char chol_smem_raw[];   // three CH_NB x (CH_NB + 1) tiles
+    double(*R)[CH_NB + 1] = reinterpret_cast<double(*)[CH_NB + 1]>(chol_smem_raw);
+    double(*Ls)[CH_NB + 1] = R + CH_NB;
+    double(*Xs)[CH_NB + 1] = Ls + CH_NB;
+    __shared__ double col[2][CH_NB];
+    __shared__ double piv[2][3];
+    __shared__ double dinv[CH_NB];
+    __shared__ long long mp;
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const long long floor_bits = floor > 0.0 ? __double_as_longlong(floor) : 0ll;
     for (int e = t; e < CH_NB * CH_NB; e += blockDim.x) {
         const int i = e / CH_NB, j = e % CH_NB;
-        A[i][j] = (j <= i) ? (T)G[i * ld + j] : (T)0;
-        X[i][j] = (T)0;
+        const double g = (j <= i) ? G[i * ld + j] : 0.0;
+        R[i][j] = g;
+        Ls[i][j] = 0.0;
+        Xs[i][j] = 0.0;
+        if (j == 0) col[0][i] = g;
+    }
+    if (t == 0) {
+        mp = __double_as_longlong(1.0e300);
+        chol_pivot(G[0], 0, piv[0], &mp, fail, defrows, defcount, row0, floor_bits);
     }
     __syncthreads();
-    double mp = 1.0e300;
+    const int k0 = lane, k1 = lane + 32;
     for (int j = 0; j < CH_NB; ++j) {
-        if (t == 0) {
-            double p = (double)A[j][j];
-            if (floor > 0.0 && isfinite(p) && p < floor) {
-                // no direction left outside the rows before: mark the row for replacement
-                const int k = atomicAdd(defcount, 1);
-                defrows[k] = (int)(row0 + j);
-                p = 1.0;
-            } else if (!(p > 0.0) || !isfinite(p)) {
-                *fail = 1;
-                p = 1.0;
-                mp = fmin(mp, p);
-            } else {
-                mp = fmin(mp, p);
+        const int b = j & 1;
+        const double inv_p = piv[b][0];
+        // this warp's rows i > j, i = warp (mod 8); lane q < 8 forms row q's multiplier and
+        // keeps its entry of L's column j (unscaled)
+        const int i0 = j + 1 + ((warp - (j + 1)) & 7);
+        double fq = 0.0;
+        {
+            const int iq = i0 + 8 * lane;
+            if (lane < 8 && iq < CH_NB) {
+                const double a = col[b][iq];
+                fq = a * inv_p;
+                Ls[iq][j] = a;
             }
-            const T dj = (T)sqrt(p);
-            A[j][j] = dj;
-            rinv = (T)1 / dj;
-            dinv[j] = rinv;
         }
-        __syncthreads();
-        for (int i = j + 1 + t; i < CH_NB; i += blockDim.x) A[i][j] *= rinv;
-        __syncthreads();
-        // rank-1 update of the trailing lower triangle: warp w takes rows j+1+w, +8, ...
-        for (int i = j + 1 + warp; i < CH_NB; i += 8) {
-            const T aij = A[i][j];
-            for (int l = j + 1 + lane; l <= i; l += 32) A[i][l] -= aij * A[l][j];
+        if (warp == (j & 7)) {
+            // row j is final: its row of L^{-1} and the diagonal of L
+            const double inv_d = piv[b][2];
+            for (int k = lane; k <= j; k += 32) Xs[j][k] = (k == j ? 1.0 : R[j][k]) * inv_d;
+            if (lane == 0) {
+                Ls[j][j] = piv[b][1];
+                dinv[j] = inv_d;
+            }
+        }
+        // the sources of positions k0, k1 are the same for every row
+        const double s0 = k0 == j ? 1.0 : (k0 < j ? R[j][k0] : col[b][k0]);
+        const double s1 = k1 == j ? 1.0 : (k1 < j ? R[j][k1] : col[b][k1]);
+        double base0[8], base1[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int i = i0 + 8 * q;
+            base0[q] = (i < CH_NB && k0 <= i && k0 != j) ? R[i][k0] : 0.0;
+            base1[q] = (i < CH_NB && k1 <= i && k1 != j) ? R[i][k1] : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int i = i0 + 8 * q;
+            if (i >= CH_NB) break;   // warp-uniform
+            const double f = __shfl_sync(0xffffffffu, fq, q);
+            if (k0 <= i) {
+                const double v = fma(-f, s0, base0[q]);
+                R[i][k0] = v;
+                if (k0 == j + 1) {
+                    if (i == j + 1)
+                        chol_pivot(v, j + 1, piv[b ^ 1], &mp, fail, defrows, defcount, row0, floor_bits);
+                    else
+                        col[b ^ 1][i] = v;
+                }
+            }
+            if (i >= 32 && k1 <= i) {
+                const double v = fma(-f, s1, base1[q]);
+                R[i][k1] = v;
+                if (k1 == j + 1) {
+                    if (i == j + 1)
+                        chol_pivot(v, j + 1, piv[b ^ 1], &mp, fail, defrows, defcount, row0, floor_bits);
+                    else
+                        col[b ^ 1][i] = v;
+                }
+            }
         }
         __syncthreads();
     }
-    if (t == 0) atomicMin(minpiv, (unsigned long long)__double_as_longlong(mp));
-    // column col of L^{-1} by forward substitution, four lanes per column: each
-    // lane sums every fourth term, two shuffles combine them (the diagonal's
-    // reciprocals are kept)
-    {
-        // the row loop is uniform across the warp (its 8 columns start at 8w);
-        // a column takes part once i reaches it
-        const int col = t >> 2, q = t & 3, first = (t >> 5) * 8;
-        const bool live = col < CH_NB;   // 256 threads cover 64 columns; a 32-wide block uses half
-        for (int i = first; i < CH_NB; ++i) {
-            T s = (T)0;
-            if (live && i >= col)
-                for (int l = col + q; l < i; l += 4) s += A[i][l] * X[l][col];
-            s += __shfl_xor_sync(0xffffffffu, s, 1);
-            s += __shfl_xor_sync(0xffffffffu, s, 2);
-            if (live && q == 0 && i >= col) X[i][col] = (((i == col) ? (T)1 : (T)0) - s) * dinv[i];
-            __syncwarp();
-        }
-    }
-    __syncthreads();
+    if (t == 0) atomicMin(minpiv, (unsigned long long)mp);
     for (int e = t; e < CH_NB * CH_NB; e += blockDim.x) {
         const int i = e / CH_NB, j = e % CH_NB;
-        G[i * ld + j] = (double)A[i][j];
-        Linv[i * ld + j] = (double)X[i][j];
+        G[i * ld + j] = i > j ? Ls[i][j] * dinv[j] : Ls[i][j];
+        Linv[i * ld + j] = Xs[i][j];
     }
 }
 
@@ -273,7 +364,7 @@ struct CholMarks {
 int chol_inv(ct_handle* h, double* G, double* Linv, int64_t ld, int64_t n, double* S,
              unsigned long long* d_minpiv, int* d_fail, const CholMarks& mk, int64_t row0) {
     if (n <= CH_NB) {
-        constexpr int smem = 2 * CH_NB * (CH_NB + 1) * (int)sizeof(double);
+        constexpr int smem = 3 * CH_NB * (CH_NB + 1) * (int)sizeof(double);
         static int attr_dev = -1;
         if (attr_dev != h->device) {
             CT_CUDA(h, cudaFuncSetAttribute(chol_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));

@@ -263,11 +263,9 @@ __device__ __forceinline__ void cgs_dots_group(int64_t n, const double* __restri
 }
 
 // pass A: coeff[v] = <V[v], w> for v < nvec
-__global__ void __launch_bounds__(RT) cgs_dots_kernel(int64_t n, const double* __restrict__ w,
-                                                      const double* __restrict__ V, int64_t ldv, int nvec, int vec2,
-                                                      double* partials, unsigned* counter, double* coeff,
-                                                      const int* skip, const int* gate) {
-    if (ct_skip(skip) || (gate && *(volatile const int*)gate == 0)) return;
+__device__ __forceinline__ void cgs_dots_dev(int64_t n, const double* __restrict__ w, const double* __restrict__ V,
+                                             int64_t ldv, int nvec, int vec2, double* partials, unsigned* counter,
+                                             double* coeff) {
     __shared__ double sm[CGS_VB][RT / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int v0 = 0; v0 < nvec; v0 += CGS_VB) {
@@ -314,12 +312,9 @@ __global__ void __launch_bounds__(RT) cgs_dots_kernel(int64_t n, const double* _
 
 // pass B: w -= sum_v coeff[v] V[v] with |w|^2; the last block forms beta_j = |w|
 // and makes the breakdown test beta < thr (dmrg.mojo:630-673)
-__global__ void __launch_bounds__(RT) cgs_update_kernel(int64_t n, double* __restrict__ w,
-                                                        const double* __restrict__ V, int64_t ldv, int nvec, int vec2,
-                                                        const double* coeff, double* partials, unsigned* counter,
-                                                        double* scalars, int* flags, int j, double thr,
-                                                        const int* skip, const int* gate) {
-    if (ct_skip(skip) || (gate && *(volatile const int*)gate == 0)) return;
+__device__ __forceinline__ void cgs_update_dev(int64_t n, double* __restrict__ w, const double* __restrict__ V,
+                                               int64_t ldv, int nvec, int vec2, const double* coeff, double* partials,
+                                               unsigned* counter, double* scalars, int* flags, int j, double thr) {
     __shared__ double sm[32];
     __shared__ double c[CT_MAX_KRYLOV];
     for (int v = threadIdx.x; v < nvec; v += RT) c[v] = coeff[v];
@@ -411,11 +406,9 @@ __device__ __forceinline__ void cgs32_dots_group(int64_t n, const double* __rest
     }
 }
 
-__global__ void __launch_bounds__(RT) cgs32_dots_kernel(int64_t n, const double* __restrict__ w,
-                                                        const float* __restrict__ V, int64_t ldv, int nvec, int vec4,
-                                                        double* partials, unsigned* counter, double* coeff,
-                                                        const int* skip) {
-    if (ct_skip(skip)) return;
+__device__ __forceinline__ void cgs32_dots_dev(int64_t n, const double* __restrict__ w, const float* __restrict__ V,
+                                               int64_t ldv, int nvec, int vec4, double* partials, unsigned* counter,
+                                               double* coeff) {
     __shared__ double sm[CGS_VB][RT / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int v0 = 0; v0 < nvec; v0 += CGS_VB) {
@@ -459,12 +452,10 @@ __global__ void __launch_bounds__(RT) cgs32_dots_kernel(int64_t n, const double*
     if (threadIdx.x == 0) *counter = 0u;
 }
 
-__global__ void __launch_bounds__(RT) cgs32_update_kernel(int64_t n, double* __restrict__ w,
-                                                          const float* __restrict__ V, int64_t ldv, int nvec, int vec4,
-                                                          const double* coeff, double* partials, unsigned* counter,
-                                                          double* scalars, int* flags, int j, double thr,
-                                                          const int* skip) {
-    if (ct_skip(skip)) return;
+__device__ __forceinline__ void cgs32_update_dev(int64_t n, double* __restrict__ w, const float* __restrict__ V,
+                                                 int64_t ldv, int nvec, int vec4, const double* coeff,
+                                                 double* partials, unsigned* counter, double* scalars, int* flags,
+                                                 int j, double thr, int second, double ratio64) {
     __shared__ double sm[32];
     __shared__ float c[CT_MAX_KRYLOV];
     for (int v = threadIdx.x; v < nvec; v += RT) c[v] = (float)coeff[v];
@@ -512,13 +503,21 @@ __global__ void __launch_bounds__(RT) cgs32_update_kernel(int64_t n, double* __r
     for (int v = threadIdx.x; v < nvec; v += RT) cc += coeff[v] * coeff[v];
     cc = ct_block_sum<RT>(cc, sm);
     if (threadIdx.x == 0) {
-        // The FP32 correction leaves ~3e-7 |c| of the removed part in the new residual,
-        // i.e. ~3e-7 |c| / beta of orthogonality loss for v_{j+1}.  Up to |c| = 0.1 beta
-        // that stays near 3e-8, about the semi-orthogonality Lanczos needs; beyond it
-        // (a Krylov space close to exhausted, where w lies mostly inside the basis and
-        // |c| / beta reaches 1e5) the FP64 pass runs on the FP64 basis and decides
-        // beta and breakdown itself.
-        flags[FL_REDO] = (cc > 1e-2 * s) ? 1 : 0;
+        // The FP32 dots of w against a basis vector it is nearly parallel to err by
+        // ~1e-7 of the coefficient (the terms share a sign), so the pass leaves ~1e-7 |c|
+        // along the basis: ~1e-7 |c| / beta of orthogonality loss for v_{j+1}.  Up to
+        // |c| = 0.1 beta that stays near 1e-8, about the semi-orthogonality Lanczos needs.
+        // Beyond it a second FP32 pass (FL_REDO) runs on the now nearly orthogonal w,
+        // whose dots err at random rather than coherently; it leaves ~1e-14 |c| / beta,
+        // enough up to |c| / beta = ratio64 (1e4).  Above that (a Krylov space close to
+        // exhausted, |c| / beta up to 1e5 and more) the second pass is the FP64 one
+        // (FL_REDO64), on the FP64 basis.  Either decides beta and breakdown again.
+        if (!second) {
+            const bool big = cc > 1e-2 * s;
+            const bool huge = cc > ratio64 * ratio64 * s;
+            flags[FL_REDO] = (big && !huge) ? 1 : 0;
+            flags[FL_REDO64] = huge ? 1 : 0;
+        }
         const double b = sqrt(s);
         if (b < thr) {
             flags[FL_NUMITER] = j + 1;
@@ -528,6 +527,67 @@ __global__ void __launch_bounds__(RT) cgs32_update_kernel(int64_t n, double* __r
         }
         *counter = 0u;
     }
+}
+
+// FP64 pass (FP64 form, and a gated second pass of the mixed form)
+__global__ void __launch_bounds__(RT) cgs_dots_kernel(int64_t n, const double* __restrict__ w,
+                                                      const double* __restrict__ V, int64_t ldv, int nvec, int vec2,
+                                                      double* partials, unsigned* counter, double* coeff,
+                                                      const int* skip) {
+    if (ct_skip(skip)) return;
+    cgs_dots_dev(n, w, V, ldv, nvec, vec2, partials, counter, coeff);
+}
+__global__ void __launch_bounds__(RT) cgs_update_kernel(int64_t n, double* __restrict__ w,
+                                                        const double* __restrict__ V, int64_t ldv, int nvec, int vec2,
+                                                        const double* coeff, double* partials, unsigned* counter,
+                                                        double* scalars, int* flags, int j, double thr,
+                                                        const int* skip) {
+    if (ct_skip(skip)) return;
+    cgs_update_dev(n, w, V, ldv, nvec, vec2, coeff, partials, counter, scalars, flags, j, thr);
+}
+
+// first pass of the mixed form, against the FP32 copy of the basis
+__global__ void __launch_bounds__(RT) cgs32_dots_kernel(int64_t n, const double* __restrict__ w,
+                                                        const float* __restrict__ V, int64_t ldv, int nvec, int vec4,
+                                                        double* partials, unsigned* counter, double* coeff,
+                                                        const int* skip) {
+    if (ct_skip(skip)) return;
+    cgs32_dots_dev(n, w, V, ldv, nvec, vec4, partials, counter, coeff);
+}
+__global__ void __launch_bounds__(RT) cgs32_update_kernel(int64_t n, double* __restrict__ w,
+                                                          const float* __restrict__ V, int64_t ldv, int nvec, int vec4,
+                                                          const double* coeff, double* partials, unsigned* counter,
+                                                          double* scalars, int* flags, int j, double thr,
+                                                          const int* skip, double ratio64) {
+    if (ct_skip(skip)) return;
+    cgs32_update_dev(n, w, V, ldv, nvec, vec4, coeff, partials, counter, scalars, flags, j, thr, 0, ratio64);
+}
+
+// second pass of the mixed form, gated on the device by the first: against the FP64
+// basis when FL_REDO64 is set, else against the FP32 copy when FL_REDO is set, else
+// nothing (one launch pair either way; the gates do not change between the two)
+__global__ void __launch_bounds__(RT) cgs_redo_dots_kernel(int64_t n, const double* __restrict__ w,
+                                                           const double* __restrict__ V, const float* __restrict__ V32,
+                                                           int64_t ldv, int nvec, int vec2, int vec4,
+                                                           double* partials, unsigned* counter, double* coeff,
+                                                           const int* skip, const int* flags) {
+    if (ct_skip(skip)) return;
+    if (*(volatile const int*)(flags + FL_REDO64))
+        cgs_dots_dev(n, w, V, ldv, nvec, vec2, partials, counter, coeff);
+    else if (*(volatile const int*)(flags + FL_REDO))
+        cgs32_dots_dev(n, w, V32, ldv, nvec, vec4, partials, counter, coeff);
+}
+__global__ void __launch_bounds__(RT) cgs_redo_update_kernel(int64_t n, double* __restrict__ w,
+                                                             const double* __restrict__ V,
+                                                             const float* __restrict__ V32, int64_t ldv, int nvec,
+                                                             int vec2, int vec4, const double* coeff,
+                                                             double* partials, unsigned* counter, double* scalars,
+                                                             int* flags, int j, double thr, const int* skip) {
+    if (ct_skip(skip)) return;
+    if (*(volatile const int*)(flags + FL_REDO64))
+        cgs_update_dev(n, w, V, ldv, nvec, vec2, coeff, partials, counter, scalars, flags, j, thr);
+    else if (*(volatile const int*)(flags + FL_REDO))
+        cgs32_update_dev(n, w, V32, ldv, nvec, vec4, coeff, partials, counter, scalars, flags, j, thr, 1, 0.0);
 }
 
 // v_{j+1} = w / beta_j in FP64 and its FP32 copy
@@ -891,7 +951,7 @@ int ct_lanczos_update(ct_handle* h, int64_t n, double* w, const double* vj, cons
 // reference recurrence has updated w; beta_j (or the breakdown stop) goes to the
 // scalar slots.  The caller then forms v_{j+1} = w / beta_j.
 int ct_lanczos_reorth_pass(ct_handle* h, int64_t n, double* w, const double* V, int64_t ldv, int j,
-                           double beta_threshold, const int* skip, const int* gate) {
+                           double beta_threshold, const int* skip) {
     const int nvec = j + 1;
     if (nvec > 64) return CT_ERR_UNSUPPORTED;
     int g = grid_for(h, n);
@@ -899,18 +959,20 @@ int ct_lanczos_reorth_pass(ct_handle* h, int64_t n, double* w, const double* V, 
     const int vec2 = ((n & 1) == 0 && (ldv & 1) == 0 && aligned16(w) && aligned16(V)) ? 1 : 0;
     unsigned* counter = reinterpret_cast<unsigned*>(h->d_flags + FL_CNT);
     double* coeff = h->d_scalars + SC_MISC;
-    cgs_dots_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, vec2, h->d_partials, counter, coeff, skip, gate);
+    cgs_dots_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, vec2, h->d_partials, counter, coeff, skip);
     ct_note_launch();
     cgs_update_kernel<<<g, RT, 0, h->stream>>>(n, w, V, ldv, nvec, vec2, coeff, h->d_partials, counter,
-                                               h->d_scalars, h->d_flags, j, beta_threshold, skip, gate);
+                                               h->d_scalars, h->d_flags, j, beta_threshold, skip);
     ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
 
-// Reorthogonalisation pass against the FP32 copy V32 of the basis (mixed form).
+// Reorthogonalisation pass against the FP32 copy V32 of the basis (mixed form).  It sets
+// the gates of the second pass: FL_REDO (against V32) when it removed more than 0.1 beta,
+// FL_REDO64 (against the FP64 basis) above ratio64 beta.
 int ct_lanczos_reorth_pass32(ct_handle* h, int64_t n, double* w, const float* V32, int64_t ldv, int j,
-                             double beta_threshold, const int* skip) {
+                             double beta_threshold, const int* skip, double ratio64) {
     const int nvec = j + 1;
     if (nvec > 64) return CT_ERR_UNSUPPORTED;
     int g = grid_for(h, n);
@@ -921,7 +983,30 @@ int ct_lanczos_reorth_pass32(ct_handle* h, int64_t n, double* w, const float* V3
     cgs32_dots_kernel<<<g, RT, 0, h->stream>>>(n, w, V32, ldv, nvec, vec4, h->d_partials, counter, coeff, skip);
     ct_note_launch();
     cgs32_update_kernel<<<g, RT, 0, h->stream>>>(n, w, V32, ldv, nvec, vec4, coeff, h->d_partials, counter,
-                                                 h->d_scalars, h->d_flags, j, beta_threshold, skip); ct_note_launch();
+                                                 h->d_scalars, h->d_flags, j, beta_threshold, skip, ratio64);
+    ct_note_launch();
+    CT_LAUNCH_CHECK(h);
+    return CT_OK;
+}
+
+// The gated second pass after ct_lanczos_reorth_pass32 (V: the FP64 basis, V32 its copy,
+// both with leading dimension ldv).
+int ct_lanczos_reorth_redo(ct_handle* h, int64_t n, double* w, const double* V, const float* V32, int64_t ldv, int j,
+                           double beta_threshold, const int* skip) {
+    const int nvec = j + 1;
+    if (nvec > 64) return CT_ERR_UNSUPPORTED;
+    int g = grid_for(h, n);
+    if ((int64_t)g * nvec > CT_NPARTIALS) g = CT_NPARTIALS / nvec;
+    const int vec2 = ((n & 1) == 0 && (ldv & 1) == 0 && aligned16(w) && aligned16(V)) ? 1 : 0;
+    const int vec4 = ((n & 3) == 0 && (ldv & 3) == 0 && aligned16(w) && aligned16(V32)) ? 1 : 0;
+    unsigned* counter = reinterpret_cast<unsigned*>(h->d_flags + FL_CNT);
+    double* coeff = h->d_scalars + SC_MISC;
+    cgs_redo_dots_kernel<<<g, RT, 0, h->stream>>>(n, w, V, V32, ldv, nvec, vec2, vec4, h->d_partials, counter, coeff,
+                                                  skip, h->d_flags);
+    ct_note_launch();
+    cgs_redo_update_kernel<<<g, RT, 0, h->stream>>>(n, w, V, V32, ldv, nvec, vec2, vec4, coeff, h->d_partials,
+                                                    counter, h->d_scalars, h->d_flags, j, beta_threshold, skip);
+    ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
