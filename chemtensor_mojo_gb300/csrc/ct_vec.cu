@@ -149,15 +149,6 @@ __global__ void permute_kernel(const double* in, double* out, PermArgs a) {
 }
 
 // ---- Lanczos -------------------------------------------------------------------
-// alpha_j = <v_j, w>   -> scalars[SC_ALPHA + j]
-__global__ void __launch_bounds__(RT) lanczos_alpha_finish(const double* partials, int np, double* scalars,
-                                                           int j, const int* skip) {
-    if (ct_skip(skip)) return;
-    __shared__ double sm[32];
-    const double s = finish_sum(partials, np, sm);
-    if (threadIdx.x == 0) scalars[SC_ALPHA + j] = s;
-}
-
 // w -= alpha_j v_j + beta_{j-1} v_{j-1}; partial |w|^2
 __global__ void __launch_bounds__(RT) lanczos_update_kernel(int64_t n, double* w, const double* vj,
                                                             const double* vjm1, const double* scalars,
@@ -168,11 +159,38 @@ __global__ void __launch_bounds__(RT) lanczos_update_kernel(int64_t n, double* w
     const double b = (j > 0) ? scalars[SC_BETA + j - 1] : 0.0;
     double acc = 0.0;
     const int64_t stride = (int64_t)gridDim.x * RT;
-    for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) {
-        double x = w[i] - a * vj[i];
-        if (vjm1) x -= b * vjm1[i];
-        w[i] = x;
-        acc = fma(x, x, acc);
+    if (aligned16(w) && aligned16(vj) && (!vjm1 || aligned16(vjm1))) {
+        // 16-byte accesses; an odd last element by one thread
+        const int64_t n2 = n / 2;
+        double2* w2 = reinterpret_cast<double2*>(w);
+        const double2* a2 = reinterpret_cast<const double2*>(vj);
+        const double2* c2 = reinterpret_cast<const double2*>(vjm1);
+        for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n2; i += stride) {
+            double2 x = w2[i];
+            const double2 v = a2[i];
+            x.x -= a * v.x;
+            x.y -= a * v.y;
+            if (vjm1) {
+                const double2 u = c2[i];
+                x.x -= b * u.x;
+                x.y -= b * u.y;
+            }
+            w2[i] = x;
+            acc = fma(x.x, x.x, fma(x.y, x.y, acc));
+        }
+        if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+            double x = w[n - 1] - a * vj[n - 1];
+            if (vjm1) x -= b * vjm1[n - 1];
+            w[n - 1] = x;
+            acc = fma(x, x, acc);
+        }
+    } else {
+        for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) {
+            double x = w[i] - a * vj[i];
+            if (vjm1) x -= b * vjm1[i];
+            w[i] = x;
+            acc = fma(x, x, acc);
+        }
     }
     acc = ct_block_sum<RT>(acc, sm);
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
@@ -529,6 +547,43 @@ __device__ __forceinline__ void cgs32_update_dev(int64_t n, double* __restrict__
     }
 }
 
+// alpha_j = <v_j, w> -> scalars[SC_ALPHA + j]: block partials over 16-byte loads, then
+// the block that arrives last sums them in block order (the same fixed-order sum as a
+// separate one-block finisher, without its launch)
+__global__ void __launch_bounds__(RT) lanczos_alpha_kernel(int64_t n, const double* __restrict__ vj,
+                                                           const double* __restrict__ w, double* partials,
+                                                           unsigned* counter, double* scalars, int j,
+                                                           const int* skip) {
+    if (ct_skip(skip)) return;
+    __shared__ double sm[32];
+    double acc = 0.0;
+    const int64_t stride = (int64_t)gridDim.x * RT;
+    const int64_t start = (int64_t)blockIdx.x * RT + threadIdx.x;
+    if (aligned16(vj) && aligned16(w)) {
+        const int64_t n2 = n / 2;
+        const double2* x2 = reinterpret_cast<const double2*>(vj);
+        const double2* y2 = reinterpret_cast<const double2*>(w);
+        for (int64_t i = start; i < n2; i += stride) {
+            const double2 a = x2[i], b = y2[i];
+            acc = fma(a.x, b.x, acc);
+            acc = fma(a.y, b.y, acc);
+        }
+        if ((n & 1) && start == 0) acc = fma(vj[n - 1], w[n - 1], acc);
+    } else {
+        for (int64_t i = start; i < n; i += stride) acc = fma(vj[i], w[i], acc);
+    }
+    acc = ct_block_sum<RT>(acc, sm);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+    if (!last_block_arrived(counter)) return;
+    double r = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += RT) r += __ldcg(partials + b);
+    r = ct_block_sum<RT>(r, sm);
+    if (threadIdx.x == 0) {
+        scalars[SC_ALPHA + j] = r;
+        *counter = 0u;
+    }
+}
+
 // FP64 pass (FP64 form, and a gated second pass of the mixed form)
 __global__ void __launch_bounds__(RT) cgs_dots_kernel(int64_t n, const double* __restrict__ w,
                                                       const double* __restrict__ V, int64_t ldv, int nvec, int vec2,
@@ -595,10 +650,30 @@ __global__ void lanczos_next32_kernel(int64_t n, const double* w, double* vnext,
                                       const double* scalars, int j, const int* skip) {
     if (ct_skip(skip)) return;
     const double inv = 1.0 / scalars[SC_BETA + j];
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double v = w[i] * inv;
-        vnext[i] = v;
-        vnext32[i] = (float)v;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    if (aligned16(w) && aligned16(vnext) && ((uintptr_t)vnext32 & 7) == 0) {
+        // 16-byte FP64 and 8-byte FP32 accesses; an odd last element by one thread
+        const int64_t n2 = n / 2;
+        const double2* w2 = reinterpret_cast<const double2*>(w);
+        double2* v2 = reinterpret_cast<double2*>(vnext);
+        float2* f2 = reinterpret_cast<float2*>(vnext32);
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride) {
+            const double2 x = w2[i];
+            const double2 v = make_double2(x.x * inv, x.y * inv);
+            v2[i] = v;
+            f2[i] = make_float2((float)v.x, (float)v.y);
+        }
+        if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+            const double v = w[n - 1] * inv;
+            vnext[n - 1] = v;
+            vnext32[n - 1] = (float)v;
+        }
+    } else {
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+            const double v = w[i] * inv;
+            vnext[i] = v;
+            vnext32[i] = (float)v;
+        }
     }
 }
 
@@ -931,8 +1006,9 @@ int ct_lanczos_init(ct_handle* h, int max_iter) {
 
 int ct_lanczos_alpha(ct_handle* h, int64_t n, const double* vj, const double* w, int j, const int* skip) {
     const int g = grid_for(h, n);
-    partial_kernel<0><<<g, RT, 0, h->stream>>>(n, vj, w, h->d_partials, skip); ct_note_launch();
-    lanczos_alpha_finish<<<1, RT, 0, h->stream>>>(h->d_partials, g, h->d_scalars, j, skip); ct_note_launch();
+    unsigned* counter = reinterpret_cast<unsigned*>(h->d_flags + FL_CNT);
+    lanczos_alpha_kernel<<<g, RT, 0, h->stream>>>(n, vj, w, h->d_partials, counter, h->d_scalars, j, skip);
+    ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
 }
