@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -45,9 +46,24 @@ def _compile(src: Path, obj: Path, debug: bool, verbose: bool) -> None:
         raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stdout}\n{r.stderr}")
 
 
+def _stamp(debug: bool) -> str:
+    """What the objects were built for: the host machine, the compiler and the flags."""
+    r = subprocess.run([_nvcc(), "--version"], capture_output=True, text=True)
+    tail = r.stdout.strip().splitlines()[-1] if r.stdout.strip() else ""
+    return f"{platform.machine()}|{tail}|{' '.join(_flags(debug))}"
+
+
 def build(force: bool = False, verbose: bool = False, debug: bool = False) -> Path:
-    """Compile every kernel source and link libctdmrg.so; returns its path."""
+    """Compile every kernel source and link libctdmrg.so; returns its path.
+
+    Objects are reused by modification time only when ``_build/stamp`` names the same
+    machine, compiler and flags; otherwise (a tree copied from another machine, a new
+    toolkit, a debug build) everything is compiled again."""
     BUILD.mkdir(exist_ok=True)
+    stamp_file = BUILD / "stamp"
+    stamp = _stamp(debug)
+    if not stamp_file.exists() or stamp_file.read_text() != stamp:
+        force = True
     sources = sorted(CSRC.glob("*.cu"))
     headers = list(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "ctdmrg.h"]
     newest_hdr = max(p.stat().st_mtime for p in headers if p.exists())
@@ -73,6 +89,7 @@ def build(force: bool = False, verbose: bool = False, debug: bool = False) -> Pa
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    stamp_file.write_text(stamp)
     return LIB
 
 
