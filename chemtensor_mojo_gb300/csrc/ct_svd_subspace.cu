@@ -130,28 +130,38 @@ __global__ void chol_prepare_kernel(double* G, double* Linv, int64_t c, int64_t 
     }
 }
 
-// 2^e as a double for e in [-1022, 1023] (exact: the exponent field alone)
-__device__ __forceinline__ double chol_pow2(int e) { return __longlong_as_double((long long)(e + 1023) << 52); }
-
 // 1/sqrt(p) in FP64 for finite p > 0, by Newton-Raphson on the reciprocal square root:
-// p = m 2^(2k) with m in [1, 4) (exact power-of-two scaling), an FP32 estimate r of
-// m^(-1/2) (~23 correct bits), then twice r <- r + r (1 - m r^2) / 2, each step doubling
-// the correct bits (~46, then FP64 rounding), and the result r 2^(-k).  On this part
-// FP64 issues at ~1/64 of the FP32 rate, and an IEEE FP64 square root and division in
-// one lane cost the whole warp tens of FP64 issue slots per pivot.
+// p = m 2^(2k) with m in [1, 4), an FP32 estimate r of m^(-1/2) (~23 correct bits), then
+// twice r <- r + (r/2) (1 - m r^2), each step doubling the correct bits (~46, then FP64
+// rounding), and the result r 2^(-k).  The scalings by powers of two, the halving and the
+// FP32 <-> FP64 conversions are exact operations on the exponent and mantissa fields,
+// done with integer instructions: on this part FP64 issues at ~1/64 of the FP32 rate, the
+// pivot is on the leaf's critical path, and it keeps 8 FP64 operations (the Newton steps
+// and r^2, p r at the end).
 __device__ __forceinline__ double chol_rsqrt(double p) {
+    constexpr long long ONE_EXP = 1ll << 52;   // one unit of the FP64 exponent field
     int adj = 0;
-    if (p < 2.2250738585072014e-308) {   // subnormal: into the normal range, exactly
-        p *= 18446744073709551616.0;     // 2^64
+    long long bits = __double_as_longlong(p);
+    if ((bits >> 52) == 0) {   // subnormal: into the normal range, exactly
+        p *= 18446744073709551616.0;   // 2^64
         adj = 32;
+        bits = __double_as_longlong(p);
     }
-    const int e = (int)((__double_as_longlong(p) >> 52) & 0x7ff) - 1023;
+    const int e = (int)((bits >> 52) & 0x7ff) - 1023;
     const int k = e >> 1;   // floor(e / 2)
-    const double m = p * chol_pow2(-2 * k);
-    double r = (double)rsqrtf((float)m);
-    r = fma(0.5 * r, fma(-(m * r), r, 1.0), r);
-    r = fma(0.5 * r, fma(-(m * r), r, 1.0), r);
-    return r * chol_pow2(adj - k);
+    const long long mb = bits - (long long)(2 * k) * ONE_EXP;   // m = p 2^(-2k)
+    const double m = __longlong_as_double(mb);
+    const int em = (int)((mb >> 52) & 0x7ff) - 1023;            // 0 or 1
+    const float mf = __int_as_float(((em + 127) << 23) | (int)((mb >> 29) & 0x7fffff));   // m, truncated
+    const int rb = __float_as_int(rsqrtf(mf));
+    double r = __longlong_as_double((long long)((rb >> 23) - 127 + 1023) * ONE_EXP +
+                                    ((long long)(rb & 0x7fffff) << 29));
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const double h = __longlong_as_double(__double_as_longlong(r) - ONE_EXP);   // r / 2
+        r = fma(h, fma(-(m * r), r, 1.0), r);
+    }
+    return __longlong_as_double(__double_as_longlong(r) + (long long)(adj - k) * ONE_EXP);
 }
 
 // Pivot j of the leaf (by one lane): the replacement rules, the running minimum (as
