@@ -68,6 +68,7 @@ namespace {
 // per chi=1024 warm split, with the earlier three-barrier leaf): the extra
 // recursion level's small products cost more than the leaves saved.
 constexpr int CH_NB = 64;
+constexpr int CH_THREADS = 288;      // leaf: 8 row warps and the pivot warp
 constexpr int FL_CHOL_FAIL = 100;    // d_flags slot: non-positive pivot seen
 constexpr int FL_DEF_COUNT = 101;    // d_flags slot: rows marked for replacement in a first pass
 // smallest accepted Cholesky pivot of a first pass (the squared share of a
@@ -207,15 +208,17 @@ __device__ __forceinline__ void chol_pivot(double p, int j, double* pv, long lon
 // where a_lj is column j of the trailing matrix, snapshotted when the step before
 // finished it (col[], double-buffered).  Column j of L is a_ij / sqrt(p_j) (stored
 // unscaled during the sweep, scaled once at the end), row j of L^{-1} is
-// R[j][k] / sqrt(p_j) (R[j][j] = 1).  The lane that finishes the next diagonal
-// element computes the next pivot's 1/p, sqrt(p), 1/sqrt(p) at once (double-
-// buffered too), so no warp waits on a serial pivot.  256 threads: warp w owns the
-// rows i = w (mod 8), up to 8 per step, lane l the positions l and l + 32 of each;
-// a warp loads all its rows before its multiply-adds, so their latencies overlap.
+// R[j][k] / sqrt(p_j) (R[j][j] = 1).  A ninth warp forms the next pivot at the start
+// of each step, p_{j+1} = a_{j+1,j+1} - a_{j+1,j}^2 / p_j (the same arithmetic as the
+// row update, whose owner leaves that element unwritten: nothing reads it again), and
+// its 1/p, sqrt(p), 1/sqrt(p) (double-buffered), while warps 0..7 run the step's
+// multiply-adds: the pivot chain is no longer behind any row's.  Warp w < 8 owns the
+// rows i = w (mod 8), up to 8 per step, lane l the positions l and l + 32 of each; a
+// warp loads all its rows before its multiply-adds, so their latencies overlap.
 // On this part FP64 issues at ~1/64 of the FP32 rate: the sweep's cost is its FP64
 // instruction count (about 2.8k warp-instructions of multiply-adds) and one barrier
 // per column.
-__global__ void __launch_bounds__(256) chol_diag_kernel(double* G, double* Linv, int64_t ld,
+__global__ void __launch_bounds__(CH_THREADS) chol_diag_kernel(double* G, double* Linv, int64_t ld,
                                                         unsigned long long* minpiv, int* fail, int* defrows,
                                                         int* defcount, int64_t row0, double floor) {
     extern __shared__ __align__(16) unsigned char chol_smem_raw[];   // three CH_NB x (CH_NB + 1) tiles
@@ -245,6 +248,16 @@ __global__ void __launch_bounds__(256) chol_diag_kernel(double* G, double* Linv,
     for (int j = 0; j < CH_NB; ++j) {
         const int b = j & 1;
         const double inv_p = piv[b][0];
+        if (warp == 8) {
+            // the pivot of step j + 1 from a_{j+1,j} and a_{j+1,j+1}, both final since step j - 1
+            if (lane == 0 && j + 1 < CH_NB) {
+                const double a = col[b][j + 1];
+                const double v = fma(-(a * inv_p), a, R[j + 1][j + 1]);
+                chol_pivot(v, j + 1, piv[b ^ 1], &mp, fail, defrows, defcount, row0, floor_bits);
+            }
+            __syncthreads();
+            continue;
+        }
         // this warp's rows i > j, i = warp (mod 8); lane q < 8 forms row q's multiplier and
         // keeps its entry of L's column j (unscaled)
         const int i0 = j + 1 + ((warp - (j + 1)) & 7);
@@ -281,25 +294,16 @@ __global__ void __launch_bounds__(256) chol_diag_kernel(double* G, double* Linv,
             const int i = i0 + 8 * q;
             if (i >= CH_NB) break;   // warp-uniform
             const double f = __shfl_sync(0xffffffffu, fq, q);
-            if (k0 <= i) {
+            // (the next pivot's element, i == k == j + 1, is warp 8's)
+            if (k0 <= i && !(i == j + 1 && k0 == j + 1)) {
                 const double v = fma(-f, s0, base0[q]);
                 R[i][k0] = v;
-                if (k0 == j + 1) {
-                    if (i == j + 1)
-                        chol_pivot(v, j + 1, piv[b ^ 1], &mp, fail, defrows, defcount, row0, floor_bits);
-                    else
-                        col[b ^ 1][i] = v;
-                }
+                if (k0 == j + 1) col[b ^ 1][i] = v;
             }
-            if (i >= 32 && k1 <= i) {
+            if (i >= 32 && k1 <= i && !(i == j + 1 && k1 == j + 1)) {
                 const double v = fma(-f, s1, base1[q]);
                 R[i][k1] = v;
-                if (k1 == j + 1) {
-                    if (i == j + 1)
-                        chol_pivot(v, j + 1, piv[b ^ 1], &mp, fail, defrows, defcount, row0, floor_bits);
-                    else
-                        col[b ^ 1][i] = v;
-                }
+                if (k1 == j + 1) col[b ^ 1][i] = v;
             }
         }
         __syncthreads();
@@ -380,7 +384,7 @@ int chol_inv(ct_handle* h, double* G, double* Linv, int64_t ld, int64_t n, doubl
             CT_CUDA(h, cudaFuncSetAttribute(chol_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
             attr_dev = h->device;
         }
-        chol_diag_kernel<<<1, 256, smem, h->stream>>>(G, Linv, ld, d_minpiv, d_fail, mk.rows, mk.count, row0,
+        chol_diag_kernel<<<1, CH_THREADS, smem, h->stream>>>(G, Linv, ld, d_minpiv, d_fail, mk.rows, mk.count, row0,
                                                       mk.rows ? mk.floor : 0.0);
         ct_note_launch();
         CT_LAUNCH_CHECK(h);
