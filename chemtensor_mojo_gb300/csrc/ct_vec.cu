@@ -149,7 +149,10 @@ __global__ void permute_kernel(const double* in, double* out, PermArgs a) {
 }
 
 // ---- Lanczos -------------------------------------------------------------------
-// w -= alpha_j v_j + beta_{j-1} v_{j-1}; partial |w|^2
+// w -= alpha_j v_j + beta_{j-1} v_{j-1}; partial |w|^2 when NORM (the mixed form's
+// reorthogonalisation measures the norm itself, and on this part FP64 issues at 1/64 of
+// the FP32 rate: the unused norm was a third of the kernel's FP64 work)
+template <bool NORM>
 __global__ void __launch_bounds__(RT) lanczos_update_kernel(int64_t n, double* w, const double* vj,
                                                             const double* vjm1, const double* scalars,
                                                             int j, double* partials, const int* skip) {
@@ -176,24 +179,26 @@ __global__ void __launch_bounds__(RT) lanczos_update_kernel(int64_t n, double* w
                 x.y -= b * u.y;
             }
             w2[i] = x;
-            acc = fma(x.x, x.x, fma(x.y, x.y, acc));
+            if (NORM) acc = fma(x.x, x.x, fma(x.y, x.y, acc));
         }
         if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
             double x = w[n - 1] - a * vj[n - 1];
             if (vjm1) x -= b * vjm1[n - 1];
             w[n - 1] = x;
-            acc = fma(x, x, acc);
+            if (NORM) acc = fma(x, x, acc);
         }
     } else {
         for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += stride) {
             double x = w[i] - a * vj[i];
             if (vjm1) x -= b * vjm1[i];
             w[i] = x;
-            acc = fma(x, x, acc);
+            if (NORM) acc = fma(x, x, acc);
         }
     }
-    acc = ct_block_sum<RT>(acc, sm);
-    if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+    if (NORM) {
+        acc = ct_block_sum<RT>(acc, sm);
+        if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+    }
 }
 
 // beta_j = sqrt(sum); breakdown test beta < 100 n eps (dmrg.mojo:630-673)
@@ -427,7 +432,8 @@ __device__ __forceinline__ void cgs32_dots_group(int64_t n, const double* __rest
 __device__ __forceinline__ void cgs32_dots_dev(int64_t n, const double* __restrict__ w, const float* __restrict__ V,
                                                int64_t ldv, int nvec, int vec4, double* partials, unsigned* counter,
                                                double* coeff) {
-    __shared__ double sm[CGS_VB][RT / 32];
+    static_assert(RT == 256 && CGS_VB == 16, "the block reduction maps 256 threads onto 16 x 16");
+    __shared__ float red[CGS_VB][RT + 1];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int v0 = 0; v0 < nvec; v0 += CGS_VB) {
         const int nv = min(CGS_VB, nvec - v0);
@@ -444,19 +450,24 @@ __device__ __forceinline__ void cgs32_dots_dev(int64_t n, const double* __restri
 #undef CT_CGS_CASE
             default: break;
         }
-        double accd[CGS_VB];
+        // block sums of the nv per-thread FP32 sums, in FP64 from the first addition on:
+        // through shared memory, thread t adds 16 of coefficient t / 16's entries, then
+        // 16-lane shuffles (~36 FP64 instructions per warp instead of a 5-level shuffle
+        // tree per coefficient, ~80; FP64 issues at 1/64 of the FP32 rate on this part)
 #pragma unroll
-        for (int k = 0; k < CGS_VB; ++k) accd[k] = (k < nv) ? ct_warp_sum((double)acc[k]) : 0.0;
-        if (lane == 0) {
-#pragma unroll
-            for (int k = 0; k < CGS_VB; ++k)
-                if (k < nv) sm[k][wid] = accd[k];
-        }
+        for (int k = 0; k < CGS_VB; ++k)
+            if (k < nv) red[k][threadIdx.x] = acc[k];
         __syncthreads();
-        if (threadIdx.x < nv) {
+        {
+            const int k = threadIdx.x >> 4, r0 = threadIdx.x & 15;
             double r = 0.0;
-            for (int q = 0; q < RT / 32; ++q) r += sm[threadIdx.x][q];
-            partials[(int64_t)blockIdx.x * nvec + v0 + threadIdx.x] = r;
+            if (k < nv) {
+#pragma unroll
+                for (int q = 0; q < RT / 16; ++q) r += (double)red[k][r0 + 16 * q];
+            }
+#pragma unroll
+            for (int off = 8; off > 0; off >>= 1) r += __shfl_xor_sync(0xffffffffu, r, off, 16);
+            if (k < nv && r0 == 0) partials[(int64_t)blockIdx.x * nvec + v0 + k] = r;
         }
         __syncthreads();
     }
@@ -1016,7 +1027,7 @@ int ct_lanczos_alpha(ct_handle* h, int64_t n, const double* vj, const double* w,
 int ct_lanczos_update(ct_handle* h, int64_t n, double* w, const double* vj, const double* vjm1, int j,
                       double beta_threshold, const int* skip) {
     const int g = grid_for(h, n);
-    lanczos_update_kernel<<<g, RT, 0, h->stream>>>(n, w, vj, vjm1, h->d_scalars, j, h->d_partials, skip); ct_note_launch();
+    lanczos_update_kernel<true><<<g, RT, 0, h->stream>>>(n, w, vj, vjm1, h->d_scalars, j, h->d_partials, skip); ct_note_launch();
     lanczos_beta_finish<<<1, RT, 0, h->stream>>>(h->d_partials, g, h->d_scalars, h->d_flags, j,
                                                  beta_threshold, skip); ct_note_launch();
     CT_LAUNCH_CHECK(h);
@@ -1056,7 +1067,10 @@ int ct_lanczos_reorth_pass32(ct_handle* h, int64_t n, double* w, const float* V3
     const int vec4 = ((n & 3) == 0 && (ldv & 3) == 0 && aligned16(w) && aligned16(V32)) ? 1 : 0;
     unsigned* counter = reinterpret_cast<unsigned*>(h->d_flags + FL_CNT);
     double* coeff = h->d_scalars + SC_MISC;
-    cgs32_dots_kernel<<<g, RT, 0, h->stream>>>(n, w, V32, ldv, nvec, vec4, h->d_partials, counter, coeff, skip);
+    // the dots: two blocks per SM keep ~150 KB of loads in flight per SM, and fewer blocks
+    // mean fewer block reductions (FP64)
+    const int gd = g < 2 * h->num_sms ? g : 2 * h->num_sms;
+    cgs32_dots_kernel<<<gd, RT, 0, h->stream>>>(n, w, V32, ldv, nvec, vec4, h->d_partials, counter, coeff, skip);
     ct_note_launch();
     cgs32_update_kernel<<<g, RT, 0, h->stream>>>(n, w, V32, ldv, nvec, vec4, coeff, h->d_partials, counter,
                                                  h->d_scalars, h->d_flags, j, beta_threshold, skip, ratio64);
@@ -1106,7 +1120,7 @@ int ct_f64_to_f32(ct_handle* h, int64_t n, const double* x, float* y, const int*
 int ct_lanczos_update_nonorm(ct_handle* h, int64_t n, double* w, const double* vj, const double* vjm1, int j,
                              const int* skip) {
     const int g = grid_for(h, n);
-    lanczos_update_kernel<<<g, RT, 0, h->stream>>>(n, w, vj, vjm1, h->d_scalars, j, h->d_partials, skip);
+    lanczos_update_kernel<false><<<g, RT, 0, h->stream>>>(n, w, vj, vjm1, h->d_scalars, j, h->d_partials, skip);
     ct_note_launch();
     CT_LAUNCH_CHECK(h);
     return CT_OK;
