@@ -104,6 +104,7 @@ SIGNATURES = {
     "ct_random_mps_host": [I32, I32, I32, C.c_uint64, C.POINTER(I64), PP],
     "ct_rng_randnf_host": [C.c_uint64, I64, C.POINTER(C.c_float)],
     "ct_tc_gemm_time": [P, I64, I64, I64, I32, C.POINTER(D)],
+    "ct_tc_gemm_plan": [I64, I64, I64, I32, C.POINTER(I64)],
     "ct_svd_split_warm": [P, P, I64, I64, I64, I64, I32, P, I32, P, P, P, C.POINTER(I32), C.POINTER(D),
                           C.POINTER(D)],
     "ct_kernel_timing": [P, I32],

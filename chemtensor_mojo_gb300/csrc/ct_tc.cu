@@ -1403,6 +1403,34 @@ int tc_gemm_run(ct_handle* h, const SplitOperand& A, const SplitOperand& B, int6
     return CT_OK;
 }
 
+// The launcher's choices for an M x N product over ldk (a multiple of 32): the tile width and
+// whether to compute the transposed product C^T = B A^T (B's rows as the tile rows) when its
+// tiles fill the waves better -- 4096 x 1024 x 5120 takes 128 tiles of 128 x 256 on 152 SMs,
+// its transpose 1024 x 4096 takes 152 tiles of 128 x 224.  single_level: C's rows have one
+// stride (the transposed epilogue's condition).
+struct TcChoice {
+    int bn = 128;
+    bool trans = false;
+    bool chunked = false;
+};
+TcChoice tc_choose(int num_sms, bool no_alloc, int64_t M, int64_t N, int64_t ldk, bool single_level) {
+    TcChoice c;
+    c.chunked = tc_use_persistent() && tc_kchunk() > 0 && !tc_use_stream_k();
+    const int hkc = c.chunked && !no_alloc ? tc_kchunk() : 0;
+    double cost = 0.0;
+    c.bn = tc_pick_bn(M, N, ldk, num_sms, c.chunked, hkc, &cost);
+    const int tmode = tc_trans_mode();
+    if (c.chunked && single_level && (tmode == 1 || (tmode < 0 && !tc_bn_mode()))) {
+        double cost_t = 0.0;
+        const int bt = tc_pick_bn(N, M, ldk, num_sms, c.chunked, hkc, &cost_t);
+        if (tmode == 1 || cost_t < 0.97 * cost) {
+            c.bn = bt;
+            c.trans = true;
+        }
+    }
+    return c;
+}
+
 int tc_gemm_launch(ct_handle* h, const SplitOperand& A, const SplitOperand& B, int64_t M, int64_t N,
                    const TcEpi& epi, const int* skip) {
     if (A.ldk != B.ldk) return CT_ERR_SHAPE;
@@ -1415,29 +1443,19 @@ int tc_gemm_launch(ct_handle* h, const SplitOperand& A, const SplitOperand& B, i
     }
     int slot = -1;
     CT_TRY(ct_ktime_begin(h, KT_TC_GEMM, 2.0 * (double)M * (double)N * (double)A.ldk, &slot));
-    const bool chunked = tc_use_persistent() && tc_kchunk() > 0 && !tc_use_stream_k();
-    const int hkc = chunked && !h->no_alloc ? tc_kchunk() : 0;
-    double cost = 0.0;
-    int bn = tc_pick_bn(M, N, A.ldk, h->num_sms, chunked, hkc, &cost);
-    // The transposed product C^T = B A^T (B's rows as the tile rows) when its tiles fill the
-    // waves better: 4096 x 1024 x 5120 takes 128 tiles of 128 x 256 on 152 SMs, its transpose
-    // 1024 x 4096 takes 152 tiles of 128 x 224.  The epilogue stores C^T's rows as C's columns.
+    const TcChoice ch = tc_choose(h->num_sms, h->no_alloc, M, N, A.ldk, e.M0 >= M);
+    const int bn = ch.bn;
     const SplitOperand* opA = &A;
     const SplitOperand* opB = &B;
     int64_t Mr = M, Nr = N;
-    const int tmode = tc_trans_mode();
-    if (chunked && e.M0 >= M && (tmode == 1 || (tmode < 0 && !tc_bn_mode()))) {
-        double cost_t = 0.0;
-        const int bt = tc_pick_bn(N, M, A.ldk, h->num_sms, chunked, hkc, &cost_t);
-        if (tmode == 1 || cost_t < 0.97 * cost) {
-            bn = bt;
-            e.trans = 1;
-            e.vec = 0;
-            opA = &B;
-            opB = &A;
-            Mr = N;
-            Nr = M;
-        }
+    if (ch.trans) {
+        // the epilogue stores C^T's rows as C's columns
+        e.trans = 1;
+        e.vec = 0;
+        opA = &B;
+        opB = &A;
+        Mr = N;
+        Nr = M;
     }
     const int rc = bn == 256 ? tc_gemm_run<256, GEMM_STAGES_W>(h, *opA, *opB, Mr, Nr, e, skip)
                  : bn == 224 ? tc_gemm_run<224, GEMM_STAGES_W>(h, *opA, *opB, Mr, Nr, e, skip)
@@ -1799,6 +1817,33 @@ int ct_tc_gemm_ex(ct_handle* h, Arena& ar, int trans_a, int trans_b, int64_t m, 
     TcEpi e{};
     e.C = C; e.out_fp64 = out_fp64; e.M0 = m; e.sCm1 = 0; e.sCm0 = ldc; e.alpha = alpha; e.beta = beta;
     return tc_gemm_launch(h, a, b, m, n, e, nullptr);
+}
+
+// The launcher's plan for a plain m x n x k TF32x3 product on num_sms SMs, host only (no
+// device, no handle): out[0] tile width, [1] 1 when the transposed product runs, [2] tiles,
+// [3] whole tiles of the hybrid schedule, [4] CTAs sharing the stream-K units (0: none),
+// [5] stream-K units (k-blocks), [6] most pieces of a stream-K tile, [7] k-blocks per tile.
+extern "C" CT_API int ct_tc_gemm_plan(int64_t m, int64_t n, int64_t k, int num_sms, int64_t* out) {
+    if (!out || m <= 0 || n <= 0 || k <= 0 || num_sms <= 0) return CT_ERR_INVALID;
+    const int64_t ldk = ct_round_up(k, TC_BK);
+    const TcChoice c = tc_choose(num_sms, false, m, n, ldk, true);
+    const int64_t Mr = c.trans ? n : m, Nr = c.trans ? m : n;
+    const int64_t tiles = ct_cdiv(Nr, c.bn) * ct_cdiv(Mr, TC_BM);
+    TcHybrid hy;
+    if (!(c.chunked && tc_plan_hybrid(tiles, num_sms, ldk / TC_BK, tc_kchunk(), hy))) {
+        hy = TcHybrid{};
+        hy.tiles_dp = (int)tiles;
+        hy.maxp = 1;
+    }
+    out[0] = c.bn;
+    out[1] = c.trans ? 1 : 0;
+    out[2] = tiles;
+    out[3] = hy.tiles_dp;
+    out[4] = hy.gsk;
+    out[5] = hy.units;
+    out[6] = hy.maxp;
+    out[7] = ldk / TC_BK;
+    return CT_OK;
 }
 
 // Times launches of the raw TF32x3 GEMM kernel (operands already split and

@@ -338,6 +338,14 @@ CT_API int ct_heff2_apply_noalloc(void* stream, const double* theta, const doubl
  * m x n x k problem with operands already split and resident in HBM.       */
 CT_API int ct_tc_gemm_time(ct_handle* h, int64_t m, int64_t n, int64_t k, int reps, double* ms_per_launch);
 
+/* The TF32x3 GEMM launcher's plan for a plain m x n x k product on num_sms
+ * SMs, computed on the host (no device needed): out[0] tile width (128, 192,
+ * 224 or 256), out[1] 1 when C^T = B A^T is computed instead, out[2] tiles,
+ * out[3] whole tiles of the hybrid schedule, out[4] CTAs sharing the stream-K
+ * k-blocks (0: no stream-K part), out[5] stream-K k-blocks, out[6] most pieces
+ * of one stream-K tile, out[7] k-blocks (32 of K) per tile. */
+CT_API int ct_tc_gemm_plan(int64_t m, int64_t n, int64_t k, int num_sms, int64_t* out);
+
 /* Live timing of the tensor-core GEMM inside real work (no reference
  * counterpart).  ct_kernel_timing(h, 1) resets the totals and makes every
  * TF32x3 GEMM launch on h record a CUDA event pair on h's stream;
