@@ -95,16 +95,31 @@ __global__ void fill_kernel(double* x, int64_t n, double v) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         x[i] = v;
 }
+// One FP64 reciprocal per block, shared (once per kernel: the shared slot is not reused): an
+// IEEE FP64 division or square root is tens of FP64 instructions, and on this part FP64 issues
+// at ~1/64 of the FP32 rate, so one per thread of an elementwise grid (~600 k threads) cost
+// more FP64 time than the kernel's memory traffic.
+__device__ __forceinline__ double block_reciprocal(double x) {
+    __shared__ double r;
+    if (threadIdx.x == 0) r = 1.0 / x;
+    __syncthreads();
+    return r;
+}
+
 // y = x / sqrt(*nsq); status zero_code when sqrt(nsq) < 1e-14 (dmrg.mojo:605-611)
 __global__ void scale_inv_sqrt_kernel(int64_t n, const double* x, double* y, const double* nsq,
                                       const int* skip, int* status, int zero_code) {
     if (ct_skip(skip)) return;
-    const double nrm = sqrt(*nsq);
+    __shared__ double nrm_s;
+    if (threadIdx.x == 0) nrm_s = sqrt(*nsq);
+    __syncthreads();
+    const double nrm = nrm_s;
     const bool zero = !(nrm >= 1e-14);
     if (zero) {
         if (blockIdx.x == 0 && threadIdx.x == 0 && zero_code != 0) ct_set_status(status, zero_code);
     }
-    const double inv = zero ? 0.0 : 1.0 / nrm;
+    const double r = block_reciprocal(zero ? 1.0 : nrm);
+    const double inv = zero ? 0.0 : r;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         y[i] = x[i] * inv;
 }
@@ -221,7 +236,7 @@ __global__ void __launch_bounds__(RT) lanczos_beta_finish(const double* partials
 __global__ void lanczos_next_kernel(int64_t n, const double* w, double* vnext, const double* scalars, int j,
                                     const int* skip) {
     if (ct_skip(skip)) return;
-    const double inv = 1.0 / scalars[SC_BETA + j];
+    const double inv = block_reciprocal(scalars[SC_BETA + j]);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         vnext[i] = w[i] * inv;
 }
@@ -660,7 +675,7 @@ __global__ void __launch_bounds__(RT) cgs_redo_update_kernel(int64_t n, double* 
 __global__ void lanczos_next32_kernel(int64_t n, const double* w, double* vnext, float* vnext32,
                                       const double* scalars, int j, const int* skip) {
     if (ct_skip(skip)) return;
-    const double inv = 1.0 / scalars[SC_BETA + j];
+    const double inv = block_reciprocal(scalars[SC_BETA + j]);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     if (aligned16(w) && aligned16(vnext) && ((uintptr_t)vnext32 & 7) == 0) {
         // 16-byte FP64 and 8-byte FP32 accesses; an odd last element by one thread
