@@ -532,14 +532,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 //     may access) and column group (w - 2) / 4 of the tile, holding BN / EPW
 //     FP32 running sums per thread.  EPW = 4 for the 128 x 128 tile (a chunk of
 //     64 of K is ~2000 cycles of MMAs there, so the per-chunk epilogue must be
-//     short), 2 for the 128 x 256 tile (its 128 sums per thread leave no room
-//     for more warps in the register file);
+//     short), 2 for the 128 x 192 / 224 / 256 tiles (their 96 to 128 sums per
+//     thread leave no room for more warps in the register file);
 //   * acc_full[b] is committed by the MMA thread after a chunk's last MMA,
 //     acc_empty[b] released by the epilogue warps once the chunk is in
 //     registers, so the MMAs of the next chunks run while chunk i is read (with
-//     four buffers the MMA thread is three chunks ahead, which hides the
-//     commit -> epilogue -> release latency of a short chunk); a tile's stores
-//     overlap the next tile's first chunks.
+//     four buffers -- two for the wide tiles -- the MMA thread is three chunks
+//     -- one -- ahead, which hides the commit -> epilogue -> release latency of a
+//     short chunk); a tile's stores overlap the next tile's first chunks;
+//   * with epi.trans the kernel's tile rows are C's columns: each thread stores
+//     its row's values down a column of C, so a warp store covers 32 consecutive
+//     words.
 __host__ __device__ constexpr int tc_chunk_epw(int BN) { return BN >= 192 ? 2 : 4; }
 // tcgen05.alloc takes a power of two (>= 32) of columns
 __host__ __device__ constexpr uint32_t tc_pow2_cols(int n) { return n <= 32 ? 32u : 2u * tc_pow2_cols((n + 1) / 2); }
